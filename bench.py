@@ -1,0 +1,378 @@
+#!/usr/bin/env python3
+"""Benchmark of the 7-point fp32 diffusion sweep at 512^3 on one GB300.
+
+Workload (the reference's diffusion benchmark, examples/diffusion-benchmark,
+at 512^3): f_new = cc*c + cw*w + ce*e + cs*s + cn*n + cb*b + ct*t with
+cc=0.4 and the six neighbour weights 0.1, neighbours clamped at the faces,
+double-buffered (two PSStencilMaps, g1->g2 and g2->g1).  One bench step is one
+time step: one sweep over all 512^3 cells.  Inputs: uniform[0,1) from the
+SplitMix64 stream, seed 1.
+
+Printed JSON line (one, rank 0):
+  value      GLUPS (giga lattice-site updates per second) with the grids
+             resident in HBM, timed with CUDA events on the runtime's stream;
+  e2e        the same metric for one whole job through the public C API with
+             host buffers: PSGridCopyin (pinned host -> device), PSStencilRun of
+             K steps, PSGridCopyout (device -> pinned host);
+  roofline   achieved HBM GB/s of the sweep kernel (8 algorithmic bytes per
+             cell update: one fp32 read, one fp32 write) against the measured
+             copy bandwidth in MEASURED_PEAKS.json;
+  cpu_baseline  the CPU restatement of the REF target (oracle/) on the host
+             cores, OpenMP over z, on a bounded sample of the same workload.
+
+--impl reference times only the CPU implementation (the reference's REF
+target restated in C, all host threads) on the same metric.
+Multi-GPU (torchrun): independent replicas, one per GPU (the path has no
+data exchange); value is the sum over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N = 512
+COEF = (0.1, 0.1, 0.1, 0.1, 0.1, 0.1, 0.4)  # ce cw cn cs ct cb cc
+BYTES_PER_LUP = 8
+METRIC = "GLUPS, 7-point fp32 diffusion 512^3 (clamped, double-buffered)"
+WORKLOAD = "7-point fp32 diffusion 512x512x512, clamped, cc=0.4 others 0.1"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max/sum over ranks (gloo on CPU tensors) for replicas."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def reduce(self, v, op):
+        if self.ws == 1:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.td.all_reduce(t, op=getattr(self.td.ReduceOp, op))
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """dram bytes per launch of the sweep kernel from the committed ncu
+    summary (profiles/diffusion7_512.md, line `traffic_bytes_per_launch:`)."""
+    p = os.path.join(ROOT, "profiles", "diffusion7_512.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (the oracle is the checker and the CPU baseline only)
+# ---------------------------------------------------------------------------
+
+def cpu_sweeps(seconds, nthreads=0, zslab=None):
+    """Times oracle sweeps of the 512^3 workload on host cores until about
+    `seconds` have elapsed.  With zslab, each sweep covers z in [0, zslab)
+    of the full grid (a bounded sample).  Returns (glups, sweeps, threads)."""
+    from oracle import pyoracle
+    from physis_gb300 import synth
+    nt = nthreads if nthreads > 0 else pyoracle.num_threads()
+    f1 = synth.uniform((N, N, N), 1)
+    f2 = np.zeros_like(f1)
+    zs = zslab or N
+    dom = (0, N, 0, N, 0, zs)
+    pyoracle.sweep7(pyoracle.V_DIFFUSION7, f1, f2, dom, COEF, nthreads=nt)
+    t0 = time.perf_counter()
+    sweeps = 0
+    while True:
+        pyoracle.sweep7(pyoracle.V_DIFFUSION7, f1, f2, dom, COEF, nthreads=nt)
+        f1, f2 = f2, f1
+        sweeps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return N * N * zs * sweeps / el / 1e9, sweeps, nt
+
+
+def run_reference(args, dist):
+    if dist.rank != 0:
+        return
+    from oracle import pyoracle
+    from physis_gb300 import synth
+    nt = pyoracle.num_threads()
+    zs = 32  # each step: one sweep over z in [0,32) of the 512^3 field
+    f1 = synth.uniform((N, N, N), 1)
+    f2 = np.zeros_like(f1)
+    dom = (0, N, 0, N, 0, zs)
+    for _ in range(args.warmup):
+        pyoracle.sweep7(pyoracle.V_DIFFUSION7, f1, f2, dom, COEF, nthreads=nt)
+        f1, f2 = f2, f1
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        pyoracle.sweep7(pyoracle.V_DIFFUSION7, f1, f2, dom, COEF, nthreads=nt)
+        f1, f2 = f2, f1
+    el = time.perf_counter() - t0
+    value = N * N * zs * args.steps / el / 1e9
+    sample = (f"one step = one REF-order sweep of z-slab [0,{zs}) of the 512^3 "
+              f"field ({N * N * zs} cells), OpenMP over z")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GLUPS",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic uniform[0,1) seed 1 (SplitMix64)",
+        "config": {"workload": WORKLOAD, "grid": [N, N, N],
+                   "implementation": "oracle/ps_oracle.c: C restatement of the "
+                   "Physis REF target (the reference's REF runtime needs Boost and "
+                   "its translator; neither builds here)"},
+        "cpu_baseline": {"value": value, "unit": "GLUPS", "cores": nt,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "GLUPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU leg
+# ---------------------------------------------------------------------------
+
+def run_gpu(args, dist):
+    os.environ.setdefault("PS_DEVICE", str(dist.local))
+    import physis_gb300 as ps
+    from physis_gb300 import synth
+    ps.init()
+    L = ps.lib()
+    shape = (N, N, N)
+    init = synth.uniform(shape, 1)
+    g1, g2 = ps.Grid(shape), ps.Grid(shape)
+    g1.copyin(init)
+    g2.copyin(init)
+    dom = ps.full_domain(shape)
+    if args.ty or args.ns or args.zchunk:
+        ps.set_launch_shape(ps.PS_KERNEL_DIFFUSION7, ty=args.ty, ns=args.ns,
+                            zchunk=args.zchunk)
+    m1 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g1, g2], COEF)
+    m2 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g2, g1], COEF)
+    K, W = args.steps, args.warmup
+
+    def steps(k):
+        # k single-map steps, alternating direction (PSStencilRun per map)
+        pairs, rem = divmod(k, 2)
+        if pairs:
+            ps.stencil_run([m1, m2], pairs)
+        if rem:
+            ps.stencil_run([m1], 1)
+
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    attempt = 0
+    while True:
+        steps(W)
+        ps.synchronize()
+        dist.barrier()
+        n0 = ps.launch_count()
+        L.PSEventRecord(0)
+        steps(K)
+        L.PSEventRecord(1)
+        ps.synchronize()
+        ms = L.PSEventElapsedMs(0, 1)
+        launches = ps.launch_count() - n0
+        dist.barrier()
+        clk = clocks.stop()
+        bad = {"hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown"}
+        if attempt == 0 and bad & set(clk.get("reasons", [])):
+            attempt += 1
+            clocks = ClockSampler(dist.local)
+            clocks.start()
+            continue
+        break
+    ps.check()
+    ms_max = dist.reduce(ms, "MAX")
+    cells = float(N) ** 3
+    value = dist.ws * cells * K / (ms_max / 1e3) / 1e9
+
+    # end to end through the public API with pinned host buffers
+    import ctypes
+    nbytes = N * N * N * 4
+    hin = L.PSHostAlloc(nbytes)
+    hout = L.PSHostAlloc(nbytes)
+    ctypes.memmove(hin, init.ctypes.data, nbytes)
+    dist.barrier()
+    t0 = time.perf_counter()
+    L.PSGridCopyin(g1.handle, hin)
+    steps(K)
+    L.PSGridCopyout(g1.handle if K % 2 == 0 else g2.handle, hout)
+    e2e_s = time.perf_counter() - t0
+    ps.check()
+    e2e_max = dist.reduce(e2e_s, "MAX")
+    e2e = dist.ws * cells * K / e2e_max / 1e9
+    L.PSHostFree(hin)
+    L.PSHostFree(hout)
+
+    peak, peak_kind = measured_peaks()
+    achieved = cells * BYTES_PER_LUP / (ms / K / 1e3) / 1e9
+    traffic = profiled_traffic()
+    shape_used = ps.get_launch_shape(ps.PS_KERNEL_DIFFUSION7)
+
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        glups, sweeps, nt = cpu_sweeps(args.cpu_seconds)
+        cpu = {"value": glups, "unit": "GLUPS", "cores": nt, "kind": "port",
+               "sample": f"{sweeps} REF-order sweeps of the full 512^3 field "
+                         f"(oracle/ps_oracle.c, OpenMP over z, "
+                         f"{args.cpu_seconds:.0f} s budget)"}
+    if dist.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "GLUPS",
+            "n_gpus": dist.ws, "steps": K, "warmup": W,
+            "ms_per_step": ms_max / K, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic uniform[0,1) seed 1 (SplitMix64)",
+            "config": {
+                "workload": WORKLOAD, "grid": [N, N, N],
+                "parallelism": f"replicas{dist.ws}" if dist.ws > 1 else "single-gpu",
+                "l2": "inputs larger than L2 (two 512 MiB grids vs 129 MB L2)",
+                "launch_shape": {"ty": shape_used[0], "ns": shape_used[1],
+                                 "zchunk": shape_used[2] or "auto"},
+                "e2e_job": "PSGridCopyin(pinned) + K steps + PSGridCopyout(pinned)",
+            },
+            "e2e": {"value": e2e, "unit": "GLUPS",
+                    "h2d_bytes_per_step": nbytes / K,
+                    "d2h_bytes_per_step": nbytes / K,
+                    "job_seconds": e2e_max},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "peak_source": peak_kind,
+                         "bytes_per_lup": BYTES_PER_LUP},
+            "hbm_gbs_achieved": achieved,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    g1.free()
+    g2.free()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ty", type=int, default=0)
+    ap.add_argument("--ns", type=int, default=0)
+    ap.add_argument("--zchunk", type=int, default=0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_gpu(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,142 @@
+/*
+ * physis_gb300.h -- additions to the Physis API exported by libphysis_gb300.so.
+ *
+ * 1. Non-variadic forms of the variadic Physis entry points, for foreign
+ *    function interfaces (ctypes, cgo, JNI) that cannot build C varargs
+ *    portably.  Each states the variadic call it is equivalent to.
+ * 2. Error reporting (the reference aborts instead; physis_common.h:144-146,
+ *    runtime_common_cuda.h:16-27).
+ * 3. Device-resident access, timing on the runtime's stream and launch
+ *    counting, used by benchmarks.
+ * 4. Launch-shape control and the autotuner.
+ * 5. Test hooks that exercise failure handling without faulting a GPU.
+ */
+#ifndef PHYSIS_GB300_EXT_H_
+#define PHYSIS_GB300_EXT_H_
+
+#include "physis_gb300/physis.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Every declaration below is exported from the shared library even when it
+ * is built with -fvisibility=hidden. */
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+/* ---- 1. Non-variadic entry points ------------------------------------- */
+
+/* PSInit(NULL, NULL, 3) with an explicit trace switch. */
+void PSInitV(int trace);
+
+/* PSGrid{N}D{Type}New for any type (PS_FLOAT, ...) and rank 1..3; dims[i]
+ * for i >= ndims are ignored.  Returns NULL on failure. */
+void *PSGridNewV(int type, int ndims, const PSIndex *dims);
+
+/* __PSStencilMap(kernel, *dom, grids[0..ngrids), scalars[0..nscalars)). */
+PSStencil PSStencilMapV(int kernel, const PSDomain3D *dom, int ngrids,
+                        void *const *grids, int nscalars,
+                        const double *scalars);
+
+/* PSStencilRun(stencils[0], ..., stencils[n-1], iter). */
+void PSStencilRunV(int n, const PSStencil *stencils, int iter);
+
+/* PSReduce(v, op, g). */
+void PSReduceGridV(void *v, int op, void *g);
+
+/* PSReduce(v, op, kernel, *dom, grids..., scalars...). */
+void PSReduceKernelV(void *v, int op, int kernel, const PSDomain3D *dom,
+                     int ngrids, void *const *grids, int nscalars,
+                     const double *scalars);
+
+/* Like PSReduceGridV but returns the FP64 combine of a float/double grid
+ * before it is rounded to the element type. */
+void PSReduceGridF64(double *v, int op, void *g);
+
+/* ---- 2. Errors -------------------------------------------------------- */
+
+enum PSErrorCode {
+  PS_OK = 0,
+  PS_ERR_NOT_INITIALIZED = 1,
+  PS_ERR_INVALID_ARGUMENT = 2,
+  PS_ERR_OUT_OF_MEMORY = 3,
+  PS_ERR_CUDA = 4,
+  PS_ERR_UNKNOWN_KERNEL = 5,
+  PS_ERR_BAD_HANDLE = 6,
+  PS_ERR_UNSUPPORTED = 7,
+  PS_ERR_DEVICE_TIMEOUT = 8,
+  PS_ERR_NO_DEVICE = 9,
+  PS_ERR_IO = 10
+};
+/* First error recorded since the last PSClearError (sticky). */
+int PSGetLastError(void);
+const char *PSGetLastErrorString(void);
+const char *PSGetErrorName(int code);
+void PSClearError(void);
+
+/* ---- 3. Device access, timing, counters ------------------------------- */
+
+/* Device address, row pitch in bytes (a multiple of 128) and element size of
+ * a grid.  Element (x,y,z) is at ptr + (z*ny + y)*pitch + x*esz. */
+void *PSGridDevicePtr(void *g);
+size_t PSGridPitch(void *g);
+int PSGridElemSize(void *g);
+int PSGridType(void *g);
+/* Copies a dense host buffer in/out without synchronising (the runtime's
+ * stream orders it with kernels); host memory must stay valid until
+ * PSSynchronize.  Pinned host memory gives DMA at full link speed. */
+void PSGridCopyinAsync(void *g, const void *src);
+void PSGridCopyoutAsync(void *g, void *dst);
+/* Page-locked host allocation for the async copies. */
+void *PSHostAlloc(size_t bytes);
+void PSHostFree(void *p);
+/* Waits for all work on the runtime's stream; checks the device error word
+ * (a device-side bounded wait that gave up sets PS_ERR_DEVICE_TIMEOUT). */
+void PSSynchronize(void);
+/* The runtime's CUDA stream (a cudaStream_t). */
+void *PSGetStream(void);
+/* CUDA events on the runtime's stream: PSEventRecord(slot) records event
+ * `slot` (0..63); PSEventElapsedMs(a, b) returns ms from a to b after
+ * waiting for b. */
+void PSEventRecord(int slot);
+float PSEventElapsedMs(int a, int b);
+/* Number of kernels this library launched since PSInit. */
+long long PSGetLaunchCount(void);
+/* Number of streaming multiprocessors of the runtime's device. */
+int PSGetSMCount(void);
+
+/* ---- 4. Launch shapes and the autotuner -------------------------------- */
+
+/* Launch shape of a z-marching sweep: ty warp-rows per CTA (tile height),
+ * ns ring stages, zchunk planes per CTA, ns2 second-ring stages (Himeno
+ * coefficient planes).  A value <= 0 keeps the current setting. */
+typedef struct {
+  int ty;
+  int ns;
+  int zchunk;
+  int ns2;
+} PSLaunchShape;
+/* Sets the shape used for maps of `kernel` from now on (0 = all kernels). */
+void PSSetLaunchShape(int kernel, const PSLaunchShape *shape);
+void PSGetLaunchShape(int kernel, PSLaunchShape *shape);
+
+/* ---- 5. Test hooks ------------------------------------------------------ */
+
+/* The next `n` device allocations fail as if the GPU were out of memory. */
+void PSTestFailNextAllocs(int n);
+/* Launches one CTA that waits on an mbarrier nothing completes, with a
+ * bounded wait of `limit` tries; afterwards PSSynchronize reports
+ * PS_ERR_DEVICE_TIMEOUT and the context stays usable. */
+void PSTestDeviceWaitTimeout(unsigned limit);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PHYSIS_GB300_EXT_H_ */

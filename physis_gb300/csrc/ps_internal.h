@@ -1,0 +1,106 @@
+// Internal interface between the host runtime (runtime.cpp) and the kernel
+// translation units.  Plain structs only; nothing here is exported.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace psg {
+
+// PSPrimitiveType values (include/physis/types.h:16-23 in the reference).
+enum ElemType { kInt = 0, kLong = 1, kFloat = 2, kDouble = 3 };
+// PSReduceOp values (include/physis/reduce.h:16-21 in the reference).
+enum ReduceOp { kMax = 0, kMin = 1, kSum = 2, kProd = 3 };
+
+// Builtin stencil kernel ids (the values of PS_KERNEL_* in
+// include/physis_gb300/physis.h).
+enum BuiltinKernel {
+  kKernelCopy = 1,
+  kKernelDiffusion7 = 2,
+  kKernelHimeno19 = 3,
+  kKernelHimeno19Gosa = 4,
+  kKernelSum7 = 5,
+  kKernelSum7Periodic = 6,
+};
+
+// Device view of one pitched grid: element (x,y,z) lives at
+// ptr + z*pitch*ny + y*pitch + x*esz.  pitch is a multiple of 128 bytes and
+// ptr is 256-byte aligned.
+struct GridView {
+  void *ptr;
+  int64_t pitch;  // bytes per x-row
+  int nx, ny, nz;
+  int type;       // ElemType
+  int esz;        // element size in bytes
+};
+
+// Half-open box [min, max) per dimension (x, y, z).
+struct Box {
+  int min[3];
+  int max[3];
+};
+
+// Launch shape of a 2.5D z-marching stencil kernel: `ty` warp-rows per CTA
+// (the tile is 16 bytes x 32 lanes wide in x), `ns` shared-memory ring
+// stages, `zchunk` planes marched per CTA.
+struct MarchConfig {
+  int ty;
+  int ns;
+  int zchunk;
+  int ns2;  // second ring (coefficient planes) where a kernel has one
+};
+
+// Builds a 3D tiled tensor map over g with box {box_w, box_h, 1} elements.
+// Implemented in runtime.cpp (driver entry point looked up at run time).
+bool make_tmap_3d(CUtensorMap *map, const GridView &g, int box_w, int box_h);
+
+// ---- 7-point family (stencil7.cu) ---------------------------------------
+struct Stencil7Args {
+  int kernel;  // kKernelDiffusion7 / kKernelSum7 / kKernelCopy
+  GridView in, out;
+  Box dom;
+  double coef[7];  // map argument order: ce cw cn cs ct cb cc
+};
+// Number of bytes of dynamic shared memory the launch will use.
+size_t stencil7_smem_bytes(int esz, const MarchConfig &cfg);
+cudaError_t launch_stencil7(const Stencil7Args &a, const MarchConfig &cfg,
+                            const CUtensorMap *tin, int *dev_err,
+                            cudaStream_t s);
+
+// ---- Himeno 19-point Jacobi (himeno19.cu) --------------------------------
+struct Himeno19Args {
+  GridView g[14];  // p0 p1 a0 a1 a2 a3 b0 b1 b2 c0 c1 c2 bnd wrk1
+  Box dom;
+  float omega;
+  bool gosa;       // fused residual sum of ss*ss
+};
+struct ResidualSink {
+  double *partials;     // one FP64 partial per CTA
+  int max_partials;
+  unsigned *ticket;     // last-CTA-done counter (kept at 0 between launches)
+  double *result;       // where the FP64 total goes
+};
+size_t himeno19_smem_bytes(const MarchConfig &cfg);
+int himeno19_num_ctas(const Himeno19Args &a, const MarchConfig &cfg);
+cudaError_t launch_himeno19(const Himeno19Args &a, const MarchConfig &cfg,
+                            const CUtensorMap *tmaps /* 13: p0-halo, 12 coef */,
+                            const ResidualSink &sink, int *dev_err,
+                            cudaStream_t s);
+
+// ---- Reductions (reduce.cu) ----------------------------------------------
+// Reduces every element of g with op.  The 8-byte result is written to
+// *result: FP64 for float and double grids, int64 for int (wrapped to 32
+// bits) and long grids.  partials holds one 8-byte slot per CTA.
+int reduce_num_ctas(const GridView &g, int sm_count);
+cudaError_t launch_reduce(const GridView &g, int op, uint64_t *partials,
+                          int num_ctas, unsigned *ticket, uint64_t *result,
+                          int *dev_err, cudaStream_t s);
+
+// ---- Test support (failure detection without a GPU fault) ----------------
+// Runs one CTA that waits on an mbarrier that nothing completes, with a
+// short iteration limit; the wait gives up and sets kDevErrWaitTimeout.
+cudaError_t launch_wait_timeout_probe(int *dev_err, uint32_t limit,
+                                      cudaStream_t s);
+
+}  // namespace psg

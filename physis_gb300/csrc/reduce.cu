@@ -1,0 +1,264 @@
+// PSReduce over a whole pitched grid on GB300 (sm_103a).
+//
+// Replaces the reference's Thrust call (runtime/reduce_cuda.h:19-40,
+// runtime/reduce_cuda.cu:14-40) and plays the role of its CUB block reduce
+// (runtime/reduce_grid_mpi_cuda_exp.cu:177-330).  Semantics follow the REF
+// target: every element of the grid, operators max/min/sum/prod
+// (runtime/reduce.h:14-49).
+//
+// One pass: warps stride over x-rows; lanes read 16-byte vectors (a warp
+// reads 512 contiguous bytes per step) and accumulate in the element type
+// (FP32 for float grids; a float PS_PROD accumulates in FP64, because a long
+// FP32 product loses about sqrt(n) ulps whatever the order), then warp
+// shuffles and a shared-memory tree give one partial per CTA.  Partials are stored as 8-byte values (FP64 for
+// float/double grids, 64-bit integers for int/long grids) and the last CTA to
+// finish (atomic ticket) combines them in a fixed order: FP64 for floating
+// grids, wrapping integer arithmetic for integer grids (the REF fold wraps the
+// same way).  The result is deterministic run to run.
+#include <type_traits>
+
+#include "ps_device.cuh"
+#include "ps_internal.h"
+
+namespace psg {
+namespace {
+
+constexpr int kReduceThreads = 256;
+
+template <typename T> struct RTraits;
+template <> struct RTraits<float> {
+  typedef float Acc;      // per-thread / per-CTA accumulation
+  typedef double Comb;    // final combine
+};
+template <> struct RTraits<double> {
+  typedef double Acc;
+  typedef double Comb;
+};
+template <> struct RTraits<int> {
+  typedef unsigned Acc;   // wraps modulo 2^32 for sum/prod
+  typedef unsigned Comb;
+};
+template <> struct RTraits<long long> {
+  typedef unsigned long long Acc;
+  typedef unsigned long long Comb;
+};
+
+template <typename T, typename A>
+__device__ __forceinline__ A identity(int op) {
+  switch (op) {
+    case kSum: return (A)0;
+    case kProd: return (A)1;
+  }
+  return (A)0;  // min/max start from the first element seen (see below)
+}
+
+// Combine for floating accumulators (min/max by value).
+template <typename A>
+__device__ __forceinline__ A combine_f(int op, A a, A b) {
+  switch (op) {
+    case kMax: return (a > b) ? a : b;
+    case kMin: return (a < b) ? a : b;
+    case kSum: return RN<A>::add(a, b);
+    default: return RN<A>::mul(a, b);
+  }
+}
+
+// Integers: min/max compare as signed T, sum/prod wrap in unsigned A.
+template <typename T, typename A>
+__device__ __forceinline__ A combine_i(int op, A a, A b) {
+  switch (op) {
+    case kMax: return ((T)a > (T)b) ? a : b;
+    case kMin: return ((T)a < (T)b) ? a : b;
+    case kSum: return a + b;
+    default: return a * b;
+  }
+}
+
+template <typename T, typename A>
+__device__ __forceinline__ A combine(int op, A a, A b) {
+  if constexpr (std::is_integral<T>::value) {
+    return combine_i<T, A>(op, a, b);
+  } else {
+    return combine_f<A>(op, a, b);
+  }
+}
+
+// Integers keep their bit pattern in the unsigned accumulator.
+template <typename T, typename A>
+__device__ __forceinline__ A to_acc(T v) { return (A)v; }
+
+template <typename A>
+__device__ __forceinline__ A shfl_x(A v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+
+template <typename T, typename A, typename C>
+__global__ void __launch_bounds__(kReduceThreads)
+reduce_kernel(const char *__restrict__ base, int64_t pitch, int nx, int ny, int nz,
+              int op, uint64_t *partials, unsigned *ticket, uint64_t *result) {
+  constexpr int VEC = 16 / (int)sizeof(T);
+  __shared__ A red[kReduceThreads / 32];
+  __shared__ bool red_has[kReduceThreads / 32];
+  __shared__ int last_cta;
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t rows = (int64_t)ny * nz;
+  const int64_t gw = (int64_t)blockIdx.x * (kReduceThreads / 32) + warp;
+  const int64_t nw = (int64_t)gridDim.x * (kReduceThreads / 32);
+  const int nvec = nx / VEC;
+  const int tail = nx - nvec * VEC;
+
+  // min/max have no identity that is exact for every type; track whether
+  // this thread has seen an element instead.
+  A acc = identity<T, A>(op);
+  bool has = false;
+  for (int64_t r = gw; r < rows; r += nw) {
+    const char *rp = base + (r / ny) * pitch * ny + (r % ny) * pitch;
+    const uint4 *vp = reinterpret_cast<const uint4 *>(rp);
+#pragma unroll 4
+    for (int v = lane; v < nvec; v += 32) {
+      union { uint4 u; T t[VEC]; } cvt;
+      cvt.u = __ldcs(vp + v);
+#pragma unroll
+      for (int i = 0; i < VEC; ++i) {
+        const A e = to_acc<T, A>(cvt.t[i]);
+        acc = has ? combine<T, A>(op, acc, e)
+                  : ((op == kSum || op == kProd) ? combine<T, A>(op, acc, e) : e);
+        has = true;
+      }
+    }
+    if (lane < tail) {
+      const A e = to_acc<T, A>(reinterpret_cast<const T *>(rp)[nvec * VEC + lane]);
+      acc = has ? combine<T, A>(op, acc, e)
+                : ((op == kSum || op == kProd) ? combine<T, A>(op, acc, e) : e);
+      has = true;
+    }
+  }
+  // warp tree
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const A other = shfl_x(acc, o);
+    const bool ohas = __shfl_xor_sync(0xffffffffu, (int)has, o) != 0;
+    if (ohas) acc = has ? combine<T, A>(op, acc, other) : other;
+    has = has || ohas;
+  }
+  if (lane == 0) {
+    red[warp] = acc;
+    red_has[warp] = has;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    A b = identity<T, A>(op);
+    bool bh = false;
+    for (int w = 0; w < kReduceThreads / 32; ++w) {
+      if (!red_has[w]) continue;
+      b = bh ? combine<T, A>(op, b, red[w]) : red[w];
+      bh = true;
+    }
+    // Partial as an 8-byte slot; an empty CTA stores the op's identity
+    // (only possible for sum/prod shapes, min/max CTAs always see data
+    // because the host sizes the grid to the row count).
+    C cb = bh ? (C)b : (C)identity<T, A>(op);
+    uint64_t bits = 0;
+    if constexpr (sizeof(C) == 8) {
+      bits = *reinterpret_cast<uint64_t *>(&cb);
+    } else {
+      bits = (uint64_t)(uint32_t)cb;
+    }
+    partials[blockIdx.x] = bits;
+    __threadfence();
+    const unsigned prev = atomicAdd(ticket, 1u);
+    last_cta = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last_cta && warp == 0) {
+    __threadfence();
+    C v = (C)identity<T, A>(op);
+    bool vh = false;
+    for (unsigned i = lane; i < gridDim.x; i += 32) {
+      const uint64_t bits = __ldcg(reinterpret_cast<const unsigned long long *>(partials) + i);
+      C e;
+      if constexpr (sizeof(C) == 8) {
+        e = *reinterpret_cast<const C *>(&bits);
+      } else {
+        e = (C)(uint32_t)bits;
+      }
+      v = vh ? combine<T, C>(op, v, e) : e;
+      vh = true;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const C other = shfl_x(v, o);
+      const bool oh = __shfl_xor_sync(0xffffffffu, (int)vh, o) != 0;
+      if (oh) v = vh ? combine<T, C>(op, v, other) : other;
+      vh = vh || oh;
+    }
+    if (lane == 0) {
+      uint64_t bits;
+      if constexpr (sizeof(C) == 8) {
+        bits = *reinterpret_cast<uint64_t *>(&v);
+      } else {
+        bits = (uint64_t)(int64_t)(int32_t)v;  // int grids: sign-extend
+      }
+      *result = bits;
+      *ticket = 0u;
+    }
+  }
+}
+
+// One CTA waiting on an mbarrier that nothing arrives at: the bounded wait
+// gives up after `limit` tries and records kDevErrWaitTimeout.
+__global__ void wait_timeout_probe_kernel(int *err, uint32_t limit) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) mbar_wait(&bar, 0, err, limit);
+}
+
+template <typename T, typename A = typename RTraits<T>::Acc,
+          typename C = typename RTraits<T>::Comb>
+cudaError_t launch_t(const GridView &g, int op, uint64_t *partials, int num_ctas,
+                     unsigned *ticket, uint64_t *result, cudaStream_t s) {
+  reduce_kernel<T, A, C><<<num_ctas, kReduceThreads, 0, s>>>(
+      static_cast<const char *>(g.ptr), g.pitch, g.nx, g.ny, g.nz, op, partials,
+      ticket, result);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+int reduce_num_ctas(const GridView &g, int sm_count) {
+  const int64_t rows = (int64_t)g.ny * g.nz;
+  const int64_t warps = kReduceThreads / 32;
+  int64_t n = (rows + warps - 1) / warps;
+  const int64_t cap = (int64_t)sm_count * 8;
+  if (n > cap) n = cap;
+  if (n < 1) n = 1;
+  return (int)n;
+}
+
+cudaError_t launch_reduce(const GridView &g, int op, uint64_t *partials,
+                          int num_ctas, unsigned *ticket, uint64_t *result,
+                          int *dev_err, cudaStream_t s) {
+  (void)dev_err;
+  if (op < kMax || op > kProd) return cudaErrorInvalidValue;
+  switch (g.type) {
+    case kFloat:
+      if (op == kProd)
+        return launch_t<float, double, double>(g, op, partials, num_ctas, ticket, result, s);
+      return launch_t<float>(g, op, partials, num_ctas, ticket, result, s);
+    case kDouble: return launch_t<double>(g, op, partials, num_ctas, ticket, result, s);
+    case kInt: return launch_t<int>(g, op, partials, num_ctas, ticket, result, s);
+    case kLong: return launch_t<long long>(g, op, partials, num_ctas, ticket, result, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_wait_timeout_probe(int *dev_err, uint32_t limit,
+                                      cudaStream_t s) {
+  wait_timeout_probe_kernel<<<1, 32, 0, s>>>(dev_err, limit);
+  return cudaGetLastError();
+}
+
+}  // namespace psg

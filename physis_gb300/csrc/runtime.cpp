@@ -1,0 +1,1038 @@
+// Host runtime of libphysis_gb300.so: the PS* C ABI over device-resident
+// pitched grids, builtin stencil maps and the launchers in stencil7.cu,
+// himeno19.cu and reduce.cu.
+//
+// Replaces, for one GPU, the reference's CUDA runtime library
+// (runtime/libphysis_rt_cuda.cc) and the per-program code its translator
+// generates for PSStencilMap / PSStencilRun (translator/
+// reference_runtime_builder.cc:391-541, 837-894; cuda_runtime_builder.cc:
+// 1465-1583).  Differences by design:
+//  * grids are pitched: every x-row starts on a 128-byte boundary (the
+//    reference allocates dense rows, libphysis_rt_cuda.cc:48-99), so TMA boxes
+//    and 16-byte vector accesses are always aligned;
+//  * all work goes to one runtime-owned stream; PSGridCopyin/Copyout and
+//    PSReduce wait for it, like the reference's blocking cudaMemcpy;
+//  * errors are recorded (sticky) instead of exiting the process.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <unordered_set>
+#include <vector>
+
+#include "physis_gb300/physis_gb300.h"
+#undef PSStencilRun
+#include "ps_internal.h"
+
+using psg::GridView;
+using psg::MarchConfig;
+
+namespace {
+
+constexpr uint32_t kGridMagic = 0x50534744u;  // "PSGD"
+constexpr int kStencilTag = 0x5A000000;       // PSStencil = tag | map index
+constexpr int kStencilTagMask = 0x7F000000;
+constexpr int kMaxMaps = 1 << 24;
+constexpr int kNumEvents = 64;
+constexpr int kMaxPartials = 1 << 16;
+constexpr int kNumKernels = 8;
+
+struct TmapEntry {
+  void *ptr;
+  int w, h;
+  CUtensorMap map;
+};
+
+struct Grid {
+  uint32_t magic;
+  int type, esz, ndims;
+  int dim[3];
+  size_t pitch, bytes;
+  void *dev;
+  std::vector<TmapEntry> tmaps;
+};
+
+struct Map {
+  int kernel;
+  __PSDomain dom;
+  std::vector<Grid *> grids;
+  std::vector<double> scalars;
+};
+
+struct Runtime {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int sm_count = 0;
+  bool trace = false;
+  int *dev_err = nullptr;
+  uint64_t *partials = nullptr;
+  unsigned *ticket = nullptr;
+  uint64_t *results = nullptr;  // slot 0: reductions, slot 1: residuals
+  cudaEvent_t events[kNumEvents] = {};
+  long long launches = 0;
+  std::vector<Map> maps;
+  std::unordered_set<Grid *> grids;
+  MarchConfig shapes[kNumKernels];
+  int fail_allocs = 0;
+};
+
+Runtime *rt = nullptr;
+int g_err = PS_OK;
+std::string g_errmsg;
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t,
+                                  void *, const cuuint64_t *, const cuuint64_t *,
+                                  const cuuint32_t *, const cuuint32_t *,
+                                  CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn g_encode = nullptr;
+
+const char *err_name(int code) {
+  switch (code) {
+    case PS_OK: return "PS_OK";
+    case PS_ERR_NOT_INITIALIZED: return "PS_ERR_NOT_INITIALIZED";
+    case PS_ERR_INVALID_ARGUMENT: return "PS_ERR_INVALID_ARGUMENT";
+    case PS_ERR_OUT_OF_MEMORY: return "PS_ERR_OUT_OF_MEMORY";
+    case PS_ERR_CUDA: return "PS_ERR_CUDA";
+    case PS_ERR_UNKNOWN_KERNEL: return "PS_ERR_UNKNOWN_KERNEL";
+    case PS_ERR_BAD_HANDLE: return "PS_ERR_BAD_HANDLE";
+    case PS_ERR_UNSUPPORTED: return "PS_ERR_UNSUPPORTED";
+    case PS_ERR_DEVICE_TIMEOUT: return "PS_ERR_DEVICE_TIMEOUT";
+    case PS_ERR_NO_DEVICE: return "PS_ERR_NO_DEVICE";
+    case PS_ERR_IO: return "PS_ERR_IO";
+  }
+  return "PS_ERR_UNKNOWN";
+}
+
+bool abort_on_error() {
+  const char *e = getenv("PS_ABORT_ON_ERROR");
+  return e && e[0] == '1';
+}
+
+// Records the first error since the last PSClearError; always returns false
+// so call sites can `return fail(...)`.
+bool fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list vl;
+  va_start(vl, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, vl);
+  va_end(vl);
+  if (g_err == PS_OK) {
+    g_err = code;
+    g_errmsg = std::string(err_name(code)) + ": " + buf;
+  }
+  if (abort_on_error()) {
+    fprintf(stderr, "physis_gb300: %s: %s\n", err_name(code), buf);
+    abort();
+  }
+  return false;
+}
+
+bool cuda_ok(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return true;
+  if (e == cudaErrorMemoryAllocation)
+    return fail(PS_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+  return fail(PS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+bool need_rt(const char *fn) {
+  if (rt) return true;
+  return fail(PS_ERR_NOT_INITIALIZED, "%s called before PSInit", fn);
+}
+
+Grid *as_grid(void *g, const char *fn) {
+  Grid *p = static_cast<Grid *>(g);
+  if (!rt) {
+    fail(PS_ERR_NOT_INITIALIZED, "%s called before PSInit", fn);
+    return nullptr;
+  }
+  if (!p || !rt->grids.count(p) || p->magic != kGridMagic) {
+    fail(PS_ERR_BAD_HANDLE, "%s: %p is not a live grid", fn, g);
+    return nullptr;
+  }
+  return p;
+}
+
+int esize(int type) {
+  switch (type) {
+    case PS_INT: return 4;
+    case PS_LONG: return 8;
+    case PS_FLOAT: return 4;
+    case PS_DOUBLE: return 8;
+  }
+  return 0;
+}
+
+GridView view(const Grid *g) {
+  GridView v;
+  v.ptr = g->dev;
+  v.pitch = (int64_t)g->pitch;
+  v.nx = g->dim[0];
+  v.ny = g->dim[1];
+  v.nz = g->dim[2];
+  v.type = g->type;
+  v.esz = g->esz;
+  return v;
+}
+
+// Checks the device error word; a device-side wait that gave up leaves a
+// non-zero value.  Also re-arms the reduction ticket, which an interrupted
+// reduction may have left non-zero.
+bool check_device_errors() {
+  int h = 0;
+  if (!cuda_ok(cudaMemcpyAsync(&h, rt->dev_err, sizeof(int), cudaMemcpyDeviceToHost,
+                               rt->stream), "read device error word"))
+    return false;
+  if (!cuda_ok(cudaStreamSynchronize(rt->stream), "cudaStreamSynchronize")) return false;
+  if (h != 0) {
+    cudaMemsetAsync(rt->dev_err, 0, sizeof(int), rt->stream);
+    cudaMemsetAsync(rt->ticket, 0, sizeof(unsigned), rt->stream);
+    cudaStreamSynchronize(rt->stream);
+    return fail(PS_ERR_DEVICE_TIMEOUT,
+                "a device-side wait gave up (error bits 0x%x); results of the "
+                "affected launch are invalid", h);
+  }
+  return true;
+}
+
+bool sync_rt() {
+  cudaError_t e = cudaStreamSynchronize(rt->stream);
+  if (!cuda_ok(e, "cudaStreamSynchronize")) return false;
+  return check_device_errors();
+}
+
+const CUtensorMap *tmap_for(Grid *g, int w, int h) {
+  for (auto &e : g->tmaps)
+    if (e.ptr == g->dev && e.w == w && e.h == h) return &e.map;
+  TmapEntry e;
+  e.ptr = g->dev;
+  e.w = w;
+  e.h = h;
+  if (!psg::make_tmap_3d(&e.map, view(g), w, h)) return nullptr;
+  g->tmaps.push_back(e);
+  return &g->tmaps.back().map;
+}
+
+struct KernelSig {
+  int ngrids, nscalars;
+  const char *name;
+};
+
+bool kernel_sig(int k, KernelSig *s) {
+  switch (k) {
+    case PS_KERNEL_COPY: *s = {2, 0, "PS_KERNEL_COPY"}; return true;
+    case PS_KERNEL_DIFFUSION7: *s = {2, 7, "PS_KERNEL_DIFFUSION7"}; return true;
+    case PS_KERNEL_HIMENO19: *s = {14, 1, "PS_KERNEL_HIMENO19"}; return true;
+    case PS_KERNEL_HIMENO19_GOSA: *s = {14, 1, "PS_KERNEL_HIMENO19_GOSA"}; return true;
+    case PS_KERNEL_SUM7: *s = {2, 0, "PS_KERNEL_SUM7"}; return true;
+  }
+  return false;
+}
+
+// Validates a map's grids, scalars and domain against its builtin.
+bool validate_map(const Map &m) {
+  KernelSig sig;
+  if (!kernel_sig(m.kernel, &sig))
+    return fail(PS_ERR_UNKNOWN_KERNEL, "unknown builtin stencil id %d", m.kernel);
+  const Grid *g0 = m.grids[0];
+  for (const Grid *g : m.grids) {
+    if (g->type != g0->type || g->dim[0] != g0->dim[0] || g->dim[1] != g0->dim[1] ||
+        g->dim[2] != g0->dim[2])
+      return fail(PS_ERR_INVALID_ARGUMENT,
+                  "%s: all grids of a map must have the same type and size", sig.name);
+  }
+  if (m.grids[0] == m.grids[1])
+    return fail(PS_ERR_INVALID_ARGUMENT, "%s: input and output grid are the same",
+                sig.name);
+  const bool is_float = g0->type == PS_FLOAT, is_fp = is_float || g0->type == PS_DOUBLE;
+  if ((m.kernel == PS_KERNEL_DIFFUSION7 && !is_fp) ||
+      ((m.kernel == PS_KERNEL_HIMENO19 || m.kernel == PS_KERNEL_HIMENO19_GOSA) && !is_float))
+    return fail(PS_ERR_UNSUPPORTED, "%s: unsupported element type %d", sig.name, g0->type);
+  const bool interior = (m.kernel == PS_KERNEL_SUM7 || m.kernel == PS_KERNEL_HIMENO19 ||
+                         m.kernel == PS_KERNEL_HIMENO19_GOSA);
+  for (int d = 0; d < 3; ++d) {
+    const int lo = m.dom.min[d], hi = m.dom.max[d], n = g0->dim[d];
+    if (lo < 0 || hi > n || lo > hi)
+      return fail(PS_ERR_INVALID_ARGUMENT,
+                  "%s: domain [%d,%d) in dim %d outside grid of size %d", sig.name, lo,
+                  hi, d, n);
+    if (interior && lo < hi && (lo < 1 || hi > n - 1))
+      return fail(PS_ERR_INVALID_ARGUMENT,
+                  "%s reads neighbours without clamping: its domain [%d,%d) in dim %d "
+                  "must stay inside [1,%d)", sig.name, lo, hi, d, n - 1);
+  }
+  return true;
+}
+
+int shape_slot(int kernel) { return (kernel > 0 && kernel < kNumKernels) ? kernel : 0; }
+
+// Fills in an automatic zchunk: enough CTAs for ~8 per SM.
+MarchConfig resolve_shape(int kernel, int xy_tiles, int nzdom) {
+  MarchConfig c = rt->shapes[shape_slot(kernel)];
+  if (c.zchunk <= 0) {
+    const int target = rt->sm_count * 8;
+    int zsplit = (target + xy_tiles - 1) / (xy_tiles > 0 ? xy_tiles : 1);
+    if (zsplit < 1) zsplit = 1;
+    int zc = (nzdom + zsplit - 1) / zsplit;
+    if (zc < 16) zc = 16;
+    c.zchunk = zc;
+  }
+  const int min_chunk = (nzdom + 65534) / 65535;  // grid.z limit
+  if (c.zchunk < min_chunk) c.zchunk = min_chunk;
+  return c;
+}
+
+bool launch_map(const Map &m, bool want_gosa) {
+  const Grid *g0 = m.grids[0];
+  psg::Box box;
+  for (int d = 0; d < 3; ++d) {
+    box.min[d] = m.dom.min[d];
+    box.max[d] = m.dom.max[d];
+  }
+  if (box.min[0] >= box.max[0] || box.min[1] >= box.max[1] || box.min[2] >= box.max[2])
+    return true;  // empty domain: nothing to do, as in the REF loops
+  cudaError_t e;
+  if (m.kernel == PS_KERNEL_HIMENO19 || m.kernel == PS_KERNEL_HIMENO19_GOSA) {
+    psg::Himeno19Args a;
+    for (int i = 0; i < 14; ++i) a.g[i] = view(m.grids[i]);
+    a.dom = box;
+    a.omega = (float)m.scalars[0];
+    a.gosa = want_gosa;
+    const int xbase = (box.min[0] / 4) * 4;
+    const int tiles_x = (box.max[0] - xbase + 127) / 128;
+    MarchConfig probe = rt->shapes[shape_slot(m.kernel)];
+    const int tiles_y = (box.max[1] - box.min[1] + probe.ty - 1) / probe.ty;
+    MarchConfig cfg = resolve_shape(m.kernel, tiles_x * tiles_y, box.max[2] - box.min[2]);
+    if (want_gosa) {
+      while (psg::himeno19_num_ctas(a, cfg) > kMaxPartials) cfg.zchunk *= 2;
+    }
+    CUtensorMap maps[13];
+    const CUtensorMap *t = tmap_for(m.grids[0], 136, cfg.ty + 2);
+    if (!t) return false;
+    maps[0] = *t;
+    for (int i = 0; i < 12; ++i) {
+      t = tmap_for(m.grids[2 + i], 128, cfg.ty);
+      if (!t) return false;
+      maps[1 + i] = *t;
+    }
+    psg::ResidualSink sink;
+    sink.partials = reinterpret_cast<double *>(rt->partials);
+    sink.max_partials = kMaxPartials;
+    sink.ticket = rt->ticket;
+    sink.result = reinterpret_cast<double *>(rt->results + 1);
+    e = psg::launch_himeno19(a, cfg, maps, sink, rt->dev_err, rt->stream);
+    if (!cuda_ok(e, "himeno19 launch")) return false;
+    ++rt->launches;
+    return true;
+  }
+  psg::Stencil7Args a;
+  a.kernel = m.kernel;
+  a.in = view(m.grids[0]);
+  a.out = view(m.grids[1]);
+  a.dom = box;
+  for (int i = 0; i < 7; ++i) a.coef[i] = i < (int)m.scalars.size() ? m.scalars[i] : 0.0;
+  const int vec = 16 / g0->esz;
+  const int tx = 32 * vec;
+  const int xbase = (box.min[0] / vec) * vec;
+  const int tiles_x = (box.max[0] - xbase + tx - 1) / tx;
+  MarchConfig probe = rt->shapes[shape_slot(m.kernel)];
+  const int tiles_y = (box.max[1] - box.min[1] + probe.ty - 1) / probe.ty;
+  MarchConfig cfg = resolve_shape(m.kernel, tiles_x * tiles_y, box.max[2] - box.min[2]);
+  const CUtensorMap *t = tmap_for(m.grids[0], tx + 2 * vec, cfg.ty + 2);
+  if (!t) return false;
+  e = psg::launch_stencil7(a, cfg, t, rt->dev_err, rt->stream);
+  if (!cuda_ok(e, "stencil7 launch")) return false;
+  ++rt->launches;
+  return true;
+}
+
+void *grid_new(int type, int ndims, const PSIndex *dims) {
+  if (!need_rt("PSGrid*New")) return nullptr;
+  const int esz = esize(type);
+  if (!esz) {
+    fail(PS_ERR_INVALID_ARGUMENT, "unknown grid element type %d", type);
+    return nullptr;
+  }
+  if (ndims < 1 || ndims > 3) {
+    fail(PS_ERR_INVALID_ARGUMENT, "grid rank %d not in 1..3", ndims);
+    return nullptr;
+  }
+  int dim[3] = {1, 1, 1};
+  for (int d = 0; d < ndims; ++d) {
+    if (dims[d] <= 0) {
+      fail(PS_ERR_INVALID_ARGUMENT, "grid size %d in dim %d must be positive", dims[d], d);
+      return nullptr;
+    }
+    dim[d] = dims[d];
+  }
+  const size_t pitch = (((size_t)dim[0] * esz) + 127) / 128 * 128;
+  const size_t bytes = pitch * (size_t)dim[1] * (size_t)dim[2];
+  void *dev = nullptr;
+  if (rt->fail_allocs > 0) {
+    --rt->fail_allocs;
+    fail(PS_ERR_OUT_OF_MEMORY, "device allocation of %zu bytes failed (test hook)", bytes);
+    return nullptr;
+  }
+  if (!cuda_ok(cudaMalloc(&dev, bytes), "cudaMalloc")) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (!cuda_ok(cudaMemsetAsync(dev, 0, bytes, rt->stream), "cudaMemsetAsync") ||
+      !cuda_ok(cudaStreamSynchronize(rt->stream), "cudaStreamSynchronize")) {
+    cudaFree(dev);
+    return nullptr;
+  }
+  Grid *g = new Grid();
+  g->magic = kGridMagic;
+  g->type = type;
+  g->esz = esz;
+  g->ndims = ndims;
+  for (int d = 0; d < 3; ++d) g->dim[d] = dim[d];
+  g->pitch = pitch;
+  g->bytes = bytes;
+  g->dev = dev;
+  rt->grids.insert(g);
+  return g;
+}
+
+bool copy_grid(Grid *g, void *host, bool in, bool sync) {
+  const size_t row = (size_t)g->dim[0] * g->esz;
+  const size_t rows = (size_t)g->dim[1] * g->dim[2];
+  cudaError_t e;
+  if (row == g->pitch) {
+    e = in ? cudaMemcpyAsync(g->dev, host, row * rows, cudaMemcpyHostToDevice, rt->stream)
+           : cudaMemcpyAsync(host, g->dev, row * rows, cudaMemcpyDeviceToHost, rt->stream);
+  } else {
+    e = in ? cudaMemcpy2DAsync(g->dev, g->pitch, host, row, row, rows,
+                               cudaMemcpyHostToDevice, rt->stream)
+           : cudaMemcpy2DAsync(host, row, g->dev, g->pitch, row, rows,
+                               cudaMemcpyDeviceToHost, rt->stream);
+  }
+  if (!cuda_ok(e, in ? "grid copy-in" : "grid copy-out")) return false;
+  return sync ? sync_rt() : true;
+}
+
+PSStencil add_map(Map &&m) {
+  if (!validate_map(m)) return -1;
+  if ((int)rt->maps.size() >= kMaxMaps) {
+    fail(PS_ERR_OUT_OF_MEMORY, "more than %d stencil maps", kMaxMaps);
+    return -1;
+  }
+  rt->maps.push_back(std::move(m));
+  return kStencilTag | (int)(rt->maps.size() - 1);
+}
+
+Map *lookup_map(PSStencil s) {
+  if ((s & kStencilTagMask) != kStencilTag) return nullptr;
+  const int idx = s & ~kStencilTagMask;
+  if (idx < 0 || idx >= (int)rt->maps.size()) return nullptr;
+  return &rt->maps[idx];
+}
+
+bool map_from(int kernel, const __PSDomain &dom, int ngrids, void *const *grids,
+              int nscalars, const double *scalars, Map *out) {
+  KernelSig sig;
+  if (!kernel_sig(kernel, &sig))
+    return fail(PS_ERR_UNKNOWN_KERNEL, "unknown builtin stencil id %d", kernel);
+  if (ngrids != sig.ngrids || nscalars != sig.nscalars)
+    return fail(PS_ERR_INVALID_ARGUMENT, "%s takes %d grids and %d scalars, got %d and %d",
+                sig.name, sig.ngrids, sig.nscalars, ngrids, nscalars);
+  out->kernel = kernel;
+  out->dom = dom;
+  out->grids.clear();
+  for (int i = 0; i < ngrids; ++i) {
+    Grid *g = as_grid(grids[i], sig.name);
+    if (!g) return false;
+    out->grids.push_back(g);
+  }
+  out->scalars.assign(scalars, scalars + nscalars);
+  return true;
+}
+
+bool run_maps(const std::vector<Map *> &ms, int iter) {
+  std::chrono::steady_clock::time_point t0;
+  if (rt->trace) {
+    fprintf(stderr, "Physis: Stencil started\n");
+    t0 = std::chrono::steady_clock::now();
+  }
+  for (int i = 0; i < iter; ++i)
+    for (Map *m : ms)
+      if (!launch_map(*m, m->kernel == PS_KERNEL_HIMENO19_GOSA)) return false;
+  if (rt->trace) {
+    if (!sync_rt()) return false;
+    const double ms_ = std::chrono::duration<double, std::milli>(
+                           std::chrono::steady_clock::now() - t0).count();
+    fprintf(stderr, "Physis: Stencil finished (time: %f ms)\n", ms_);
+  }
+  return true;
+}
+
+bool read_result(int slot, uint64_t *bits) {
+  if (!cuda_ok(cudaMemcpyAsync(bits, rt->results + slot, 8, cudaMemcpyDeviceToHost,
+                               rt->stream), "read reduction result"))
+    return false;
+  return sync_rt();
+}
+
+bool reduce_grid(Grid *g, int op, uint64_t *bits) {
+  if (op < PS_MAX || op > PS_PROD)
+    return fail(PS_ERR_INVALID_ARGUMENT, "unknown reduction op %d", op);
+  const GridView v = view(g);
+  const int n = psg::reduce_num_ctas(v, rt->sm_count);
+  if (n > kMaxPartials) return fail(PS_ERR_UNSUPPORTED, "reduction grid too large");
+  cudaError_t e = psg::launch_reduce(v, op, rt->partials, n, rt->ticket, rt->results,
+                                     rt->dev_err, rt->stream);
+  if (!cuda_ok(e, "reduce launch")) return false;
+  ++rt->launches;
+  return read_result(0, bits);
+}
+
+void store_reduced(void *v, int type, uint64_t bits) {
+  switch (type) {
+    case PS_FLOAT: {
+      double d;
+      memcpy(&d, &bits, 8);
+      *static_cast<float *>(v) = (float)d;
+      break;
+    }
+    case PS_DOUBLE: memcpy(v, &bits, 8); break;
+    case PS_INT: {
+      int32_t i = (int32_t)(uint32_t)bits;
+      memcpy(v, &i, 4);
+      break;
+    }
+    case PS_LONG: memcpy(v, &bits, 8); break;
+  }
+}
+
+bool reduce_kernel_form(void *v, int op, int kernel, const __PSDomain &dom, int ngrids,
+                        void *const *grids, int nscalars, const double *scalars,
+                        double *out64) {
+  if (kernel != PS_KERNEL_HIMENO19_GOSA)
+    return fail(PS_ERR_UNSUPPORTED,
+                "PSReduce kernel form: builtin %d yields no per-point value", kernel);
+  if (op != PS_SUM)
+    return fail(PS_ERR_UNSUPPORTED, "PSReduce kernel form supports PS_SUM only");
+  Map m;
+  if (!map_from(kernel, dom, ngrids, grids, nscalars, scalars, &m)) return false;
+  if (!validate_map(m)) return false;
+  if (!launch_map(m, true)) return false;
+  uint64_t bits = 0;
+  if (!read_result(1, &bits)) return false;
+  double d;
+  memcpy(&d, &bits, 8);
+  if (m.dom.min[0] >= m.dom.max[0] || m.dom.min[1] >= m.dom.max[1] ||
+      m.dom.min[2] >= m.dom.max[2])
+    d = 0.0;
+  if (v) *static_cast<float *>(v) = (float)d;
+  if (out64) *out64 = d;
+  return true;
+}
+
+}  // namespace
+
+namespace psg {
+
+bool make_tmap_3d(CUtensorMap *map, const GridView &g, int box_w, int box_h) {
+  if (!g_encode) return fail(PS_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  CUtensorMapDataType dt;
+  switch (g.type) {
+    case kFloat: dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32; break;
+    case kDouble: dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT64; break;
+    case kInt: dt = CU_TENSOR_MAP_DATA_TYPE_INT32; break;
+    default: dt = CU_TENSOR_MAP_DATA_TYPE_INT64; break;
+  }
+  cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
+  cuuint64_t strides[2] = {(cuuint64_t)g.pitch, (cuuint64_t)g.pitch * (cuuint64_t)g.ny};
+  cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)box_h, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = g_encode(map, dt, 3, g.ptr, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return fail(PS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d) for box %dx%d", (int)r,
+                box_w, box_h);
+  return true;
+}
+
+}  // namespace psg
+
+extern "C" {
+
+void PSInit(int *argc, char ***argv, int grid_num_dims, ...) {
+  (void)grid_num_dims;
+  bool trace = false;
+  if (argc && argv && *argv) {
+    int w = 0;
+    for (int r = 0; r < *argc; ++r) {
+      if ((*argv)[r] && strcmp((*argv)[r], "--physis-trace") == 0) {
+        trace = true;
+        continue;
+      }
+      (*argv)[w++] = (*argv)[r];
+    }
+    if (w < *argc) (*argv)[w] = nullptr;
+    *argc = w;
+  }
+  const char *te = getenv("PS_TRACE");
+  if (te && te[0] == '1') trace = true;
+  PSInitV(trace ? 1 : 0);
+}
+
+void PSInitV(int trace) {
+  if (rt) {
+    rt->trace = rt->trace || trace;
+    return;
+  }
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    fail(PS_ERR_NO_DEVICE, "no CUDA device available (%s)",
+         e != cudaSuccess ? cudaGetErrorString(e) : "count is 0");
+    return;
+  }
+  Runtime *r = new Runtime();
+  const char *de = getenv("PS_DEVICE");
+  r->device = de ? atoi(de) : 0;
+  if (!cuda_ok(cudaSetDevice(r->device), "cudaSetDevice")) {
+    delete r;
+    return;
+  }
+  cudaDeviceProp prop;
+  if (!cuda_ok(cudaGetDeviceProperties(&prop, r->device), "cudaGetDeviceProperties")) {
+    delete r;
+    return;
+  }
+  if (prop.major < 10) {
+    fail(PS_ERR_UNSUPPORTED, "device %s (sm_%d%d) is not a Blackwell GPU; this library "
+         "is built for sm_103a only", prop.name, prop.major, prop.minor);
+    delete r;
+    return;
+  }
+  r->sm_count = prop.multiProcessorCount;
+  r->trace = trace != 0;
+  if (!g_encode) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                         cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+      fail(PS_ERR_CUDA, "cannot resolve cuTensorMapEncodeTiled");
+      delete r;
+      return;
+    }
+    g_encode = reinterpret_cast<EncodeTiledFn>(fn);
+  }
+  if (!cuda_ok(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking),
+               "cudaStreamCreate") ||
+      !cuda_ok(cudaMalloc(&r->dev_err, sizeof(int)), "cudaMalloc") ||
+      !cuda_ok(cudaMalloc(&r->partials, sizeof(uint64_t) * kMaxPartials), "cudaMalloc") ||
+      !cuda_ok(cudaMalloc(&r->ticket, sizeof(unsigned)), "cudaMalloc") ||
+      !cuda_ok(cudaMalloc(&r->results, sizeof(uint64_t) * 8), "cudaMalloc")) {
+    delete r;
+    return;
+  }
+  cudaMemset(r->dev_err, 0, sizeof(int));
+  cudaMemset(r->ticket, 0, sizeof(unsigned));
+  cudaMemset(r->results, 0, sizeof(uint64_t) * 8);
+  for (int i = 0; i < kNumEvents; ++i) cudaEventCreate(&r->events[i]);
+  // Default launch shapes (the autotuner may replace them).
+  for (int k = 0; k < kNumKernels; ++k) r->shapes[k] = MarchConfig{8, 4, 0, 0};
+  r->shapes[PS_KERNEL_HIMENO19] = MarchConfig{4, 5, 0, 2};
+  r->shapes[PS_KERNEL_HIMENO19_GOSA] = MarchConfig{4, 5, 0, 2};
+  cudaDeviceSynchronize();
+  rt = r;
+}
+
+void PSFinalize(void) {
+  if (!rt) return;
+  cudaStreamSynchronize(rt->stream);
+  for (Grid *g : rt->grids) {
+    cudaFree(g->dev);
+    g->magic = 0;
+    delete g;
+  }
+  rt->grids.clear();
+  cudaFree(rt->dev_err);
+  cudaFree(rt->partials);
+  cudaFree(rt->ticket);
+  cudaFree(rt->results);
+  for (int i = 0; i < kNumEvents; ++i) cudaEventDestroy(rt->events[i]);
+  cudaStreamDestroy(rt->stream);
+  delete rt;
+  rt = nullptr;
+}
+
+void PSPrintInternalInfo(FILE *out) {
+  if (!out) out = stderr;
+  if (!rt) {
+    fprintf(out, "physis_gb300: not initialized\n");
+    return;
+  }
+  cudaDeviceProp p;
+  cudaGetDeviceProperties(&p, rt->device);
+  fprintf(out, "physis_gb300: device %d %s sm_%d%d, %d SMs, %zu grids, %zu maps\n",
+          rt->device, p.name, p.major, p.minor, rt->sm_count, rt->grids.size(),
+          rt->maps.size());
+}
+
+void *PSGridNewV(int type, int ndims, const PSIndex *dims) {
+  return grid_new(type, ndims, dims);
+}
+
+#define PS_DEFINE_NEW(RANK, NAME, TYPE, ...)                 \
+  PS##NAME PS##NAME##New(__VA_ARGS__, ...) {                 \
+    PSIndex d[3] = {PS_NEW_DIMS_##RANK};                     \
+    return static_cast<PS##NAME>(grid_new(TYPE, RANK, d));   \
+  }
+#define PS_NEW_DIMS_1 nx, 1, 1
+#define PS_NEW_DIMS_2 nx, ny, 1
+#define PS_NEW_DIMS_3 nx, ny, nz
+PS_DEFINE_NEW(1, Grid1DFloat, PS_FLOAT, PSIndex nx)
+PS_DEFINE_NEW(1, Grid1DDouble, PS_DOUBLE, PSIndex nx)
+PS_DEFINE_NEW(1, Grid1DInt, PS_INT, PSIndex nx)
+PS_DEFINE_NEW(1, Grid1DLong, PS_LONG, PSIndex nx)
+PS_DEFINE_NEW(2, Grid2DFloat, PS_FLOAT, PSIndex nx, PSIndex ny)
+PS_DEFINE_NEW(2, Grid2DDouble, PS_DOUBLE, PSIndex nx, PSIndex ny)
+PS_DEFINE_NEW(2, Grid2DInt, PS_INT, PSIndex nx, PSIndex ny)
+PS_DEFINE_NEW(2, Grid2DLong, PS_LONG, PSIndex nx, PSIndex ny)
+PS_DEFINE_NEW(3, Grid3DFloat, PS_FLOAT, PSIndex nx, PSIndex ny, PSIndex nz)
+PS_DEFINE_NEW(3, Grid3DDouble, PS_DOUBLE, PSIndex nx, PSIndex ny, PSIndex nz)
+PS_DEFINE_NEW(3, Grid3DInt, PS_INT, PSIndex nx, PSIndex ny, PSIndex nz)
+PS_DEFINE_NEW(3, Grid3DLong, PS_LONG, PSIndex nx, PSIndex ny, PSIndex nz)
+
+void PSGridCopyin(void *g, const void *src_array) {
+  Grid *p = as_grid(g, "PSGridCopyin");
+  if (!p) return;
+  if (!src_array) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSGridCopyin: NULL source");
+    return;
+  }
+  copy_grid(p, const_cast<void *>(src_array), true, true);
+}
+
+void PSGridCopyout(void *g, void *dst_array) {
+  Grid *p = as_grid(g, "PSGridCopyout");
+  if (!p) return;
+  if (!dst_array) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSGridCopyout: NULL destination");
+    return;
+  }
+  copy_grid(p, dst_array, false, true);
+}
+
+void PSGridCopyinAsync(void *g, const void *src) {
+  Grid *p = as_grid(g, "PSGridCopyinAsync");
+  if (p && src) copy_grid(p, const_cast<void *>(src), true, false);
+}
+
+void PSGridCopyoutAsync(void *g, void *dst) {
+  Grid *p = as_grid(g, "PSGridCopyoutAsync");
+  if (p && dst) copy_grid(p, dst, false, false);
+}
+
+void PSGridFree(void *g) {
+  Grid *p = as_grid(g, "PSGridFree");
+  if (!p) return;
+  cudaStreamSynchronize(rt->stream);
+  cudaFree(p->dev);
+  rt->grids.erase(p);
+  p->magic = 0;
+  delete p;
+}
+
+PSIndex PSGridDim(void *g, int d) {
+  Grid *p = as_grid(g, "PSGridDim");
+  if (!p) return 0;
+  if (d < 0 || d >= 3) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSGridDim: dimension %d", d);
+    return 0;
+  }
+  return p->dim[d];
+}
+
+void *PSGridDevicePtr(void *g) {
+  Grid *p = as_grid(g, "PSGridDevicePtr");
+  return p ? p->dev : nullptr;
+}
+size_t PSGridPitch(void *g) {
+  Grid *p = as_grid(g, "PSGridPitch");
+  return p ? p->pitch : 0;
+}
+int PSGridElemSize(void *g) {
+  Grid *p = as_grid(g, "PSGridElemSize");
+  return p ? p->esz : 0;
+}
+int PSGridType(void *g) {
+  Grid *p = as_grid(g, "PSGridType");
+  return p ? p->type : -1;
+}
+
+PSDomain1D PSDomain1DNew(PSIndex minx, PSIndex maxx) {
+  PSDomain1D d = {{minx, 0, 0}, {maxx, 1, 1}, {minx, 0, 0}, {maxx, 1, 1}};
+  return d;
+}
+PSDomain2D PSDomain2DNew(PSIndex minx, PSIndex maxx, PSIndex miny, PSIndex maxy) {
+  PSDomain2D d = {{minx, miny, 0}, {maxx, maxy, 1}, {minx, miny, 0}, {maxx, maxy, 1}};
+  return d;
+}
+PSDomain3D PSDomain3DNew(PSIndex minx, PSIndex maxx, PSIndex miny, PSIndex maxy,
+                         PSIndex minz, PSIndex maxz) {
+  PSDomain3D d = {{minx, miny, minz}, {maxx, maxy, maxz},
+                  {minx, miny, minz}, {maxx, maxy, maxz}};
+  return d;
+}
+
+PSStencil __PSStencilMap(void *kernel, ...) {
+  if (!need_rt("PSStencilMap")) return -1;
+  const int k = (int)(intptr_t)kernel;
+  KernelSig sig;
+  if (!kernel_sig(k, &sig)) {
+    fail(PS_ERR_UNKNOWN_KERNEL, "unknown builtin stencil id %d", k);
+    return -1;
+  }
+  va_list vl;
+  va_start(vl, kernel);
+  __PSDomain dom = va_arg(vl, __PSDomain);
+  void *grids[16];
+  double sc[16];
+  for (int i = 0; i < sig.ngrids; ++i) grids[i] = va_arg(vl, void *);
+  for (int i = 0; i < sig.nscalars; ++i) sc[i] = va_arg(vl, double);
+  va_end(vl);
+  Map m;
+  if (!map_from(k, dom, sig.ngrids, grids, sig.nscalars, sc, &m)) return -1;
+  return add_map(std::move(m));
+}
+
+PSStencil PSStencilMapV(int kernel, const PSDomain3D *dom, int ngrids, void *const *grids,
+                        int nscalars, const double *scalars) {
+  if (!need_rt("PSStencilMapV")) return -1;
+  if (!dom || (ngrids && !grids) || (nscalars && !scalars)) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSStencilMapV: NULL argument");
+    return -1;
+  }
+  Map m;
+  if (!map_from(kernel, *dom, ngrids, grids, nscalars, scalars, &m)) return -1;
+  return add_map(std::move(m));
+}
+
+void PSStencilRunV(int n, const PSStencil *stencils, int iter) {
+  if (!need_rt("PSStencilRun")) return;
+  if (n <= 0 || !stencils || iter < 0) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSStencilRun: %d stencils, iter %d", n, iter);
+    return;
+  }
+  std::vector<Map *> ms;
+  for (int i = 0; i < n; ++i) {
+    Map *m = lookup_map(stencils[i]);
+    if (!m) {
+      fail(PS_ERR_BAD_HANDLE, "PSStencilRun: %d is not a stencil", stencils[i]);
+      return;
+    }
+    ms.push_back(m);
+  }
+  run_maps(ms, iter);
+}
+
+void PSStencilRun(PSStencil s, ...) {
+  if (!need_rt("PSStencilRun")) return;
+  std::vector<PSStencil> list;
+  int iter = 1;
+  list.push_back(s);
+  va_list vl;
+  va_start(vl, s);
+  for (int guard = 0; guard < 4096; ++guard) {
+    const int a = va_arg(vl, int);
+    if (a == PS_RUN_END) break;
+    if ((a & kStencilTagMask) == kStencilTag) {
+      list.push_back(a);
+    } else {
+      iter = a;
+      const int end = va_arg(vl, int);
+      if (end != PS_RUN_END) {
+        va_end(vl);
+        fail(PS_ERR_INVALID_ARGUMENT,
+             "PSStencilRun: the iteration count must be the last argument");
+        return;
+      }
+      break;
+    }
+  }
+  va_end(vl);
+  PSStencilRunV((int)list.size(), list.data(), iter);
+}
+
+void PSReduceGridV(void *v, int op, void *g) {
+  Grid *p = as_grid(g, "PSReduce");
+  if (!p) return;
+  if (!v) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSReduce: NULL result pointer");
+    return;
+  }
+  uint64_t bits;
+  if (reduce_grid(p, op, &bits)) store_reduced(v, p->type, bits);
+}
+
+void PSReduceGridF64(double *v, int op, void *g) {
+  Grid *p = as_grid(g, "PSReduceGridF64");
+  if (!p) return;
+  if (p->type != PS_FLOAT && p->type != PS_DOUBLE) {
+    fail(PS_ERR_UNSUPPORTED, "PSReduceGridF64 needs a float or double grid");
+    return;
+  }
+  uint64_t bits;
+  if (v && reduce_grid(p, op, &bits)) memcpy(v, &bits, 8);
+}
+
+void PSReduceKernelV(void *v, int op, int kernel, const PSDomain3D *dom, int ngrids,
+                     void *const *grids, int nscalars, const double *scalars) {
+  if (!need_rt("PSReduce")) return;
+  if (!dom) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSReduceKernelV: NULL domain");
+    return;
+  }
+  reduce_kernel_form(v, op, kernel, *dom, ngrids, grids, nscalars, scalars, nullptr);
+}
+
+void PSReduce(void *v, ...) {
+  if (!need_rt("PSReduce")) return;
+  va_list vl;
+  va_start(vl, v);
+  const int op = va_arg(vl, int);
+  void *third = va_arg(vl, void *);
+  Grid *g = static_cast<Grid *>(third);
+  if (g && rt->grids.count(g)) {
+    va_end(vl);
+    PSReduceGridV(v, op, g);
+    return;
+  }
+  const int k = (int)(intptr_t)third;
+  KernelSig sig;
+  if (!kernel_sig(k, &sig)) {
+    va_end(vl);
+    fail(PS_ERR_BAD_HANDLE, "PSReduce: third argument is neither a grid nor a builtin");
+    return;
+  }
+  __PSDomain dom = va_arg(vl, __PSDomain);
+  void *grids[16];
+  double sc[16];
+  for (int i = 0; i < sig.ngrids; ++i) grids[i] = va_arg(vl, void *);
+  for (int i = 0; i < sig.nscalars; ++i) sc[i] = va_arg(vl, double);
+  va_end(vl);
+  if (!v) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSReduce: NULL result pointer");
+    return;
+  }
+  reduce_kernel_form(v, op, k, dom, sig.ngrids, grids, sig.nscalars, sc, nullptr);
+}
+
+int PSGetLastError(void) { return g_err; }
+const char *PSGetLastErrorString(void) { return g_errmsg.c_str(); }
+const char *PSGetErrorName(int code) { return err_name(code); }
+void PSClearError(void) {
+  g_err = PS_OK;
+  g_errmsg.clear();
+}
+
+void *PSHostAlloc(size_t bytes) {
+  void *p = nullptr;
+  if (!cuda_ok(cudaMallocHost(&p, bytes), "cudaMallocHost")) return nullptr;
+  return p;
+}
+void PSHostFree(void *p) {
+  if (p) cudaFreeHost(p);
+}
+
+void PSSynchronize(void) {
+  if (!need_rt("PSSynchronize")) return;
+  sync_rt();
+}
+
+void *PSGetStream(void) { return rt ? (void *)rt->stream : nullptr; }
+
+void PSEventRecord(int slot) {
+  if (!need_rt("PSEventRecord")) return;
+  if (slot < 0 || slot >= kNumEvents) {
+    fail(PS_ERR_INVALID_ARGUMENT, "event slot %d", slot);
+    return;
+  }
+  cuda_ok(cudaEventRecord(rt->events[slot], rt->stream), "cudaEventRecord");
+}
+
+float PSEventElapsedMs(int a, int b) {
+  if (!need_rt("PSEventElapsedMs")) return -1.0f;
+  if (a < 0 || a >= kNumEvents || b < 0 || b >= kNumEvents) {
+    fail(PS_ERR_INVALID_ARGUMENT, "event slots %d %d", a, b);
+    return -1.0f;
+  }
+  if (!cuda_ok(cudaEventSynchronize(rt->events[b]), "cudaEventSynchronize")) return -1.0f;
+  float ms = 0.0f;
+  if (!cuda_ok(cudaEventElapsedTime(&ms, rt->events[a], rt->events[b]),
+               "cudaEventElapsedTime"))
+    return -1.0f;
+  return ms;
+}
+
+long long PSGetLaunchCount(void) { return rt ? rt->launches : 0; }
+int PSGetSMCount(void) { return rt ? rt->sm_count : 0; }
+
+void PSSetLaunchShape(int kernel, const PSLaunchShape *shape) {
+  if (!need_rt("PSSetLaunchShape")) return;
+  if (!shape) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSSetLaunchShape: NULL shape");
+    return;
+  }
+  const bool him = (kernel == PS_KERNEL_HIMENO19 || kernel == PS_KERNEL_HIMENO19_GOSA);
+  const int max_ty = him ? 8 : 16;
+  if ((shape->ty > max_ty) || (shape->ns > 0 && shape->ns < (him ? 3 : 2)) ||
+      shape->ns > 16 || shape->ns2 > 8) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSSetLaunchShape: ty %d ns %d ns2 %d out of range",
+         shape->ty, shape->ns, shape->ns2);
+    return;
+  }
+  for (int k = 0; k < kNumKernels; ++k) {
+    if (kernel != 0 && k != shape_slot(kernel)) continue;
+    MarchConfig c = rt->shapes[k];
+    if (shape->ty > 0) c.ty = shape->ty;
+    if (shape->ns > 0) c.ns = shape->ns;
+    c.zchunk = shape->zchunk;  // <= 0 means automatic
+    if (shape->ns2 > 0) c.ns2 = shape->ns2;
+    const bool kh = (k == PS_KERNEL_HIMENO19 || k == PS_KERNEL_HIMENO19_GOSA);
+    const size_t smem = kh ? psg::himeno19_smem_bytes(c) : psg::stencil7_smem_bytes(8, c);
+    if (smem > 227 * 1024) {
+      fail(PS_ERR_INVALID_ARGUMENT, "PSSetLaunchShape: %zu bytes of shared memory", smem);
+      return;
+    }
+    if (kernel == 0 && kh) continue;  // a global shape does not touch Himeno's rings
+    rt->shapes[k] = c;
+  }
+}
+
+void PSGetLaunchShape(int kernel, PSLaunchShape *shape) {
+  if (!need_rt("PSGetLaunchShape") || !shape) return;
+  const MarchConfig &c = rt->shapes[shape_slot(kernel)];
+  shape->ty = c.ty;
+  shape->ns = c.ns;
+  shape->zchunk = c.zchunk;
+  shape->ns2 = c.ns2;
+}
+
+void PSTestFailNextAllocs(int n) {
+  if (need_rt("PSTestFailNextAllocs")) rt->fail_allocs = n;
+}
+
+void PSTestDeviceWaitTimeout(unsigned limit) {
+  if (!need_rt("PSTestDeviceWaitTimeout")) return;
+  if (cuda_ok(psg::launch_wait_timeout_probe(rt->dev_err, limit, rt->stream),
+              "wait-timeout probe launch"))
+    ++rt->launches;
+}
+
+}  // extern "C"
