@@ -361,7 +361,11 @@ def main():
     ap.add_argument("--ty", type=int, default=0)
     ap.add_argument("--ns", type=int, default=0)
     ap.add_argument("--zchunk", type=int, default=0)
+    ap.add_argument("--n", type=int, default=512,
+                    help="grid edge (default 512; smaller only for profiling)")
     args = ap.parse_args()
+    global N
+    N = args.n
     if args.warmup < 3:
         args.warmup = 3
     dist = Dist()

@@ -50,6 +50,8 @@ struct HParams {
 };
 
 __host__ __device__ constexpr int h_bar_bytes(int n) { return 128 * ((8 * n + 127) / 128); }
+// Every TMA destination starts on a 128-byte boundary.
+__host__ __device__ constexpr uint32_t h_align128(uint32_t b) { return (b + 127u) & ~127u; }
 
 __device__ __forceinline__ void row6(const float *pl, int idx, int lane, float (&r)[6]) {
   float v[4];
@@ -83,13 +85,14 @@ himeno19_kernel(const __grid_constant__ HimenoMaps maps, const HParams p) {
   typedef RN<float> R;
   const int TY = blockDim.y;
   const int nsp = p.nsp, nsc = p.nsc;
-  const int p_elems = kW * (TY + 2);
-  const uint32_t p_bytes = (uint32_t)(p_elems * 4);
+  const uint32_t p_bytes = (uint32_t)(kW * (TY + 2) * 4);
+  const int p_elems = (int)(h_align128(p_bytes) / 4);  // stage stride
   const int c_tile = kTX * TY;             // elements per coefficient tile
   const int c_elems = kNumCoef * c_tile;   // elements per coefficient stage
   const uint32_t c_bytes = (uint32_t)(c_elems * 4);
 
-  extern __shared__ __align__(128) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
   uint64_t *pfull = reinterpret_cast<uint64_t *>(smem);
   uint64_t *cfull = pfull + nsp;
   float *pring = reinterpret_cast<float *>(smem + h_bar_bytes(nsp + nsc));
@@ -262,8 +265,9 @@ himeno19_kernel(const __grid_constant__ HimenoMaps maps, const HParams p) {
 }  // namespace
 
 size_t himeno19_smem_bytes(const MarchConfig &cfg) {
-  return (size_t)h_bar_bytes(cfg.ns + cfg.ns2) +
-         (size_t)cfg.ns * kW * (cfg.ty + 2) * 4 +
+  // 128 bytes of slack for aligning the dynamic shared-memory base
+  return 128 + (size_t)h_bar_bytes(cfg.ns + cfg.ns2) +
+         (size_t)cfg.ns * h_align128((uint32_t)(kW * (cfg.ty + 2) * 4)) +
          (size_t)cfg.ns2 * kNumCoef * kTX * cfg.ty * 4;
 }
 
@@ -316,26 +320,23 @@ cudaError_t launch_himeno19(const Himeno19Args &a, const MarchConfig &cfg,
     return cudaErrorInvalidConfiguration;
   dim3 block(32, cfg.ty, 1);
   const size_t smem = himeno19_smem_bytes(cfg);
-  static bool attr_set[2] = {false, false};
-  if (a.gosa) {
-    if (!attr_set[1]) {
-      cudaError_t e = cudaFuncSetAttribute(himeno19_kernel<true>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           227 * 1024);
-      if (e != cudaSuccess) return e;
-      attr_set[1] = true;
-    }
-    himeno19_kernel<true><<<grid, block, smem, s>>>(maps, p);
-  } else {
-    if (!attr_set[0]) {
-      cudaError_t e = cudaFuncSetAttribute(himeno19_kernel<false>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           227 * 1024);
-      if (e != cudaSuccess) return e;
-      attr_set[0] = true;
-    }
-    himeno19_kernel<false><<<grid, block, smem, s>>>(maps, p);
+  // Opt in to the dynamic shared memory this launch needs (the kernel also
+  // has a little static shared memory, so the opt-in is the exact size).
+  static size_t attr_set[2] = {0, 0};
+  size_t &have = attr_set[a.gosa ? 1 : 0];
+  if (smem > have) {
+    cudaError_t e = a.gosa
+        ? cudaFuncSetAttribute(himeno19_kernel<true>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+        : cudaFuncSetAttribute(himeno19_kernel<false>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    have = smem;
   }
+  if (a.gosa)
+    himeno19_kernel<true><<<grid, block, smem, s>>>(maps, p);
+  else
+    himeno19_kernel<false><<<grid, block, smem, s>>>(maps, p);
   return cudaGetLastError();
 }
 

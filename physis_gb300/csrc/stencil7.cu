@@ -45,6 +45,7 @@ struct S7Params {
 };
 
 __host__ __device__ constexpr int s7_bar_bytes(int ns) { return 128 * ((8 * ns + 127) / 128); }
+__host__ __device__ constexpr uint32_t s7_stage_bytes(uint32_t b) { return (b + 127u) & ~127u; }
 
 template <typename T, int K>
 __global__ void __launch_bounds__(512, 1)
@@ -56,11 +57,15 @@ s7_march_kernel(const __grid_constant__ CUtensorMap tin, const S7Params<T> p) {
   typedef RN<T> R;
 
   const int TY = blockDim.y;
-  const int plane_elems = W * (TY + 2);
-  const uint32_t plane_bytes = (uint32_t)(plane_elems * sizeof(T));
+  // TMA writes a box of W x (TY+2) elements; each ring stage starts on a
+  // 128-byte boundary (the alignment cp.async.bulk.tensor requires of its
+  // shared-memory destination).
+  const uint32_t plane_bytes = (uint32_t)(W * (TY + 2) * sizeof(T));
+  const int plane_elems = (int)(s7_stage_bytes(plane_bytes) / sizeof(T));
   const int ns = p.ns;
 
-  extern __shared__ __align__(128) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);
   T *ring = reinterpret_cast<T *>(smem + s7_bar_bytes(ns));
 
@@ -244,13 +249,13 @@ cudaError_t launch_t(const Stencil7Args &a, const MarchConfig &cfg,
     return cudaErrorInvalidConfiguration;
   dim3 block(32, cfg.ty, 1);
   const size_t smem = stencil7_smem_bytes((int)sizeof(T), cfg);
-  static bool attr_set = false;
-  if (!attr_set) {
+  static size_t attr_set = 0;  // dynamic shared memory opted in so far
+  if (smem > attr_set) {
     cudaError_t e = cudaFuncSetAttribute(s7_march_kernel<T, K>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         227 * 1024);
+                                         (int)smem);
     if (e != cudaSuccess) return e;
-    attr_set = true;
+    attr_set = smem;
   }
   s7_march_kernel<T, K><<<grid, block, smem, st>>>(*tin, p);
   return cudaGetLastError();
@@ -275,7 +280,9 @@ cudaError_t launch_type(const Stencil7Args &a, const MarchConfig &cfg,
 size_t stencil7_smem_bytes(int esz, const MarchConfig &cfg) {
   const int vec = 16 / esz;
   const int w = 32 * vec + 2 * vec;
-  return (size_t)s7_bar_bytes(cfg.ns) + (size_t)cfg.ns * w * (cfg.ty + 2) * esz;
+  // 128 bytes of slack for aligning the dynamic shared-memory base
+  return 128 + (size_t)s7_bar_bytes(cfg.ns) +
+         (size_t)cfg.ns * s7_stage_bytes((uint32_t)(w * (cfg.ty + 2) * esz));
 }
 
 cudaError_t launch_stencil7(const Stencil7Args &a, const MarchConfig &cfg,
