@@ -244,9 +244,9 @@ def run_gpu(args, dist):
     g1.copyin(init)
     g2.copyin(init)
     dom = ps.full_domain(shape)
-    if args.ty or args.ns or args.zchunk:
-        ps.set_launch_shape(ps.PS_KERNEL_DIFFUSION7, ty=args.ty, ns=args.ns,
-                            zchunk=args.zchunk)
+    if args.warps or args.rows or args.ns or args.ctas:
+        ps.set_launch_shape(ps.PS_KERNEL_DIFFUSION7, warps=args.warps,
+                            rows=args.rows, ns=args.ns, ctas_per_sm=args.ctas)
     m1 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g1, g2], COEF)
     m2 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g2, g1], COEF)
     K, W = args.steps, args.warmup
@@ -328,8 +328,9 @@ def run_gpu(args, dist):
                 "workload": WORKLOAD, "grid": [N, N, N],
                 "parallelism": f"replicas{dist.ws}" if dist.ws > 1 else "single-gpu",
                 "l2": "inputs larger than L2 (two 512 MiB grids vs 129 MB L2)",
-                "launch_shape": {"ty": shape_used[0], "ns": shape_used[1],
-                                 "zchunk": shape_used[2] or "auto"},
+                "launch_shape": {"warps": shape_used[0], "rows": shape_used[1],
+                                 "ns": shape_used[2],
+                                 "ctas_per_sm": shape_used[4] or "auto"},
                 "e2e_job": "PSGridCopyin(pinned) + K steps + PSGridCopyout(pinned)",
             },
             "e2e": {"value": e2e, "unit": "GLUPS",
@@ -358,9 +359,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ty", type=int, default=0)
+    ap.add_argument("--warps", type=int, default=0)
+    ap.add_argument("--rows", type=int, default=0)
     ap.add_argument("--ns", type=int, default=0)
-    ap.add_argument("--zchunk", type=int, default=0)
+    ap.add_argument("--ctas", type=int, default=0)
     ap.add_argument("--n", type=int, default=512,
                     help="grid edge (default 512; smaller only for profiling)")
     args = ap.parse_args()

@@ -109,16 +109,23 @@ int PSGetSMCount(void);
 
 /* ---- 4. Launch shapes and the autotuner -------------------------------- */
 
-/* Launch shape of a z-marching sweep: ty warp-rows per CTA (tile height),
- * ns ring stages, zchunk planes per CTA, ns2 second-ring stages (Himeno
- * coefficient planes).  A value <= 0 keeps the current setting. */
+/* Launch shape of a persistent z-marching sweep.  A CTA owns tiles 32
+ * lanes x 16 bytes wide in x and warps*rows cells high in y and marches them
+ * along z; each thread holds a column of `rows` rows in registers.  ns is
+ * the number of shared-memory ring stages (planes in flight + 2), ns2 the
+ * stages of Himeno's coefficient ring, ctas_per_sm the persistent grid size
+ * per SM (0 = as many as fit).  A field <= 0 keeps the current value
+ * (ctas_per_sm <= 0 selects "as many as fit").  Himeno kernels take
+ * rows == 1 and at most 8 warps. */
 typedef struct {
-  int ty;
+  int warps;
+  int rows;
   int ns;
-  int zchunk;
   int ns2;
+  int ctas_per_sm;
 } PSLaunchShape;
-/* Sets the shape used for maps of `kernel` from now on (0 = all kernels). */
+/* Sets the shape used for maps of `kernel` from now on (0 = every 7-point
+ * kernel). */
 void PSSetLaunchShape(int kernel, const PSLaunchShape *shape);
 void PSGetLaunchShape(int kernel, PSLaunchShape *shape);
 

@@ -60,8 +60,9 @@ class PSDomain(ctypes.Structure):
 
 
 class PSLaunchShape(ctypes.Structure):
-    _fields_ = [("ty", ctypes.c_int), ("ns", ctypes.c_int),
-                ("zchunk", ctypes.c_int), ("ns2", ctypes.c_int)]
+    _fields_ = [("warps", ctypes.c_int), ("rows", ctypes.c_int),
+                ("ns", ctypes.c_int), ("ns2", ctypes.c_int),
+                ("ctas_per_sm", ctypes.c_int)]
 
 
 class PSError(RuntimeError):
@@ -267,16 +268,17 @@ def synchronize():
     check()
 
 
-def set_launch_shape(kernel, ty=0, ns=0, zchunk=0, ns2=0):
-    sh = PSLaunchShape(ty, ns, zchunk, ns2)
+def set_launch_shape(kernel, warps=0, rows=0, ns=0, ns2=0, ctas_per_sm=0):
+    sh = PSLaunchShape(warps, rows, ns, ns2, ctas_per_sm)
     lib().PSSetLaunchShape(kernel, ctypes.byref(sh))
     check()
 
 
 def get_launch_shape(kernel):
+    """(warps, rows, ns, ns2, ctas_per_sm) of a kernel's launch shape."""
     sh = PSLaunchShape()
     lib().PSGetLaunchShape(kernel, ctypes.byref(sh))
-    return sh.ty, sh.ns, sh.zchunk, sh.ns2
+    return sh.warps, sh.rows, sh.ns, sh.ns2, sh.ctas_per_sm
 
 
 def launch_count():

@@ -41,14 +41,17 @@ struct Box {
   int max[3];
 };
 
-// Launch shape of a 2.5D z-marching stencil kernel: `ty` warp-rows per CTA
-// (the tile is 16 bytes x 32 lanes wide in x), `ns` shared-memory ring
-// stages, `zchunk` planes marched per CTA.
+// Launch shape of a persistent 2.5D z-marching stencil kernel.  A tile is
+// 32 lanes x 16 bytes wide in x and warps*rows rows high; each thread owns a
+// column of `rows` rows.  `ns` is the number of shared-memory ring stages
+// for the marched field, `ns2` that of a second ring (Himeno's coefficient
+// planes).  The grid is SMs x ctas_per_sm CTAs (0 = as many as fit).
 struct MarchConfig {
-  int ty;
+  int warps;
+  int rows;
   int ns;
-  int zchunk;
-  int ns2;  // second ring (coefficient planes) where a kernel has one
+  int ns2;
+  int ctas_per_sm;
 };
 
 // Builds a 3D tiled tensor map over g with box {box_w, box_h, 1} elements.
@@ -65,7 +68,7 @@ struct Stencil7Args {
 // Number of bytes of dynamic shared memory the launch will use.
 size_t stencil7_smem_bytes(int esz, const MarchConfig &cfg);
 cudaError_t launch_stencil7(const Stencil7Args &a, const MarchConfig &cfg,
-                            const CUtensorMap *tin, int *dev_err,
+                            const CUtensorMap *tin, int *dev_err, int sm_count,
                             cudaStream_t s);
 
 // ---- Himeno 19-point Jacobi (himeno19.cu) --------------------------------
@@ -82,10 +85,9 @@ struct ResidualSink {
   double *result;       // where the FP64 total goes
 };
 size_t himeno19_smem_bytes(const MarchConfig &cfg);
-int himeno19_num_ctas(const Himeno19Args &a, const MarchConfig &cfg);
 cudaError_t launch_himeno19(const Himeno19Args &a, const MarchConfig &cfg,
                             const CUtensorMap *tmaps /* 13: p0-halo, 12 coef */,
-                            const ResidualSink &sink, int *dev_err,
+                            const ResidualSink &sink, int *dev_err, int sm_count,
                             cudaStream_t s);
 
 // ---- Reductions (reduce.cu) ----------------------------------------------

@@ -271,22 +271,6 @@ bool validate_map(const Map &m) {
 
 int shape_slot(int kernel) { return (kernel > 0 && kernel < kNumKernels) ? kernel : 0; }
 
-// Fills in an automatic zchunk: enough CTAs for ~8 per SM.
-MarchConfig resolve_shape(int kernel, int xy_tiles, int nzdom) {
-  MarchConfig c = rt->shapes[shape_slot(kernel)];
-  if (c.zchunk <= 0) {
-    const int target = rt->sm_count * 8;
-    int zsplit = (target + xy_tiles - 1) / (xy_tiles > 0 ? xy_tiles : 1);
-    if (zsplit < 1) zsplit = 1;
-    int zc = (nzdom + zsplit - 1) / zsplit;
-    if (zc < 16) zc = 16;
-    c.zchunk = zc;
-  }
-  const int min_chunk = (nzdom + 65534) / 65535;  // grid.z limit
-  if (c.zchunk < min_chunk) c.zchunk = min_chunk;
-  return c;
-}
-
 bool launch_map(const Map &m, bool want_gosa) {
   const Grid *g0 = m.grids[0];
   psg::Box box;
@@ -303,20 +287,13 @@ bool launch_map(const Map &m, bool want_gosa) {
     a.dom = box;
     a.omega = (float)m.scalars[0];
     a.gosa = want_gosa;
-    const int xbase = (box.min[0] / 4) * 4;
-    const int tiles_x = (box.max[0] - xbase + 127) / 128;
-    MarchConfig probe = rt->shapes[shape_slot(m.kernel)];
-    const int tiles_y = (box.max[1] - box.min[1] + probe.ty - 1) / probe.ty;
-    MarchConfig cfg = resolve_shape(m.kernel, tiles_x * tiles_y, box.max[2] - box.min[2]);
-    if (want_gosa) {
-      while (psg::himeno19_num_ctas(a, cfg) > kMaxPartials) cfg.zchunk *= 2;
-    }
+    const MarchConfig cfg = rt->shapes[shape_slot(m.kernel)];
     CUtensorMap maps[13];
-    const CUtensorMap *t = tmap_for(m.grids[0], 136, cfg.ty + 2);
+    const CUtensorMap *t = tmap_for(m.grids[0], 136, cfg.warps + 2);
     if (!t) return false;
     maps[0] = *t;
     for (int i = 0; i < 12; ++i) {
-      t = tmap_for(m.grids[2 + i], 128, cfg.ty);
+      t = tmap_for(m.grids[2 + i], 128, cfg.warps);
       if (!t) return false;
       maps[1 + i] = *t;
     }
@@ -325,7 +302,7 @@ bool launch_map(const Map &m, bool want_gosa) {
     sink.max_partials = kMaxPartials;
     sink.ticket = rt->ticket;
     sink.result = reinterpret_cast<double *>(rt->results + 1);
-    e = psg::launch_himeno19(a, cfg, maps, sink, rt->dev_err, rt->stream);
+    e = psg::launch_himeno19(a, cfg, maps, sink, rt->dev_err, rt->sm_count, rt->stream);
     if (!cuda_ok(e, "himeno19 launch")) return false;
     ++rt->launches;
     return true;
@@ -337,15 +314,10 @@ bool launch_map(const Map &m, bool want_gosa) {
   a.dom = box;
   for (int i = 0; i < 7; ++i) a.coef[i] = i < (int)m.scalars.size() ? m.scalars[i] : 0.0;
   const int vec = 16 / g0->esz;
-  const int tx = 32 * vec;
-  const int xbase = (box.min[0] / vec) * vec;
-  const int tiles_x = (box.max[0] - xbase + tx - 1) / tx;
-  MarchConfig probe = rt->shapes[shape_slot(m.kernel)];
-  const int tiles_y = (box.max[1] - box.min[1] + probe.ty - 1) / probe.ty;
-  MarchConfig cfg = resolve_shape(m.kernel, tiles_x * tiles_y, box.max[2] - box.min[2]);
-  const CUtensorMap *t = tmap_for(m.grids[0], tx + 2 * vec, cfg.ty + 2);
+  const MarchConfig cfg = rt->shapes[shape_slot(m.kernel)];
+  const CUtensorMap *t = tmap_for(m.grids[0], 34 * vec, cfg.warps * cfg.rows + 2);
   if (!t) return false;
-  e = psg::launch_stencil7(a, cfg, t, rt->dev_err, rt->stream);
+  e = psg::launch_stencil7(a, cfg, t, rt->dev_err, rt->sm_count, rt->stream);
   if (!cuda_ok(e, "stencil7 launch")) return false;
   ++rt->launches;
   return true;
@@ -643,10 +615,11 @@ void PSInitV(int trace) {
   cudaMemset(r->ticket, 0, sizeof(unsigned));
   cudaMemset(r->results, 0, sizeof(uint64_t) * 8);
   for (int i = 0; i < kNumEvents; ++i) cudaEventCreate(&r->events[i]);
-  // Default launch shapes (the autotuner may replace them).
-  for (int k = 0; k < kNumKernels; ++k) r->shapes[k] = MarchConfig{8, 4, 0, 0};
-  r->shapes[PS_KERNEL_HIMENO19] = MarchConfig{4, 5, 0, 2};
-  r->shapes[PS_KERNEL_HIMENO19_GOSA] = MarchConfig{4, 5, 0, 2};
+  // Default launch shapes (the autotuner may replace them):
+  // {warps, rows per thread, ring stages, second-ring stages, CTAs per SM}.
+  for (int k = 0; k < kNumKernels; ++k) r->shapes[k] = MarchConfig{4, 4, 4, 0, 0};
+  r->shapes[PS_KERNEL_HIMENO19] = MarchConfig{4, 1, 5, 2, 0};
+  r->shapes[PS_KERNEL_HIMENO19_GOSA] = MarchConfig{4, 1, 5, 2, 0};
   cudaDeviceSynchronize();
   rt = r;
 }
@@ -989,28 +962,31 @@ void PSSetLaunchShape(int kernel, const PSLaunchShape *shape) {
     fail(PS_ERR_INVALID_ARGUMENT, "PSSetLaunchShape: NULL shape");
     return;
   }
-  const bool him = (kernel == PS_KERNEL_HIMENO19 || kernel == PS_KERNEL_HIMENO19_GOSA);
-  const int max_ty = him ? 8 : 16;
-  if ((shape->ty > max_ty) || (shape->ns > 0 && shape->ns < (him ? 3 : 2)) ||
-      shape->ns > 16 || shape->ns2 > 8) {
-    fail(PS_ERR_INVALID_ARGUMENT, "PSSetLaunchShape: ty %d ns %d ns2 %d out of range",
-         shape->ty, shape->ns, shape->ns2);
-    return;
-  }
   for (int k = 0; k < kNumKernels; ++k) {
     if (kernel != 0 && k != shape_slot(kernel)) continue;
-    MarchConfig c = rt->shapes[k];
-    if (shape->ty > 0) c.ty = shape->ty;
-    if (shape->ns > 0) c.ns = shape->ns;
-    c.zchunk = shape->zchunk;  // <= 0 means automatic
-    if (shape->ns2 > 0) c.ns2 = shape->ns2;
     const bool kh = (k == PS_KERNEL_HIMENO19 || k == PS_KERNEL_HIMENO19_GOSA);
+    if (kernel == 0 && kh) continue;  // a global shape does not touch Himeno's
+    MarchConfig c = rt->shapes[k];
+    if (shape->warps > 0) c.warps = shape->warps;
+    if (shape->rows > 0) c.rows = shape->rows;
+    if (shape->ns > 0) c.ns = shape->ns;
+    if (shape->ns2 > 0) c.ns2 = shape->ns2;
+    c.ctas_per_sm = shape->ctas_per_sm > 0 ? shape->ctas_per_sm : 0;
+    const bool rows_ok = kh ? c.rows == 1
+                            : (c.rows == 1 || c.rows == 2 || c.rows == 4 || c.rows == 8);
+    const int max_warps = kh ? 8 : 16;
+    if (c.warps < 1 || c.warps > max_warps || !rows_ok || c.ns < (kh ? 3 : 2) ||
+        c.ns > 16 || (kh && (c.ns2 < 1 || c.ns2 > 8)) || c.ctas_per_sm > 32) {
+      fail(PS_ERR_INVALID_ARGUMENT,
+           "PSSetLaunchShape: warps %d rows %d ns %d ns2 %d ctas/SM %d out of range",
+           c.warps, c.rows, c.ns, c.ns2, c.ctas_per_sm);
+      return;
+    }
     const size_t smem = kh ? psg::himeno19_smem_bytes(c) : psg::stencil7_smem_bytes(8, c);
-    if (smem > 227 * 1024) {
+    if (smem > 200 * 1024) {
       fail(PS_ERR_INVALID_ARGUMENT, "PSSetLaunchShape: %zu bytes of shared memory", smem);
       return;
     }
-    if (kernel == 0 && kh) continue;  // a global shape does not touch Himeno's rings
     rt->shapes[k] = c;
   }
 }
@@ -1018,10 +994,11 @@ void PSSetLaunchShape(int kernel, const PSLaunchShape *shape) {
 void PSGetLaunchShape(int kernel, PSLaunchShape *shape) {
   if (!need_rt("PSGetLaunchShape") || !shape) return;
   const MarchConfig &c = rt->shapes[shape_slot(kernel)];
-  shape->ty = c.ty;
+  shape->warps = c.warps;
+  shape->rows = c.rows;
   shape->ns = c.ns;
-  shape->zchunk = c.zchunk;
   shape->ns2 = c.ns2;
+  shape->ctas_per_sm = c.ctas_per_sm;
 }
 
 void PSTestFailNextAllocs(int n) {

@@ -1,4 +1,4 @@
-// 7-point stencil sweeps on GB300 (sm_103a): 2.5D z-marching tiles.
+// 7-point stencil sweeps on GB300 (sm_103a): persistent 2.5D z-marching tiles.
 //
 // Replaces the translator-generated CUDA run kernel of the reference
 // (translator/cuda_runtime_builder.cc:1099-1228, 1392-1410: one thread per
@@ -8,22 +8,29 @@
 //   SUM7        unclamped 7-point sum, tests/system_tests/test_cases/test_7-pt.c:12-20
 //   COPY        out = in over the domain
 //
-// Design (one CTA = one 32*VEC x TY tile in x,y marching over zchunk planes):
-// * each z-plane of the tile plus a one-cell halo in y and a 16-byte halo in
-//   x (TMA wants 16-byte aligned x) is fetched by one TMA 3D box load into a
-//   ring of `ns` shared-memory stages; an mbarrier per stage signals arrival;
-// * one thread per 16-byte vector (VEC = 16/sizeof(T) cells): the z
-//   neighbours come from a register queue (b = previous centre, c = centre,
-//   t = next plane), the x neighbours from warp shuffles of the centre
-//   vector, the y neighbours from the rows above and below in shared memory;
-// * results leave as one 16-byte store per thread (a warp writes 512
-//   contiguous bytes); edge vectors that straddle the domain use masked
-//   scalar stores;
-// * clamped faces (neighbour index outside the grid -> centre value) are
-//   selects on the global coordinate, so the zero fill of out-of-range TMA
-//   boxes is never used;
-// * arithmetic is round-to-nearest without FMA contraction, in the REF
+// Design.  A tile is 32 lanes x 16 bytes wide in x (128 floats, 64 doubles)
+// and WARPS*RY rows high in y.  Work is the list of (tile, z) pairs with z
+// fastest; a persistent grid of SMs x occupancy CTAs splits that list into
+// equal contiguous ranges, so every CTA marches through one or two z-segments
+// of equal total length (no partial last wave) and CTAs that run at the same
+// time work on neighbouring tiles at the same depths (halos hit in L2).
+// * Each z-plane of the tile plus a one-row y halo and a 16-byte x halo
+//   (TMA wants 16-byte aligned x) arrives by one TMA 3D box load into a
+//   ring of `ns` shared-memory stages; one mbarrier per stage signals
+//   arrival.  Stage and phase advance incrementally (no divisions).
+// * Each thread owns one 16-byte vector column of RY rows: the z neighbours
+//   come from a register queue (b, c, t), the y neighbours of inner rows from
+//   the thread's own registers (only the rows above and below the column are
+//   read from shared memory), the x neighbours from warp shuffles.
+// * One 16-byte store per thread and row (a warp writes 512 contiguous
+//   bytes); vectors that straddle the domain edge use masked scalar stores.
+// * Clamped faces (neighbour outside the grid -> centre value) are selects
+//   on the global coordinate, so the zero fill of out-of-range boxes is never
+//   used.
+// * Arithmetic is round-to-nearest without FMA contraction in the REF
 //   expression order, so every cell is bit-identical to the REF target.
+#include <type_traits>
+
 #include "ps_device.cuh"
 #include "ps_internal.h"
 
@@ -38,7 +45,9 @@ struct S7Params {
   int nx, ny, nz;
   int dmin0, dmin1, dmin2, dmax0, dmax1, dmax2;
   int xbase;      // x of the first tile (multiple of VEC)
-  int zchunk;
+  int tiles_x;    // tiles per y-band
+  int nzd;        // planes in the domain
+  int64_t units;  // tiles * nzd
   int ns;
   T cc, cw, ce, cs, cn, cb, ct;  // expression order of DIFFUSION7
   int *err;
@@ -47,7 +56,7 @@ struct S7Params {
 __host__ __device__ constexpr int s7_bar_bytes(int ns) { return 128 * ((8 * ns + 127) / 128); }
 __host__ __device__ constexpr uint32_t s7_stage_bytes(uint32_t b) { return (b + 127u) & ~127u; }
 
-template <typename T, int K>
+template <typename T, int K, int RY>
 __global__ void __launch_bounds__(512, 1)
 s7_march_kernel(const __grid_constant__ CUtensorMap tin, const S7Params<T> p) {
   constexpr int VEC = 16 / (int)sizeof(T);
@@ -56,10 +65,9 @@ s7_march_kernel(const __grid_constant__ CUtensorMap tin, const S7Params<T> p) {
   constexpr bool kClamp = (K == kKernelDiffusion7);
   typedef RN<T> R;
 
-  const int TY = blockDim.y;
-  // TMA writes a box of W x (TY+2) elements; each ring stage starts on a
-  // 128-byte boundary (the alignment cp.async.bulk.tensor requires of its
-  // shared-memory destination).
+  const int TY = blockDim.y * RY;
+  // Each ring stage starts on a 128-byte boundary (required of the shared
+  // destination of cp.async.bulk.tensor).
   const uint32_t plane_bytes = (uint32_t)(W * (TY + 2) * sizeof(T));
   const int plane_elems = (int)(s7_stage_bytes(plane_bytes) / sizeof(T));
   const int ns = p.ns;
@@ -69,14 +77,8 @@ s7_march_kernel(const __grid_constant__ CUtensorMap tin, const S7Params<T> p) {
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);
   T *ring = reinterpret_cast<T *>(smem + s7_bar_bytes(ns));
 
-  const int lane = threadIdx.x, row = threadIdx.y;
-  const int tid = row * 32 + lane;
-  const int x0 = p.xbase + blockIdx.x * TX;
-  const int y0 = p.dmin1 + blockIdx.y * TY;
-  const int zs = p.dmin2 + blockIdx.z * p.zchunk;
-  const int ze = min(zs + p.zchunk, p.dmax2);
-  const int nplanes = ze - zs + 2;  // planes zs-1 .. ze
-
+  const int lane = threadIdx.x, warp = threadIdx.y;
+  const int tid = warp * 32 + lane;
   if (tid == 0) {
     prefetch_tmap(&tin);
     for (int s = 0; s < ns; ++s) mbar_init(&full[s], 1);
@@ -84,134 +86,215 @@ s7_march_kernel(const __grid_constant__ CUtensorMap tin, const S7Params<T> p) {
   }
   __syncthreads();
 
-  // Plane q of this CTA is global plane zs-1+q, held in stage q % ns.
-  auto issue = [&](int q) {
-    const int s = q % ns;
-    mbar_arrive_expect_tx(&full[s], plane_bytes);
-    tma_load_3d(ring + s * plane_elems, &tin, x0 - VEC, y0 - 1, zs - 1 + q, &full[s]);
-  };
-  if (tid == 0) {
-    const int n0 = min(ns, nplanes);
-    for (int q = 0; q < n0; ++q) issue(q);
-  }
+  // Producer state (thread 0) and consumer state (all threads): the stage
+  // that the next issued / next awaited plane uses, and its phase parity.
+  int pstage = 0;
+  uint32_t pphase = 0;
+  int cstage = 0;
+  uint32_t cphase = 0;
   bool ok = true;
-  auto wait = [&](int q) -> const T * {
-    const int s = q % ns;
-    if (!mbar_wait(&full[s], (uint32_t)((q / ns) & 1), p.err)) ok = false;
-    return ring + s * plane_elems;
-  };
 
-  const int cen = (row + 1) * W + VEC + lane * VEC;  // own vector, centre row
-  T b[VEC], c[VEC], t[VEC];
-  {
-    const T *pm = wait(0);
-    const T *pc = wait(1);
-    ld16_shared<T>(c, pc + cen);
-    ld16_shared<T>(b, pm + cen);
-    if (kClamp && zs == 0) {
-#pragma unroll
-      for (int i = 0; i < VEC; ++i) b[i] = c[i];
-    }
-  }
-  ok = __syncthreads_and(ok);
-  if (!ok) return;
-  if (tid == 0 && ns < nplanes) issue(ns);
+  int64_t u = (int64_t)blockIdx.x * p.units / gridDim.x;
+  const int64_t u_end = (int64_t)(blockIdx.x + 1) * p.units / gridDim.x;
+  const int rows0 = warp * RY;                          // first own row in the tile
+  const int cen0 = (rows0 + 1) * W + VEC + lane * VEC;  // own first row, centre
 
-  const int y = y0 + row;
-  const int x = x0 + lane * VEC;
-  const bool row_in = (y < p.dmax1);
-  const bool vec_in = (x >= p.dmin0) && (x + VEC <= p.dmax0);
+  while (u < u_end && ok) {
+    const int tile = (int)(u / p.nzd);
+    const int zoff = (int)(u - (int64_t)tile * p.nzd);
+    int64_t seg_end = (int64_t)(tile + 1) * p.nzd;
+    if (seg_end > u_end) seg_end = u_end;
+    const int zs = p.dmin2 + zoff;
+    const int ze = p.dmin2 + (int)(seg_end - (int64_t)tile * p.nzd);
+    u = seg_end;
+    const int x0 = p.xbase + (tile % p.tiles_x) * TX;
+    const int y0 = p.dmin1 + (tile / p.tiles_x) * TY;
+    const int nplanes = ze - zs + 2;  // planes zs-1 .. ze
 
-  for (int z = zs; z < ze; ++z) {
-    const int q = z - zs + 1;
-    const T *cur = ring + (q % ns) * plane_elems;
-    const T *nxt = wait(q + 1);
-    ld16_shared<T>(t, nxt + cen);
-    if (kClamp && z == p.nz - 1) {
-#pragma unroll
-      for (int i = 0; i < VEC; ++i) t[i] = c[i];
-    }
-    T o[VEC];
-    if (K == kKernelCopy) {
-#pragma unroll
-      for (int i = 0; i < VEC; ++i) o[i] = c[i];
-    } else {
-      T n[VEC], s[VEC];
-      ld16_shared<T>(n, cur + cen - W);  // y-1
-      ld16_shared<T>(s, cur + cen + W);  // y+1
-      T left = shfl_up1(c[VEC - 1]);
-      T right = shfl_down1(c[0]);
-      if (lane == 0) left = cur[cen - 1];
-      if (lane == 31) right = cur[cen + VEC];
-      if (kClamp) {
-        if (y == 0) {
-#pragma unroll
-          for (int i = 0; i < VEC; ++i) n[i] = c[i];
-        }
-        if (y == p.ny - 1) {
-#pragma unroll
-          for (int i = 0; i < VEC; ++i) s[i] = c[i];
-        }
+    // Issues plane q (global plane zs-1+q) into the producer's next stage.
+    auto issue = [&](int q) {
+      mbar_arrive_expect_tx(&full[pstage], plane_bytes);
+      tma_load_3d(ring + pstage * plane_elems, &tin, x0 - VEC, y0 - 1, zs - 1 + q,
+                  &full[pstage]);
+      if (++pstage == ns) {
+        pstage = 0;
+        pphase ^= 1u;
       }
-#pragma unroll
-      for (int i = 0; i < VEC; ++i) {
-        T w = (i == 0) ? left : c[i - 1];
-        T e = (i == VEC - 1) ? right : c[i + 1];
-        if (kClamp) {
-          if (x + i == 0) w = c[i];
-          if (x + i == p.nx - 1) e = c[i];
-          // cc*c + cw*w + ce*e + cs*s + cn*n + cb*b + ct*t, left to right
-          T v = R::mul(p.cc, c[i]);
-          v = R::add(v, R::mul(p.cw, w));
-          v = R::add(v, R::mul(p.ce, e));
-          v = R::add(v, R::mul(p.cs, s[i]));
-          v = R::add(v, R::mul(p.cn, n[i]));
-          v = R::add(v, R::mul(p.cb, b[i]));
-          v = R::add(v, R::mul(p.ct, t[i]));
-          o[i] = v;
-        } else {
-          // c + e + w + s + n + b + t, left to right
-          T v = R::add(c[i], e);
-          v = R::add(v, w);
-          v = R::add(v, s[i]);
-          v = R::add(v, n[i]);
-          v = R::add(v, b[i]);
-          v = R::add(v, t[i]);
-          o[i] = v;
-        }
+    };
+    // Waits for the next plane in issue order; returns its stage.
+    auto wait_next = [&]() -> const T * {
+      if (!mbar_wait(&full[cstage], cphase, p.err)) ok = false;
+      const T *pl = ring + cstage * plane_elems;
+      if (++cstage == ns) {
+        cstage = 0;
+        cphase ^= 1u;
       }
+      return pl;
+    };
+
+    if (tid == 0) {
+      const int n0 = min(ns, nplanes);
+      for (int q = 0; q < n0; ++q) issue(q);
     }
-    if (ok && row_in) {
-      T *dst = p.out + (int64_t)z * p.plane + (int64_t)y * p.row + x;
-      if (vec_in) {
-        st16_global<T>(dst, o);
-      } else {
+    T b[RY][VEC], c[RY][VEC], t[RY][VEC];
+    const T *pm = wait_next();   // plane zs-1
+    const T *cur = wait_next();  // plane zs
 #pragma unroll
-        for (int i = 0; i < VEC; ++i)
-          if (x + i >= p.dmin0 && x + i < p.dmax0) dst[i] = o[i];
+    for (int r = 0; r < RY; ++r) {
+      ld16_shared<T>(c[r], cur + cen0 + r * W);
+      ld16_shared<T>(b[r], pm + cen0 + r * W);
+      if (kClamp && zs == 0) {
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) b[r][i] = c[r][i];
       }
-    }
-#pragma unroll
-    for (int i = 0; i < VEC; ++i) {
-      b[i] = c[i];
-      c[i] = t[i];
     }
     ok = __syncthreads_and(ok);
     if (!ok) break;
-    if (tid == 0 && q + ns < nplanes) issue(q + ns);
+    if (tid == 0 && ns < nplanes) issue(ns);
+
+    const int x = x0 + lane * VEC;
+    const int y = y0 + rows0;  // first own row
+    const bool vec_in = (x >= p.dmin0) && (x + VEC <= p.dmax0);
+    const bool west_face = kClamp && (x == 0);            // element 0 clamps west
+    const int east_elem = kClamp ? (p.nx - 1 - x) : -1;  // element clamping east
+
+    for (int z = zs; z < ze; ++z) {
+      const int q = z - zs + 1;  // plane index of z
+      const T *nxt = wait_next();
+      T n[VEC], s[VEC];
+#pragma unroll
+      for (int r = 0; r < RY; ++r) ld16_shared<T>(t[r], nxt + cen0 + r * W);
+      if (K != kKernelCopy) {
+        ld16_shared<T>(n, cur + cen0 - W);       // row above the column
+        ld16_shared<T>(s, cur + cen0 + RY * W);  // row below the column
+      }
+      if (kClamp && z == p.nz - 1) {
+#pragma unroll
+        for (int r = 0; r < RY; ++r)
+#pragma unroll
+          for (int i = 0; i < VEC; ++i) t[r][i] = c[r][i];
+      }
+#pragma unroll
+      for (int r = 0; r < RY; ++r) {
+        T o[VEC];
+        if (K == kKernelCopy) {
+#pragma unroll
+          for (int i = 0; i < VEC; ++i) o[i] = c[r][i];
+        } else {
+          T nn[VEC], ss[VEC];
+#pragma unroll
+          for (int i = 0; i < VEC; ++i) {
+            nn[i] = (r == 0) ? n[i] : c[r - 1][i];
+            ss[i] = (r == RY - 1) ? s[i] : c[r + 1][i];
+          }
+          if (kClamp) {
+            if (y + r == 0) {
+#pragma unroll
+              for (int i = 0; i < VEC; ++i) nn[i] = c[r][i];
+            }
+            if (y + r == p.ny - 1) {
+#pragma unroll
+              for (int i = 0; i < VEC; ++i) ss[i] = c[r][i];
+            }
+          }
+          T left = shfl_up1(c[r][VEC - 1]);
+          T right = shfl_down1(c[r][0]);
+          if (lane == 0) left = cur[cen0 + r * W - 1];
+          if (lane == 31) right = cur[cen0 + r * W + VEC];
+#pragma unroll
+          for (int i = 0; i < VEC; ++i) {
+            T w = (i == 0) ? left : c[r][i - 1];
+            T e = (i == VEC - 1) ? right : c[r][i + 1];
+            if (kClamp) {
+              if (i == 0 && west_face) w = c[r][0];
+              if (i == east_elem) e = c[r][i];
+              // cc*c + cw*w + ce*e + cs*s + cn*n + cb*b + ct*t, left to right
+              T v = R::mul(p.cc, c[r][i]);
+              v = R::add(v, R::mul(p.cw, w));
+              v = R::add(v, R::mul(p.ce, e));
+              v = R::add(v, R::mul(p.cs, ss[i]));
+              v = R::add(v, R::mul(p.cn, nn[i]));
+              v = R::add(v, R::mul(p.cb, b[r][i]));
+              v = R::add(v, R::mul(p.ct, t[r][i]));
+              o[i] = v;
+            } else {
+              // c + e + w + s + n + b + t, left to right
+              T v = R::add(c[r][i], e);
+              v = R::add(v, w);
+              v = R::add(v, ss[i]);
+              v = R::add(v, nn[i]);
+              v = R::add(v, b[r][i]);
+              v = R::add(v, t[r][i]);
+              o[i] = v;
+            }
+          }
+        }
+        if (ok && y + r < p.dmax1) {
+          T *dst = p.out + (int64_t)z * p.plane + (int64_t)(y + r) * p.row + x;
+          if (vec_in) {
+            st16_global<T>(dst, o);
+          } else {
+#pragma unroll
+            for (int i = 0; i < VEC; ++i)
+              if (x + i >= p.dmin0 && x + i < p.dmax0) dst[i] = o[i];
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < RY; ++r)
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) {
+          b[r][i] = c[r][i];
+          c[r][i] = t[r][i];
+        }
+      cur = nxt;
+      ok = __syncthreads_and(ok);
+      if (!ok) break;
+      // Plane q is consumed by every thread: refill its stage with q + ns.
+      if (tid == 0 && q + ns < nplanes) issue(q + ns);
+    }
   }
   if (!ok && tid == 0) {
     // Give copies still in flight a bounded chance to land before exit.
-    for (int q = 0; q < nplanes; ++q) {
-      const int s = q % ns;
-      mbar_wait(&full[s], (uint32_t)((q / ns) & 1), nullptr, 1024);
-    }
+    for (int s = 0; s < ns; ++s) mbar_wait(&full[s], 0, nullptr, 1024);
   }
+}
+
+template <typename T, int K, int RY>
+cudaError_t launch_ry(const S7Params<T> &p, const MarchConfig &cfg,
+                      const CUtensorMap *tin, int sm_count, cudaStream_t st) {
+  const size_t smem = stencil7_smem_bytes((int)sizeof(T), cfg);
+  static size_t attr_set = 0;     // dynamic shared memory opted in so far
+  static int occ_cached[17][17];  // [warps][ns] -> CTAs per SM (0 = unknown)
+  auto kern = s7_march_kernel<T, K, RY>;
+  if (smem > attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_set = smem;
+  }
+  const int threads = 32 * cfg.warps;
+  int per_sm = cfg.ctas_per_sm;
+  if (per_sm <= 0) {
+    int &oc = occ_cached[cfg.warps][cfg.ns];
+    if (oc == 0) {
+      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oc, kern, threads, smem);
+      if (e != cudaSuccess) return e;
+      if (oc < 1) oc = 1;
+    }
+    per_sm = oc;
+  }
+  int64_t grid = (int64_t)sm_count * per_sm;
+  if (grid > p.units) grid = p.units;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, dim3(32, cfg.warps, 1), smem, st>>>(*tin, p);
+  return cudaGetLastError();
 }
 
 template <typename T, int K>
 cudaError_t launch_t(const Stencil7Args &a, const MarchConfig &cfg,
-                     const CUtensorMap *tin, int *dev_err, cudaStream_t st) {
+                     const CUtensorMap *tin, int *dev_err, int sm_count,
+                     cudaStream_t st) {
   constexpr int VEC = 16 / (int)sizeof(T);
   constexpr int TX = 32 * VEC;
   S7Params<T> p;
@@ -228,7 +311,6 @@ cudaError_t launch_t(const Stencil7Args &a, const MarchConfig &cfg,
   p.dmax1 = a.dom.max[1];
   p.dmax2 = a.dom.max[2];
   p.xbase = (a.dom.min[0] / VEC) * VEC;
-  p.zchunk = cfg.zchunk;
   p.ns = cfg.ns;
   // map argument order ce cw cn cs ct cb cc
   p.ce = (T)a.coef[0];
@@ -243,34 +325,35 @@ cudaError_t launch_t(const Stencil7Args &a, const MarchConfig &cfg,
   const int ey = a.dom.max[1] - a.dom.min[1];
   const int ez = a.dom.max[2] - a.dom.min[2];
   if (ex <= 0 || ey <= 0 || ez <= 0) return cudaSuccess;
-  dim3 grid((ex + TX - 1) / TX, (ey + cfg.ty - 1) / cfg.ty,
-            (ez + cfg.zchunk - 1) / cfg.zchunk);
-  if (grid.y > 65535 || grid.z > 65535 || cfg.ty < 1 || cfg.ty > 16 || cfg.ns < 2)
+  if (cfg.warps < 1 || cfg.warps > 16 || cfg.ns < 2 || cfg.ns > 16)
     return cudaErrorInvalidConfiguration;
-  dim3 block(32, cfg.ty, 1);
-  const size_t smem = stencil7_smem_bytes((int)sizeof(T), cfg);
-  static size_t attr_set = 0;  // dynamic shared memory opted in so far
-  if (smem > attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(s7_march_kernel<T, K>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_set = smem;
+  const int ty = cfg.warps * cfg.rows;
+  p.tiles_x = (ex + TX - 1) / TX;
+  const int tiles_y = (ey + ty - 1) / ty;
+  p.nzd = ez;
+  p.units = (int64_t)p.tiles_x * tiles_y * ez;
+  switch (cfg.rows) {
+    case 1: return launch_ry<T, K, 1>(p, cfg, tin, sm_count, st);
+    case 2: return launch_ry<T, K, 2>(p, cfg, tin, sm_count, st);
+    case 4: return launch_ry<T, K, 4>(p, cfg, tin, sm_count, st);
+    case 8: return launch_ry<T, K, 8>(p, cfg, tin, sm_count, st);
   }
-  s7_march_kernel<T, K><<<grid, block, smem, st>>>(*tin, p);
-  return cudaGetLastError();
+  return cudaErrorInvalidConfiguration;
 }
 
 template <typename T>
 cudaError_t launch_type(const Stencil7Args &a, const MarchConfig &cfg,
-                        const CUtensorMap *tin, int *dev_err, cudaStream_t st) {
+                        const CUtensorMap *tin, int *dev_err, int sm_count,
+                        cudaStream_t st) {
   switch (a.kernel) {
     case kKernelDiffusion7:
-      return launch_t<T, kKernelDiffusion7>(a, cfg, tin, dev_err, st);
+      if constexpr (std::is_floating_point<T>::value)
+        return launch_t<T, kKernelDiffusion7>(a, cfg, tin, dev_err, sm_count, st);
+      return cudaErrorInvalidValue;
     case kKernelSum7:
-      return launch_t<T, kKernelSum7>(a, cfg, tin, dev_err, st);
+      return launch_t<T, kKernelSum7>(a, cfg, tin, dev_err, sm_count, st);
     case kKernelCopy:
-      return launch_t<T, kKernelCopy>(a, cfg, tin, dev_err, st);
+      return launch_t<T, kKernelCopy>(a, cfg, tin, dev_err, sm_count, st);
   }
   return cudaErrorInvalidValue;
 }
@@ -280,22 +363,20 @@ cudaError_t launch_type(const Stencil7Args &a, const MarchConfig &cfg,
 size_t stencil7_smem_bytes(int esz, const MarchConfig &cfg) {
   const int vec = 16 / esz;
   const int w = 32 * vec + 2 * vec;
+  const int ty = cfg.warps * cfg.rows;
   // 128 bytes of slack for aligning the dynamic shared-memory base
   return 128 + (size_t)s7_bar_bytes(cfg.ns) +
-         (size_t)cfg.ns * s7_stage_bytes((uint32_t)(w * (cfg.ty + 2) * esz));
+         (size_t)cfg.ns * s7_stage_bytes((uint32_t)(w * (ty + 2) * esz));
 }
 
 cudaError_t launch_stencil7(const Stencil7Args &a, const MarchConfig &cfg,
-                            const CUtensorMap *tin, int *dev_err,
+                            const CUtensorMap *tin, int *dev_err, int sm_count,
                             cudaStream_t s) {
-  if (a.kernel == kKernelDiffusion7 &&
-      (a.in.type == kInt || a.in.type == kLong))
-    return cudaErrorInvalidValue;
   switch (a.in.type) {
-    case kFloat: return launch_type<float>(a, cfg, tin, dev_err, s);
-    case kDouble: return launch_type<double>(a, cfg, tin, dev_err, s);
-    case kInt: return launch_type<int>(a, cfg, tin, dev_err, s);
-    case kLong: return launch_type<long long>(a, cfg, tin, dev_err, s);
+    case kFloat: return launch_type<float>(a, cfg, tin, dev_err, sm_count, s);
+    case kDouble: return launch_type<double>(a, cfg, tin, dev_err, sm_count, s);
+    case kInt: return launch_type<int>(a, cfg, tin, dev_err, sm_count, s);
+    case kLong: return launch_type<long long>(a, cfg, tin, dev_err, sm_count, s);
   }
   return cudaErrorInvalidValue;
 }

@@ -212,13 +212,15 @@ def test_sum7_types_interior(rt, oracle, dtype):
     assert np.array_equal(a, r1) and np.array_equal(b, r2)
 
 
-@pytest.mark.parametrize("ty,ns,zchunk", [(1, 2, 1), (4, 3, 7), (8, 4, 16),
-                                          (16, 6, 0), (3, 5, 1000)])
-def test_launch_shapes_do_not_change_results(rt, oracle, ty, ns, zchunk):
+@pytest.mark.parametrize("warps,rows,ns,ctas", [
+    (1, 1, 2, 0), (2, 2, 3, 1), (4, 4, 4, 0), (8, 2, 6, 2), (16, 1, 3, 0),
+    (4, 8, 5, 0), (1, 8, 2, 3), (16, 4, 3, 1)])
+def test_launch_shapes_do_not_change_results(rt, oracle, warps, rows, ns, ctas):
     shape = (23, 45, 150)
     init = synth.uniform(shape, 6)
     before = ps.get_launch_shape(ps.PS_KERNEL_DIFFUSION7)
-    ps.set_launch_shape(ps.PS_KERNEL_DIFFUSION7, ty=ty, ns=ns, zchunk=zchunk)
+    ps.set_launch_shape(ps.PS_KERNEL_DIFFUSION7, warps=warps, rows=rows, ns=ns,
+                        ctas_per_sm=ctas)
     try:
         a, _ = run_pingpong(ps.PS_KERNEL_DIFFUSION7, init, ps.full_domain(shape),
                             DIFF_COEF, 2)
@@ -240,8 +242,22 @@ def _himeno_random(shape, seed):
     return arrs
 
 
+HIMENO_SHAPES = [(4, 1, 5, 2, 0), (1, 1, 3, 1, 1), (8, 1, 4, 3, 0), (2, 1, 6, 1, 2)]
+
+
 @pytest.mark.parametrize("shape", [(9, 11, 13), (20, 33, 130), (6, 70, 257)])
-def test_himeno_random_coefficients_bit_exact(rt, oracle, shape):
+@pytest.mark.parametrize("launch", HIMENO_SHAPES)
+def test_himeno_random_coefficients_bit_exact(rt, oracle, shape, launch):
+    for k in (ps.PS_KERNEL_HIMENO19, ps.PS_KERNEL_HIMENO19_GOSA):
+        ps.set_launch_shape(k, *launch)
+    try:
+        _himeno_random_case(oracle, shape)
+    finally:
+        for k in (ps.PS_KERNEL_HIMENO19, ps.PS_KERNEL_HIMENO19_GOSA):
+            ps.set_launch_shape(k, *HIMENO_SHAPES[0])
+
+
+def _himeno_random_case(oracle, shape):
     arrays = _himeno_random(shape, 11)
     gs = himeno_grids(shape, arrays)
     nz, ny, nx = shape
