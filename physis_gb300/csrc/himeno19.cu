@@ -7,9 +7,10 @@
 // (examples/himeno/himenobmtxpa_original.c:331-334), which the Physis port
 // dropped; here it costs no extra HBM traffic.
 //
-// Design (persistent, like the 7-point kernel: the (tile, z) work list with z
-// fastest is split into equal contiguous ranges over SMs x occupancy CTAs;
-// a tile is 128 x warps cells in x,y):
+// Design (persistent, like the 7-point kernel: (z-chunk, tile) work items in
+// chunk-major order taken round-robin by SMs x occupancy CTAs, so resident
+// CTAs march the same z-chunk of neighbouring tiles; a tile is 128 x warps
+// cells in x,y):
 // * p planes with a one-cell y halo and a 4-cell (16-byte) x halo arrive by
 //   TMA into a ring of `ns` stages; the sweep at plane z reads planes z-1, z
 //   and z+1 from the ring (the 19-point stencil needs xy neighbours on all
@@ -43,8 +44,8 @@ struct HParams {
   float *out;
   int64_t row, plane;  // out pitch / plane in elements
   int dmin0, dmin1, dmin2, dmax0, dmax1, dmax2;
-  int xbase, tiles_x, nzd;
-  int64_t units;
+  int xbase, tiles_x, tiles, zlen;
+  int64_t items;
   int nsp, nsc;
   float omega;
   double *partials;
@@ -132,16 +133,11 @@ himeno19_kernel(const __grid_constant__ HimenoMaps maps, const HParams p) {
   const int cen = (row + 1) * kW + 4 + lane * 4;
   const int cidx = row * kTX + lane * 4;
 
-  int64_t u = (int64_t)blockIdx.x * p.units / gridDim.x;
-  const int64_t u_end = (int64_t)(blockIdx.x + 1) * p.units / gridDim.x;
-  while (u < u_end && ok) {
-    const int tile = (int)(u / p.nzd);
-    const int zoff = (int)(u - (int64_t)tile * p.nzd);
-    int64_t seg_end = (int64_t)(tile + 1) * p.nzd;
-    if (seg_end > u_end) seg_end = u_end;
-    const int zs = p.dmin2 + zoff;
-    const int ze = p.dmin2 + (int)(seg_end - (int64_t)tile * p.nzd);
-    u = seg_end;
+  for (int64_t item = blockIdx.x; item < p.items && ok; item += gridDim.x) {
+    const int chunk = (int)(item / p.tiles);
+    const int tile = (int)(item - (int64_t)chunk * p.tiles);
+    const int zs = p.dmin2 + chunk * p.zlen;
+    const int ze = min(zs + p.zlen, p.dmax2);
     const int x0 = p.xbase + (tile % p.tiles_x) * kTX;
     const int y0 = p.dmin1 + (tile / p.tiles_x) * TY;
     const int nplanes = ze - zs + 2;  // p planes zs-1 .. ze
@@ -330,9 +326,7 @@ cudaError_t launch_himeno19(const Himeno19Args &a, const MarchConfig &cfg,
       cfg.ns2 > 8)
     return cudaErrorInvalidConfiguration;
   p.tiles_x = (ex + kTX - 1) / kTX;
-  const int tiles_y = (ey + cfg.warps - 1) / cfg.warps;
-  p.nzd = ez;
-  p.units = (int64_t)p.tiles_x * tiles_y * ez;
+  p.tiles = p.tiles_x * ((ey + cfg.warps - 1) / cfg.warps);
   const size_t smem = himeno19_smem_bytes(cfg);
   // Opt in to the dynamic shared memory this launch needs (the kernel also
   // has a little static shared memory, so the opt-in is the exact size).
@@ -357,8 +351,11 @@ cudaError_t launch_himeno19(const Himeno19Args &a, const MarchConfig &cfg,
     }
     per_sm = oc;
   }
-  int64_t grid = (int64_t)sm_count * per_sm;
-  if (grid > p.units) grid = p.units;
+  const int resident = sm_count * per_sm;
+  p.zlen = choose_zchunk(p.tiles, ez, resident);
+  p.items = (int64_t)p.tiles * ((ez + p.zlen - 1) / p.zlen);
+  int64_t grid = resident;
+  if (grid > p.items) grid = p.items;
   if (a.gosa && grid > sink.max_partials) grid = sink.max_partials;
   kern<<<(unsigned)grid, dim3(32, cfg.warps, 1), smem, s>>>(maps, p);
   return cudaGetLastError();

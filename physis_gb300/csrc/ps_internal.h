@@ -54,6 +54,13 @@ struct MarchConfig {
   int ctas_per_sm;
 };
 
+// Chunk length (planes) for a z-march over `tiles` tiles and `nz` planes by
+// `resident` concurrently resident CTAs: maximises the fraction of CTA time
+// spent on useful planes, counting whole rounds of `resident` items and one
+// extra plane of pipeline start-up per item.  Shared by the marching kernels
+// (march.cpp).
+int choose_zchunk(int tiles, int nz, int resident);
+
 // Builds a 3D tiled tensor map over g with box {box_w, box_h, 1} elements.
 // Implemented in runtime.cpp (driver entry point looked up at run time).
 bool make_tmap_3d(CUtensorMap *map, const GridView &g, int box_w, int box_h);

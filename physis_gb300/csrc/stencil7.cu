@@ -9,11 +9,12 @@
 //   COPY        out = in over the domain
 //
 // Design.  A tile is 32 lanes x 16 bytes wide in x (128 floats, 64 doubles)
-// and WARPS*RY rows high in y.  Work is the list of (tile, z) pairs with z
-// fastest; a persistent grid of SMs x occupancy CTAs splits that list into
-// equal contiguous ranges, so every CTA marches through one or two z-segments
-// of equal total length (no partial last wave) and CTAs that run at the same
-// time work on neighbouring tiles at the same depths (halos hit in L2).
+// and WARPS*RY rows high in y.  Work items are (z-chunk, tile) pairs in
+// chunk-major order; a persistent grid of SMs x occupancy CTAs takes items
+// round-robin, so the CTAs resident at any moment march the same z-chunk of
+// neighbouring tiles side by side and every halo row or column a tile reads
+// is read from L2 by its neighbour at about the same time (HBM sees each byte
+// once).  The host picks the chunk length that fills whole rounds.
 // * Each z-plane of the tile plus a one-row y halo and a 16-byte x halo
 //   (TMA wants 16-byte aligned x) arrives by one TMA 3D box load into a
 //   ring of `ns` shared-memory stages; one mbarrier per stage signals
@@ -46,8 +47,9 @@ struct S7Params {
   int dmin0, dmin1, dmin2, dmax0, dmax1, dmax2;
   int xbase;      // x of the first tile (multiple of VEC)
   int tiles_x;    // tiles per y-band
-  int nzd;        // planes in the domain
-  int64_t units;  // tiles * nzd
+  int tiles;      // tiles_x * tiles per x-column
+  int zlen;       // planes per z-chunk
+  int64_t items;  // tiles * chunks
   int ns;
   T cc, cw, ce, cs, cn, cb, ct;  // expression order of DIFFUSION7
   int *err;
@@ -94,19 +96,14 @@ s7_march_kernel(const __grid_constant__ CUtensorMap tin, const S7Params<T> p) {
   uint32_t cphase = 0;
   bool ok = true;
 
-  int64_t u = (int64_t)blockIdx.x * p.units / gridDim.x;
-  const int64_t u_end = (int64_t)(blockIdx.x + 1) * p.units / gridDim.x;
   const int rows0 = warp * RY;                          // first own row in the tile
   const int cen0 = (rows0 + 1) * W + VEC + lane * VEC;  // own first row, centre
 
-  while (u < u_end && ok) {
-    const int tile = (int)(u / p.nzd);
-    const int zoff = (int)(u - (int64_t)tile * p.nzd);
-    int64_t seg_end = (int64_t)(tile + 1) * p.nzd;
-    if (seg_end > u_end) seg_end = u_end;
-    const int zs = p.dmin2 + zoff;
-    const int ze = p.dmin2 + (int)(seg_end - (int64_t)tile * p.nzd);
-    u = seg_end;
+  for (int64_t item = blockIdx.x; item < p.items && ok; item += gridDim.x) {
+    const int chunk = (int)(item / p.tiles);
+    const int tile = (int)(item - (int64_t)chunk * p.tiles);
+    const int zs = p.dmin2 + chunk * p.zlen;
+    const int ze = min(zs + p.zlen, p.dmax2);
     const int x0 = p.xbase + (tile % p.tiles_x) * TX;
     const int y0 = p.dmin1 + (tile / p.tiles_x) * TY;
     const int nplanes = ze - zs + 2;  // planes zs-1 .. ze
@@ -261,7 +258,7 @@ s7_march_kernel(const __grid_constant__ CUtensorMap tin, const S7Params<T> p) {
 }
 
 template <typename T, int K, int RY>
-cudaError_t launch_ry(const S7Params<T> &p, const MarchConfig &cfg,
+cudaError_t launch_ry(S7Params<T> p, int tiles, int nzd, const MarchConfig &cfg,
                       const CUtensorMap *tin, int sm_count, cudaStream_t st) {
   const size_t smem = stencil7_smem_bytes((int)sizeof(T), cfg);
   static size_t attr_set = 0;     // dynamic shared memory opted in so far
@@ -284,8 +281,12 @@ cudaError_t launch_ry(const S7Params<T> &p, const MarchConfig &cfg,
     }
     per_sm = oc;
   }
-  int64_t grid = (int64_t)sm_count * per_sm;
-  if (grid > p.units) grid = p.units;
+  const int resident = sm_count * per_sm;
+  p.tiles = tiles;
+  p.zlen = choose_zchunk(tiles, nzd, resident);
+  p.items = (int64_t)tiles * ((nzd + p.zlen - 1) / p.zlen);
+  int64_t grid = resident;
+  if (grid > p.items) grid = p.items;
   if (grid < 1) grid = 1;
   kern<<<(unsigned)grid, dim3(32, cfg.warps, 1), smem, st>>>(*tin, p);
   return cudaGetLastError();
@@ -329,14 +330,12 @@ cudaError_t launch_t(const Stencil7Args &a, const MarchConfig &cfg,
     return cudaErrorInvalidConfiguration;
   const int ty = cfg.warps * cfg.rows;
   p.tiles_x = (ex + TX - 1) / TX;
-  const int tiles_y = (ey + ty - 1) / ty;
-  p.nzd = ez;
-  p.units = (int64_t)p.tiles_x * tiles_y * ez;
+  const int tiles = p.tiles_x * ((ey + ty - 1) / ty);
   switch (cfg.rows) {
-    case 1: return launch_ry<T, K, 1>(p, cfg, tin, sm_count, st);
-    case 2: return launch_ry<T, K, 2>(p, cfg, tin, sm_count, st);
-    case 4: return launch_ry<T, K, 4>(p, cfg, tin, sm_count, st);
-    case 8: return launch_ry<T, K, 8>(p, cfg, tin, sm_count, st);
+    case 1: return launch_ry<T, K, 1>(p, tiles, ez, cfg, tin, sm_count, st);
+    case 2: return launch_ry<T, K, 2>(p, tiles, ez, cfg, tin, sm_count, st);
+    case 4: return launch_ry<T, K, 4>(p, tiles, ez, cfg, tin, sm_count, st);
+    case 8: return launch_ry<T, K, 8>(p, tiles, ez, cfg, tin, sm_count, st);
   }
   return cudaErrorInvalidConfiguration;
 }
