@@ -340,17 +340,16 @@ cudaError_t launch_himeno19(const Himeno19Args &a, const MarchConfig &cfg,
     if (e != cudaSuccess) return e;
     have = smem;
   }
-  int per_sm = cfg.ctas_per_sm;
-  if (per_sm <= 0) {
-    int &oc = occ[a.gosa ? 1 : 0][cfg.warps][cfg.ns][cfg.ns2];
-    if (oc == 0) {
-      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oc, kern, 32 * cfg.warps,
-                                                                    smem);
-      if (e != cudaSuccess) return e;
-      if (oc < 1) oc = 1;
-    }
-    per_sm = oc;
+  // The round-robin schedule assumes every CTA is resident: never launch
+  // more per SM than fit.
+  int &oc = occ[a.gosa ? 1 : 0][cfg.warps][cfg.ns][cfg.ns2];
+  if (oc == 0) {
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oc, kern, 32 * cfg.warps,
+                                                                  smem);
+    if (e != cudaSuccess) return e;
+    if (oc < 1) oc = 1;
   }
+  const int per_sm = (cfg.ctas_per_sm > 0 && cfg.ctas_per_sm < oc) ? cfg.ctas_per_sm : oc;
   const int resident = sm_count * per_sm;
   p.zlen = choose_zchunk(p.tiles, ez, resident);
   p.items = (int64_t)p.tiles * ((ez + p.zlen - 1) / p.zlen);

@@ -617,7 +617,7 @@ void PSInitV(int trace) {
   for (int i = 0; i < kNumEvents; ++i) cudaEventCreate(&r->events[i]);
   // Default launch shapes (the autotuner may replace them):
   // {warps, rows per thread, ring stages, second-ring stages, CTAs per SM}.
-  for (int k = 0; k < kNumKernels; ++k) r->shapes[k] = MarchConfig{4, 4, 4, 0, 0};
+  for (int k = 0; k < kNumKernels; ++k) r->shapes[k] = MarchConfig{8, 2, 4, 0, 0};
   r->shapes[PS_KERNEL_HIMENO19] = MarchConfig{4, 1, 5, 2, 0};
   r->shapes[PS_KERNEL_HIMENO19_GOSA] = MarchConfig{4, 1, 5, 2, 0};
   cudaDeviceSynchronize();

@@ -271,16 +271,15 @@ cudaError_t launch_ry(S7Params<T> p, int tiles, int nzd, const MarchConfig &cfg,
     attr_set = smem;
   }
   const int threads = 32 * cfg.warps;
-  int per_sm = cfg.ctas_per_sm;
-  if (per_sm <= 0) {
-    int &oc = occ_cached[cfg.warps][cfg.ns];
-    if (oc == 0) {
-      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oc, kern, threads, smem);
-      if (e != cudaSuccess) return e;
-      if (oc < 1) oc = 1;
-    }
-    per_sm = oc;
+  // The round-robin schedule assumes every CTA is resident: never launch
+  // more per SM than fit.
+  int &oc = occ_cached[cfg.warps][cfg.ns];
+  if (oc == 0) {
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oc, kern, threads, smem);
+    if (e != cudaSuccess) return e;
+    if (oc < 1) oc = 1;
   }
+  const int per_sm = (cfg.ctas_per_sm > 0 && cfg.ctas_per_sm < oc) ? cfg.ctas_per_sm : oc;
   const int resident = sm_count * per_sm;
   p.tiles = tiles;
   p.zlen = choose_zchunk(tiles, nzd, resident);
