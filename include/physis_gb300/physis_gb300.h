@@ -129,7 +129,37 @@ typedef struct {
 void PSSetLaunchShape(int kernel, const PSLaunchShape *shape);
 void PSGetLaunchShape(int kernel, PSLaunchShape *shape);
 
-/* ---- 5. Test hooks ------------------------------------------------------ */
+/* ---- 5. Reduction for callers that cannot allocate --------------------- */
+
+/* No counterpart in the reference.  PSReduce over a grid that the caller
+ * holds in device memory, for callers that must not allocate GPU memory:
+ * code recording a CUDA graph or stream capture (an allocation cannot be
+ * captured and would synchronise the device), latency-bound loops that
+ * cannot afford the synchronisation an allocation implies, and processes
+ * whose device memory is already owned by another allocator.  It needs no
+ * PSInit and calls no cudaMalloc, cudaFree or allocating library routine.
+ *
+ * data   : element (x,y,z) at data + (z*ny + y)*pitch + x*esz; 16-byte
+ *          aligned, pitch a multiple of 16 bytes (grids of this library
+ *          qualify: PSGridDevicePtr / PSGridPitch);
+ * type   : PS_FLOAT, PS_DOUBLE, PS_INT or PS_LONG; op: a PSReduceOp;
+ * result : 8 bytes of device memory receiving an FP64 value (float and
+ *          double grids) or a 64-bit integer (int grids sign-extended from
+ *          the 32-bit wrapped result, long grids as is);
+ * stream : a cudaStream_t (NULL: the legacy default stream).  The call is
+ *          asynchronous on that stream.
+ * Scratch: a static device array of 2048 per-CTA partials plus a ticket,
+ * held by every GPU that loads the library until exit.  A launch that
+ * would need more partial slots than that is rejected (PS_ERR_UNSUPPORTED;
+ * a 152-SM GB300 needs at most 1216).  All calls share the array: calls
+ * whose work overlaps on the GPU race.  The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) and loads the module
+ * there; make that first call before any stream capture.
+ * Returns PS_OK or an error code (also recorded for PSGetLastError). */
+int PSReduceNoAlloc(const void *data, size_t pitch, int nx, int ny, int nz, int type,
+                    int op, void *result, void *stream);
+
+/* ---- 6. Test hooks ------------------------------------------------------ */
 
 /* The next `n` device allocations fail as if the GPU were out of memory. */
 void PSTestFailNextAllocs(int n);

@@ -49,7 +49,7 @@ PSReduceGridF64 PSGetLastError PSGetLastErrorString PSGetErrorName PSClearError
 PSGridDevicePtr PSGridPitch PSGridElemSize PSGridType PSGridCopyinAsync
 PSGridCopyoutAsync PSHostAlloc PSHostFree PSSynchronize PSGetStream
 PSEventRecord PSEventElapsedMs PSGetLaunchCount PSGetSMCount PSSetLaunchShape
-PSGetLaunchShape PSTestFailNextAllocs PSTestDeviceWaitTimeout""".split()
+PSGetLaunchShape PSTestFailNextAllocs PSTestDeviceWaitTimeout PSReduceNoAlloc""".split()
 
 
 class PSDomain(ctypes.Structure):
@@ -135,6 +135,8 @@ def lib():
     L.PSGetLaunchShape.argtypes = [i, ctypes.POINTER(PSLaunchShape)]
     L.PSTestFailNextAllocs.argtypes = [i]
     L.PSTestDeviceWaitTimeout.argtypes = [ctypes.c_uint]
+    L.PSReduceNoAlloc.argtypes = [vp, ctypes.c_size_t, i, i, i, i, i, vp, vp]
+    L.PSReduceNoAlloc.restype = i
     _lib = L
     return L
 

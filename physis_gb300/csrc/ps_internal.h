@@ -106,6 +106,11 @@ cudaError_t launch_reduce(const GridView &g, int op, uint64_t *partials,
                           int num_ctas, unsigned *ticket, uint64_t *result,
                           int *dev_err, cudaStream_t s);
 
+// The reduction above with its scratch in a static device array (no
+// allocation).  Returns PS_OK or a PSErrorCode value; *why explains a failure.
+int reduce_noalloc(const void *data, size_t pitch, int nx, int ny, int nz, int type,
+                   int op, void *result, cudaStream_t stream, const char **why);
+
 // ---- Test support (failure detection without a GPU fault) ----------------
 // Runs one CTA that waits on an mbarrier that nothing completes, with a
 // short iteration limit; the wait gives up and sets kDevErrWaitTimeout.

@@ -17,6 +17,7 @@
 // same way).  The result is deterministic run to run.
 #include <type_traits>
 
+#include "physis_gb300/physis_gb300.h"
 #include "ps_device.cuh"
 #include "ps_internal.h"
 
@@ -259,6 +260,107 @@ cudaError_t launch_wait_timeout_probe(int *dev_err, uint32_t limit,
                                       cudaStream_t s) {
   wait_timeout_probe_kernel<<<1, 32, 0, s>>>(dev_err, limit);
   return cudaGetLastError();
+}
+
+// ---- PSReduceNoAlloc: the same reduction with statically placed scratch ----
+//
+// For callers that must not allocate device memory (see the declaration in
+// physis_gb300.h).  The per-CTA partials and the last-CTA ticket live in this
+// file-scope array instead of runtime-allocated buffers; it belongs to the
+// loaded module, so every GPU that loads the library holds these 16 KiB
+// until the process exits.  All calls share it: calls whose work overlaps on
+// the GPU (other streams, or the same array from another host thread) race.
+constexpr int kNoAllocMaxPartials = 2048;
+static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocMaxPartials + 2];
+
+namespace {
+
+// Device address of g_noalloc_scratch and SM count, per device ordinal,
+// looked up on the first call made with that device current.
+struct NoAllocDevice {
+  bool ready;
+  uint64_t *scratch;
+  int sm_count;
+};
+constexpr int kNoAllocMaxDevices = 64;
+NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
+
+}  // namespace
+
+int reduce_noalloc(const void *data, size_t pitch, int nx, int ny, int nz, int type,
+                   int op, void *result, cudaStream_t stream, const char **why) {
+  // Arguments first: these checks need no GPU.
+  const int esz = (type == kFloat || type == kInt) ? 4 : (type == kDouble || type == kLong) ? 8 : 0;
+  if (!esz) { *why = "unknown element type"; return PS_ERR_INVALID_ARGUMENT; }
+  if (op < kMax || op > kProd) { *why = "unknown reduction op"; return PS_ERR_INVALID_ARGUMENT; }
+  if (!data || !result) { *why = "NULL data or result pointer"; return PS_ERR_INVALID_ARGUMENT; }
+  if (nx <= 0 || ny <= 0 || nz <= 0) { *why = "grid sizes must be positive"; return PS_ERR_INVALID_ARGUMENT; }
+  if (pitch < (size_t)nx * esz || pitch % 16 != 0) {
+    *why = "pitch must cover a row and be a multiple of 16 bytes";
+    return PS_ERR_INVALID_ARGUMENT;
+  }
+  if ((reinterpret_cast<uintptr_t>(data) & 15u) != 0 ||
+      (reinterpret_cast<uintptr_t>(result) & 7u) != 0) {
+    *why = "data must be 16-byte and result 8-byte aligned";
+    return PS_ERR_INVALID_ARGUMENT;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+    cudaGetLastError();
+    *why = "no usable current CUDA device";
+    return PS_ERR_NO_DEVICE;
+  }
+  NoAllocDevice &d = g_noalloc_dev[dev];
+  if (!d.ready) {
+    // Set-up, once per device, with that device current: the host-side name
+    // g_noalloc_scratch is not a device address, so look the address up.
+    uint64_t *ptr = nullptr;
+    if (cudaGetSymbolAddress(reinterpret_cast<void **>(&ptr), g_noalloc_scratch) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      *why = "cudaGetSymbolAddress failed for the static scratch array";
+      return PS_ERR_CUDA;
+    }
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+      cudaGetLastError();
+      *why = "cannot query the SM count";
+      return PS_ERR_CUDA;
+    }
+    d.scratch = ptr;
+    d.sm_count = sms;
+    d.ready = true;
+  }
+  GridView g;
+  g.ptr = const_cast<void *>(data);
+  g.pitch = (int64_t)pitch;
+  g.nx = nx;
+  g.ny = ny;
+  g.nz = nz;
+  g.type = type;
+  g.esz = esz;
+  // Same CTA count as the allocating entry point, so both give the same bits.
+  const int n = reduce_num_ctas(g, d.sm_count);
+  if (n > kNoAllocMaxPartials) {
+    *why = "the launch needs more per-CTA partial slots than the static scratch holds (2048)";
+    return PS_ERR_UNSUPPORTED;
+  }
+  uint64_t *partials = d.scratch;
+  unsigned *ticket = reinterpret_cast<unsigned *>(d.scratch + kNoAllocMaxPartials);
+  // The ticket must start at zero; an interrupted earlier call could have
+  // left it set.  cudaMemsetAsync allocates nothing.
+  if (cudaMemsetAsync(ticket, 0, sizeof(unsigned), stream) != cudaSuccess) {
+    cudaGetLastError();
+    *why = "cudaMemsetAsync of the ticket failed";
+    return PS_ERR_CUDA;
+  }
+  cudaError_t e = launch_reduce(g, op, partials, n, ticket, static_cast<uint64_t *>(result),
+                                nullptr, stream);
+  if (e != cudaSuccess) {
+    *why = cudaGetErrorString(e);
+    return PS_ERR_CUDA;
+  }
+  return PS_OK;
 }
 
 }  // namespace psg

@@ -1001,6 +1001,15 @@ void PSGetLaunchShape(int kernel, PSLaunchShape *shape) {
   shape->ctas_per_sm = c.ctas_per_sm;
 }
 
+int PSReduceNoAlloc(const void *data, size_t pitch, int nx, int ny, int nz, int type,
+                    int op, void *result, void *stream) {
+  const char *why = "";
+  const int code = psg::reduce_noalloc(data, pitch, nx, ny, nz, type, op, result,
+                                       static_cast<cudaStream_t>(stream), &why);
+  if (code != PS_OK) fail(code, "PSReduceNoAlloc: %s", why);
+  return code;
+}
+
 void PSTestFailNextAllocs(int n) {
   if (need_rt("PSTestFailNextAllocs")) rt->fail_allocs = n;
 }
