@@ -351,6 +351,149 @@ def run_gpu(args, dist):
     g2.free()
 
 
+# ---------------------------------------------------------------------------
+# Himeno 19-point Jacobi with the fused residual (config 3)
+# ---------------------------------------------------------------------------
+
+HIM = (257, 257, 513)  # nx, ny, nz
+HIM_BYTES_PER_LUP = 56
+HIM_METRIC = ("GLUPS, Himeno 19-point Jacobi fp32 257x257x513 with the fused "
+              "sum-of-squares residual per sweep")
+
+
+def himeno_arrays(nx, ny, nz):
+    """Set-up of himenobmtxpa_physis.c:126-141: p = k^2/(K-1)^2 (k = z),
+    a0=a1=a2=1, a3=1/6, b*=0, c*=1, bnd 1 inside / 0 on the faces, wrk1=0,
+    in the map's grid order p0 p1 a0 a1 a2 a3 b0 b1 b2 c0 c1 c2 bnd wrk1."""
+    shape = (nz, ny, nx)
+    z = np.arange(nz, dtype=np.int64)
+    pz = (z * z).astype(np.float32) / np.float32((nz - 1) * (nz - 1))
+    p0 = np.ascontiguousarray(np.broadcast_to(pz[:, None, None], shape))
+    one = np.ones(shape, np.float32)
+    zero = np.zeros(shape, np.float32)
+    bnd = np.zeros(shape, np.float32)
+    bnd[1:-1, 1:-1, 1:-1] = 1.0
+    return [p0, p0.copy(), one, one, one, np.full(shape, np.float32(1.0 / 6.0)),
+            zero, zero, zero, one, one, one, bnd, zero]
+
+
+def run_gpu_himeno(args, dist):
+    os.environ.setdefault("PS_DEVICE", str(dist.local))
+    import physis_gb300 as ps
+    ps.init()
+    L = ps.lib()
+    nx, ny, nz = HIM
+    shape = (nz, ny, nx)
+    arrays = himeno_arrays(nx, ny, nz)
+    gs = [ps.Grid(shape) for _ in range(14)]
+    for g, a in zip(gs, arrays):
+        g.copyin(a)
+    dom = ps.domain(1, nx - 1, 1, ny - 1, 1, nz - 1)
+    omega = np.float32(0.8)
+    k = ps.PS_KERNEL_HIMENO19_GOSA
+    m1 = ps.stencil_map(k, dom, gs, [omega])
+    m2 = ps.stencil_map(k, dom, [gs[1], gs[0]] + gs[2:], [omega])
+    K, W = args.steps, args.warmup
+
+    def sweeps(n):
+        pairs, rem = divmod(n, 2)
+        if pairs:
+            ps.stencil_run([m1, m2], pairs)
+        if rem:
+            ps.stencil_run([m1], 1)
+
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    sweeps(W)
+    ps.synchronize()
+    dist.barrier()
+    n0 = ps.launch_count()
+    L.PSEventRecord(0)
+    sweeps(K)
+    L.PSEventRecord(1)
+    ps.synchronize()
+    ms = L.PSEventElapsedMs(0, 1)
+    launches = ps.launch_count() - n0
+    dist.barrier()
+    clk = clocks.stop()
+    lups = float(nx - 2) * (ny - 2) * (nz - 2)
+    ms_max = dist.reduce(ms, "MAX")
+    value = dist.ws * lups * K / (ms_max / 1e3) / 1e9
+
+    # end to end: copy p in (pinned), K sweeps each returning its residual to
+    # the host through PSReduce's kernel form, copy p out (pinned)
+    import ctypes
+    nbytes = nx * ny * nz * 4
+    hin = L.PSHostAlloc(nbytes)
+    hout = L.PSHostAlloc(nbytes)
+    ctypes.memmove(hin, arrays[0].ctypes.data, nbytes)
+    dist.barrier()
+    t0 = time.perf_counter()
+    L.PSGridCopyin(gs[0].handle, hin)
+    gosa = None
+    for s_ in range(K):
+        a, b = (gs[0], gs[1]) if s_ % 2 == 0 else (gs[1], gs[0])
+        gosa = ps.reduce_kernel(ps.PS_SUM, k, dom, [a, b] + gs[2:], [omega])
+    L.PSGridCopyout((gs[0] if K % 2 == 0 else gs[1]).handle, hout)
+    e2e_s = time.perf_counter() - t0
+    ps.check()
+    e2e_max = dist.reduce(e2e_s, "MAX")
+    L.PSHostFree(hin)
+    L.PSHostFree(hout)
+
+    peak, peak_kind = measured_peaks()
+    achieved = lups * HIM_BYTES_PER_LUP / (ms / K / 1e3) / 1e9
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        from oracle import pyoracle
+        nt = pyoracle.num_threads()
+        g = [a.copy() for a in arrays]
+        zs = 64
+        d = (1, nx - 1, 1, ny - 1, 1, zs + 1)
+        pyoracle.himeno19(g, d, omega, nthreads=nt)
+        t0 = time.perf_counter()
+        n = 0
+        while time.perf_counter() - t0 < args.cpu_seconds:
+            pyoracle.himeno19(g, d, omega, nthreads=nt)
+            g[0], g[1] = g[1], g[0]
+            n += 1
+        el = time.perf_counter() - t0
+        cpu = {"value": (nx - 2) * (ny - 2) * zs * n / el / 1e9, "unit": "GLUPS",
+               "cores": nt, "kind": "port",
+               "sample": f"{n} REF-order sweeps of z in [1,{zs + 1}) "
+                         f"(oracle/ps_oracle.c, OpenMP over z)"}
+    if dist.rank == 0:
+        shape_used = ps.get_launch_shape(k)
+        line = {
+            "metric": HIM_METRIC, "value": value, "unit": "GLUPS",
+            "n_gpus": dist.ws, "steps": K, "warmup": W,
+            "ms_per_step": ms_max / K, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "Himeno benchmark set-up (deterministic), omega 0.8",
+            "config": {"workload": "Himeno 19-point Jacobi 257x257x513, interior "
+                                   "255x255x511, residual fused per sweep",
+                       "grid": [nx, ny, nz], "l2": "14 grids of 139 MB, > L2",
+                       "launch_shape": {"warps": shape_used[0], "ns": shape_used[2],
+                                        "ns2": shape_used[3]},
+                       "e2e_job": "PSGridCopyin(p) + K PSReduce kernel-form sweeps "
+                                  "(residual to host each) + PSGridCopyout(p)"},
+            "e2e": {"value": dist.ws * lups * K / e2e_max / 1e9, "unit": "GLUPS",
+                    "h2d_bytes_per_step": nbytes / K,
+                    "d2h_bytes_per_step": nbytes / K + 4,
+                    "job_seconds": e2e_max, "last_gosa": float(gosa)},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "peak_source": peak_kind,
+                         "bytes_per_lup": HIM_BYTES_PER_LUP},
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    for g in gs:
+        g.free()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -365,6 +508,10 @@ def main():
     ap.add_argument("--ctas", type=int, default=0)
     ap.add_argument("--n", type=int, default=512,
                     help="grid edge (default 512; smaller only for profiling)")
+    ap.add_argument("--workload", default="diffusion",
+                    choices=["diffusion", "himeno"],
+                    help="diffusion: 7-point 512^3 (the headline); himeno: "
+                         "19-point Jacobi 257x257x513 with fused residual")
     args = ap.parse_args()
     global N
     N = args.n
@@ -374,6 +521,8 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, dist)
+        elif args.workload == "himeno":
+            run_gpu_himeno(args, dist)
         else:
             run_gpu(args, dist)
     finally:
