@@ -129,6 +129,16 @@ typedef struct {
 void PSSetLaunchShape(int kernel, const PSLaunchShape *shape);
 void PSGetLaunchShape(int kernel, PSLaunchShape *shape);
 
+/* Temporal blocking: a PSStencilRun of the pair (g1 -> g2, g2 -> g1) of one
+ * full-grid PS_KERNEL_DIFFUSION7 stencil runs k time steps per pass over
+ * HBM (k = 1: off; at most 5 for float grids, 3 for double).  Results are
+ * bit-identical to k plain steps and g1/g2 end holding the same steps as
+ * with plain sweeps (their device storage may be exchanged).  `shape`
+ * (warps <= 8, rows 1/2/4, ns; NULL keeps the current one) is the pass's own
+ * launch shape; its tile height warps*rows must exceed 2*(k-1). */
+void PSSetTemporalBlocking(int kernel, int k, const PSLaunchShape *shape);
+void PSGetTemporalBlocking(int kernel, int *k, PSLaunchShape *shape);
+
 /* ---- 5. Reduction for callers that cannot allocate --------------------- */
 
 /* No counterpart in the reference.  PSReduce over a grid that the caller

@@ -49,7 +49,8 @@ PSReduceGridF64 PSGetLastError PSGetLastErrorString PSGetErrorName PSClearError
 PSGridDevicePtr PSGridPitch PSGridElemSize PSGridType PSGridCopyinAsync
 PSGridCopyoutAsync PSHostAlloc PSHostFree PSSynchronize PSGetStream
 PSEventRecord PSEventElapsedMs PSGetLaunchCount PSGetSMCount PSSetLaunchShape
-PSGetLaunchShape PSTestFailNextAllocs PSTestDeviceWaitTimeout PSReduceNoAlloc""".split()
+PSGetLaunchShape PSTestFailNextAllocs PSTestDeviceWaitTimeout PSReduceNoAlloc
+PSSetTemporalBlocking PSGetTemporalBlocking""".split()
 
 
 class PSDomain(ctypes.Structure):
@@ -135,6 +136,8 @@ def lib():
     L.PSGetLaunchShape.argtypes = [i, ctypes.POINTER(PSLaunchShape)]
     L.PSTestFailNextAllocs.argtypes = [i]
     L.PSTestDeviceWaitTimeout.argtypes = [ctypes.c_uint]
+    L.PSSetTemporalBlocking.argtypes = [i, i, ctypes.POINTER(PSLaunchShape)]
+    L.PSGetTemporalBlocking.argtypes = [i, ctypes.POINTER(i), ctypes.POINTER(PSLaunchShape)]
     L.PSReduceNoAlloc.argtypes = [vp, ctypes.c_size_t, i, i, i, i, i, vp, vp]
     L.PSReduceNoAlloc.restype = i
     _lib = L
@@ -281,6 +284,21 @@ def get_launch_shape(kernel):
     sh = PSLaunchShape()
     lib().PSGetLaunchShape(kernel, ctypes.byref(sh))
     return sh.warps, sh.rows, sh.ns, sh.ns2, sh.ctas_per_sm
+
+
+def set_temporal(kernel, k, warps=0, rows=0, ns=0, ctas_per_sm=0):
+    """Temporal blocking depth k (1 = off) and the passes' launch shape."""
+    sh = PSLaunchShape(warps, rows, ns, 0, ctas_per_sm)
+    lib().PSSetTemporalBlocking(kernel, k, ctypes.byref(sh))
+    check()
+
+
+def get_temporal(kernel):
+    """(k, (warps, rows, ns, ctas_per_sm)) of a kernel's temporal blocking."""
+    k = ctypes.c_int(0)
+    sh = PSLaunchShape()
+    lib().PSGetTemporalBlocking(kernel, ctypes.byref(k), ctypes.byref(sh))
+    return k.value, (sh.warps, sh.rows, sh.ns, sh.ctas_per_sm)
 
 
 def launch_count():

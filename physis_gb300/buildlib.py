@@ -15,7 +15,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libphysis_gb300.so")
-SOURCES = ["runtime.cpp", "march.cpp", "stencil7.cu", "himeno19.cu", "reduce.cu"]
+SOURCES = ["runtime.cpp", "march.cpp", "stencil7.cu", "temporal7.cu", "himeno19.cu",
+           "reduce.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -5,11 +5,15 @@
 namespace psg {
 
 int choose_zchunk(int tiles, int nz, int resident) {
+  return choose_zchunk_overhead(tiles, nz, resident, 1);
+}
+
+int choose_zchunk_overhead(int tiles, int nz, int resident, int overhead) {
   if (nz <= 1 || tiles <= 0 || resident <= 0) return nz > 0 ? nz : 1;
   int best_len = nz;
   double best = -1.0;
   // Items are (chunk, tile) pairs taken in rounds of `resident`; a round
-  // costs the planes of its longest item plus one plane of start-up.
+  // costs the planes of its longest item plus `overhead` planes of start-up.
   for (int chunks = 1; chunks <= nz; ++chunks) {
     const int len = (nz + chunks - 1) / chunks;
     const int real_chunks = (nz + len - 1) / len;
@@ -17,7 +21,7 @@ int choose_zchunk(int tiles, int nz, int resident) {
     const long long items = (long long)tiles * chunks;
     const long long rounds = (items + resident - 1) / resident;
     const double useful = (double)tiles * nz;
-    const double cost = (double)rounds * resident * (len + 1);
+    const double cost = (double)rounds * resident * (len + overhead);
     const double eff = useful / cost;
     // prefer longer chunks when efficiency ties (fewer halo planes)
     if (eff > best + 1e-9) {

@@ -60,6 +60,9 @@ struct MarchConfig {
 // extra plane of pipeline start-up per item.  Shared by the marching kernels
 // (march.cpp).
 int choose_zchunk(int tiles, int nz, int resident);
+// The same with `overhead` start-up planes per item (a k-step temporal pass
+// reads 2k extra input planes per item).
+int choose_zchunk_overhead(int tiles, int nz, int resident, int overhead);
 
 // Builds a 3D tiled tensor map over g with box {box_w, box_h, 1} elements.
 // Implemented in runtime.cpp (driver entry point looked up at run time).
@@ -77,6 +80,19 @@ size_t stencil7_smem_bytes(int esz, const MarchConfig &cfg);
 cudaError_t launch_stencil7(const Stencil7Args &a, const MarchConfig &cfg,
                             const CUtensorMap *tin, int *dev_err, int sm_count,
                             cudaStream_t s);
+
+// ---- Temporal blocking of DIFFUSION7 (temporal7.cu) -----------------------
+// One pass: out = k clamped diffusion steps of in over the whole grid.
+struct Temporal7Args {
+  GridView in, out;
+  double coef[7];  // map argument order: ce cw cn cs ct cb cc
+  int k;
+};
+int temporal7_max_k(int esz);
+size_t temporal7_smem_bytes(int esz, const MarchConfig &cfg, int k);
+cudaError_t launch_temporal7(const Temporal7Args &a, const MarchConfig &cfg,
+                             const CUtensorMap *tin, int *dev_err, int sm_count,
+                             cudaStream_t s);
 
 // ---- Himeno 19-point Jacobi (himeno19.cu) --------------------------------
 struct Himeno19Args {

@@ -16,6 +16,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cstdarg>
 #include <cstdio>
@@ -42,8 +43,10 @@ constexpr int kNumEvents = 64;
 constexpr int kMaxPartials = 1 << 16;
 constexpr int kNumKernels = 8;
 
+// Tensor maps are cached per (device view, box); an entry is dropped when
+// its grid is freed.
 struct TmapEntry {
-  void *ptr;
+  GridView v;
   int w, h;
   CUtensorMap map;
 };
@@ -54,7 +57,6 @@ struct Grid {
   int dim[3];
   size_t pitch, bytes;
   void *dev;
-  std::vector<TmapEntry> tmaps;
 };
 
 struct Map {
@@ -78,6 +80,9 @@ struct Runtime {
   std::vector<Map> maps;
   std::unordered_set<Grid *> grids;
   MarchConfig shapes[kNumKernels];
+  int tblock[kNumKernels] = {};            // temporal steps per pass (<= 1: off)
+  MarchConfig tshapes[kNumKernels];        // launch shape of temporal passes
+  std::vector<TmapEntry> tmaps;
   int fail_allocs = 0;
 };
 
@@ -206,16 +211,39 @@ bool sync_rt() {
   return check_device_errors();
 }
 
-const CUtensorMap *tmap_for(Grid *g, int w, int h) {
-  for (auto &e : g->tmaps)
-    if (e.ptr == g->dev && e.w == w && e.h == h) return &e.map;
+bool same_view(const GridView &a, const GridView &b) {
+  return a.ptr == b.ptr && a.pitch == b.pitch && a.nx == b.nx && a.ny == b.ny &&
+         a.nz == b.nz && a.type == b.type;
+}
+
+// Returns a copy of the cached (or newly encoded) tensor map for view v
+// with box {w, h, 1}; false on failure.
+bool tmap_for(const GridView &v, int w, int h, CUtensorMap *out) {
+  for (const auto &e : rt->tmaps)
+    if (e.w == w && e.h == h && same_view(e.v, v)) {
+      *out = e.map;
+      return true;
+    }
   TmapEntry e;
-  e.ptr = g->dev;
+  e.v = v;
   e.w = w;
   e.h = h;
-  if (!psg::make_tmap_3d(&e.map, view(g), w, h)) return nullptr;
-  g->tmaps.push_back(e);
-  return &g->tmaps.back().map;
+  if (!psg::make_tmap_3d(&e.map, v, w, h)) return false;
+  rt->tmaps.push_back(e);
+  *out = e.map;
+  return true;
+}
+
+void drop_tmaps(const void *ptr) {
+  auto &t = rt->tmaps;
+  for (size_t i = 0; i < t.size();) {
+    if (t[i].v.ptr == ptr) {
+      t[i] = t.back();
+      t.pop_back();
+    } else {
+      ++i;
+    }
+  }
 }
 
 struct KernelSig {
@@ -271,6 +299,30 @@ bool validate_map(const Map &m) {
 
 int shape_slot(int kernel) { return (kernel > 0 && kernel < kNumKernels) ? kernel : 0; }
 
+// One plain sweep of a 7-point-family map with explicit input/output views.
+bool launch_s7(const Map &m, const GridView &in, const GridView &out) {
+  psg::Stencil7Args a;
+  a.kernel = m.kernel;
+  a.in = in;
+  a.out = out;
+  for (int d = 0; d < 3; ++d) {
+    a.dom.min[d] = m.dom.min[d];
+    a.dom.max[d] = m.dom.max[d];
+  }
+  if (a.dom.min[0] >= a.dom.max[0] || a.dom.min[1] >= a.dom.max[1] ||
+      a.dom.min[2] >= a.dom.max[2])
+    return true;
+  for (int i = 0; i < 7; ++i) a.coef[i] = i < (int)m.scalars.size() ? m.scalars[i] : 0.0;
+  const int vec = 16 / in.esz;
+  const MarchConfig cfg = rt->shapes[shape_slot(m.kernel)];
+  CUtensorMap t;
+  if (!tmap_for(in, 34 * vec, cfg.warps * cfg.rows + 2, &t)) return false;
+  cudaError_t e = psg::launch_stencil7(a, cfg, &t, rt->dev_err, rt->sm_count, rt->stream);
+  if (!cuda_ok(e, "stencil7 launch")) return false;
+  ++rt->launches;
+  return true;
+}
+
 bool launch_map(const Map &m, bool want_gosa) {
   const Grid *g0 = m.grids[0];
   psg::Box box;
@@ -289,14 +341,9 @@ bool launch_map(const Map &m, bool want_gosa) {
     a.gosa = want_gosa;
     const MarchConfig cfg = rt->shapes[shape_slot(m.kernel)];
     CUtensorMap maps[13];
-    const CUtensorMap *t = tmap_for(m.grids[0], 136, cfg.warps + 2);
-    if (!t) return false;
-    maps[0] = *t;
-    for (int i = 0; i < 12; ++i) {
-      t = tmap_for(m.grids[2 + i], 128, cfg.warps);
-      if (!t) return false;
-      maps[1 + i] = *t;
-    }
+    if (!tmap_for(view(m.grids[0]), 136, cfg.warps + 2, &maps[0])) return false;
+    for (int i = 0; i < 12; ++i)
+      if (!tmap_for(view(m.grids[2 + i]), 128, cfg.warps, &maps[1 + i])) return false;
     psg::ResidualSink sink;
     sink.partials = reinterpret_cast<double *>(rt->partials);
     sink.max_partials = kMaxPartials;
@@ -307,19 +354,73 @@ bool launch_map(const Map &m, bool want_gosa) {
     ++rt->launches;
     return true;
   }
-  psg::Stencil7Args a;
-  a.kernel = m.kernel;
-  a.in = view(m.grids[0]);
-  a.out = view(m.grids[1]);
-  a.dom = box;
-  for (int i = 0; i < 7; ++i) a.coef[i] = i < (int)m.scalars.size() ? m.scalars[i] : 0.0;
-  const int vec = 16 / g0->esz;
-  const MarchConfig cfg = rt->shapes[shape_slot(m.kernel)];
-  const CUtensorMap *t = tmap_for(m.grids[0], 34 * vec, cfg.warps * cfg.rows + 2);
-  if (!t) return false;
-  e = psg::launch_stencil7(a, cfg, t, rt->dev_err, rt->sm_count, rt->stream);
-  if (!cuda_ok(e, "stencil7 launch")) return false;
+  (void)g0;
+  return launch_s7(m, view(m.grids[0]), view(m.grids[1]));
+}
+
+// One temporal pass: out = k steps of map m's stencil applied to in.
+bool launch_t7(const Map &m, const GridView &in, const GridView &out, int k) {
+  psg::Temporal7Args a;
+  a.in = in;
+  a.out = out;
+  a.k = k;
+  for (int i = 0; i < 7; ++i) a.coef[i] = m.scalars[i];
+  const MarchConfig cfg = rt->tshapes[shape_slot(m.kernel)];
+  const int vec = 16 / in.esz;
+  CUtensorMap t;
+  if (!tmap_for(in, 34 * vec, cfg.warps * cfg.rows + 2, &t)) return false;
+  cudaError_t e = psg::launch_temporal7(a, cfg, &t, rt->dev_err, rt->sm_count, rt->stream);
+  if (!cuda_ok(e, "temporal7 launch")) return false;
   ++rt->launches;
+  return true;
+}
+
+// A pair of maps (g1 -> g2, g2 -> g1) of the same full-grid DIFFUSION7
+// stencil can run `iter` iterations as temporal passes.
+bool temporal_pair(const Map &a, const Map &b) {
+  if (a.kernel != PS_KERNEL_DIFFUSION7 || b.kernel != PS_KERNEL_DIFFUSION7) return false;
+  const int k = rt->tblock[shape_slot(a.kernel)];
+  if (k < 2) return false;
+  const Grid *g1 = a.grids[0], *g2 = a.grids[1];
+  if (b.grids[0] != g2 || b.grids[1] != g1) return false;
+  if (g1->type != PS_FLOAT && g1->type != PS_DOUBLE) return false;
+  if (k > psg::temporal7_max_k(g1->esz)) return false;
+  for (int i = 0; i < 7; ++i)
+    if (a.scalars[i] != b.scalars[i]) return false;
+  for (int d = 0; d < 3; ++d)
+    if (a.dom.min[d] != 0 || a.dom.max[d] != g1->dim[d] || b.dom.min[d] != 0 ||
+        b.dom.max[d] != g1->dim[d])
+      return false;
+  return true;
+}
+
+// Runs (a, b) x iter as temporal passes.  Both maps cover the whole grid, so
+// every step overwrites every cell and the two grids' storage may be
+// exchanged freely; at the end g1 holds step 2*iter and g2 step 2*iter-1,
+// exactly as the plain ping-pong leaves them.
+bool run_temporal(const Map &a, int iter) {
+  Grid *g1 = a.grids[0], *g2 = a.grids[1];
+  const int total = 2 * iter;
+  if (total <= 0) return true;
+  const int k = rt->tblock[shape_slot(a.kernel)];
+  GridView cur = view(g1), oth = view(g2);
+  int t = 0;
+  // Temporal passes up to step total-1; the last step is a plain sweep so
+  // the previous step also ends up in memory.
+  while (total - 1 - t >= 2) {
+    const int kk = std::min(k, total - 1 - t);
+    if (!launch_t7(a, cur, oth, kk)) return false;
+    std::swap(cur, oth);
+    t += kk;
+  }
+  while (t < total) {
+    if (!launch_s7(a, cur, oth)) return false;
+    std::swap(cur, oth);
+    ++t;
+  }
+  // cur holds step total, oth step total-1.
+  g1->dev = cur.ptr;
+  g2->dev = oth.ptr;
   return true;
 }
 
@@ -432,9 +533,13 @@ bool run_maps(const std::vector<Map *> &ms, int iter) {
     fprintf(stderr, "Physis: Stencil started\n");
     t0 = std::chrono::steady_clock::now();
   }
-  for (int i = 0; i < iter; ++i)
-    for (Map *m : ms)
-      if (!launch_map(*m, m->kernel == PS_KERNEL_HIMENO19_GOSA)) return false;
+  if (ms.size() == 2 && temporal_pair(*ms[0], *ms[1])) {
+    if (!run_temporal(*ms[0], iter)) return false;
+  } else {
+    for (int i = 0; i < iter; ++i)
+      for (Map *m : ms)
+        if (!launch_map(*m, m->kernel == PS_KERNEL_HIMENO19_GOSA)) return false;
+  }
   if (rt->trace) {
     if (!sync_rt()) return false;
     const double ms_ = std::chrono::duration<double, std::milli>(
@@ -618,6 +723,10 @@ void PSInitV(int trace) {
   // Default launch shapes (the autotuner may replace them):
   // {warps, rows per thread, ring stages, second-ring stages, CTAs per SM}.
   for (int k = 0; k < kNumKernels; ++k) r->shapes[k] = MarchConfig{8, 2, 4, 0, 0};
+  for (int k = 0; k < kNumKernels; ++k) {
+    r->tshapes[k] = MarchConfig{8, 4, 3, 0, 0};
+    r->tblock[k] = 1;
+  }
   r->shapes[PS_KERNEL_HIMENO19] = MarchConfig{4, 1, 5, 2, 0};
   r->shapes[PS_KERNEL_HIMENO19_GOSA] = MarchConfig{4, 1, 5, 2, 0};
   cudaDeviceSynchronize();
@@ -715,6 +824,7 @@ void PSGridFree(void *g) {
   Grid *p = as_grid(g, "PSGridFree");
   if (!p) return;
   cudaStreamSynchronize(rt->stream);
+  drop_tmaps(p->dev);
   cudaFree(p->dev);
   rt->grids.erase(p);
   p->magic = 0;
@@ -988,6 +1098,50 @@ void PSSetLaunchShape(int kernel, const PSLaunchShape *shape) {
       return;
     }
     rt->shapes[k] = c;
+  }
+}
+
+void PSSetTemporalBlocking(int kernel, int k, const PSLaunchShape *shape) {
+  if (!need_rt("PSSetTemporalBlocking")) return;
+  if (kernel != PS_KERNEL_DIFFUSION7) {
+    fail(PS_ERR_UNSUPPORTED, "temporal blocking is implemented for PS_KERNEL_DIFFUSION7 only");
+    return;
+  }
+  if (k < 1 || k > psg::temporal7_max_k(4)) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSSetTemporalBlocking: k %d not in 1..%d", k,
+         psg::temporal7_max_k(4));
+    return;
+  }
+  MarchConfig c = rt->tshapes[kernel];
+  if (shape) {
+    if (shape->warps > 0) c.warps = shape->warps;
+    if (shape->rows > 0) c.rows = shape->rows;
+    if (shape->ns > 0) c.ns = shape->ns;
+    c.ctas_per_sm = shape->ctas_per_sm > 0 ? shape->ctas_per_sm : 0;
+  }
+  if (c.warps < 1 || c.warps > 8 || !(c.rows == 1 || c.rows == 2 || c.rows == 4) ||
+      c.ns < 2 || c.ns > 16 || c.warps * c.rows - 2 * (k - 1) < 1 ||
+      psg::temporal7_smem_bytes(8, c, k) > 227 * 1024) {
+    fail(PS_ERR_INVALID_ARGUMENT,
+         "PSSetTemporalBlocking: shape warps %d rows %d ns %d does not fit k %d", c.warps,
+         c.rows, c.ns, k);
+    return;
+  }
+  rt->tshapes[kernel] = c;
+  rt->tblock[kernel] = k;
+}
+
+void PSGetTemporalBlocking(int kernel, int *k, PSLaunchShape *shape) {
+  if (!need_rt("PSGetTemporalBlocking")) return;
+  const int slot = shape_slot(kernel);
+  if (k) *k = rt->tblock[slot];
+  if (shape) {
+    const MarchConfig &c = rt->tshapes[slot];
+    shape->warps = c.warps;
+    shape->rows = c.rows;
+    shape->ns = c.ns;
+    shape->ns2 = c.ns2;
+    shape->ctas_per_sm = c.ctas_per_sm;
   }
 }
 

@@ -395,3 +395,73 @@ def test_reference_style_c_program_runs(rt, tmp_path):
     assert "Physis: Stencil started" in r.stderr
     total = float(np.arange(512, dtype=np.float64).sum())
     assert "sum %f" % (7 * total) in r.stderr
+
+
+# ---- temporal blocking -------------------------------------------------------
+
+TEMPORAL = [  # (k, warps, rows, ns)
+    (2, 8, 4, 3), (3, 8, 2, 3), (4, 8, 4, 2), (5, 4, 4, 3), (2, 1, 4, 2), (3, 2, 4, 4)]
+
+
+@pytest.mark.parametrize("k,warps,rows,ns", TEMPORAL)
+@pytest.mark.parametrize("shape,iters", [((37, 45, 70), 5), ((9, 17, 250), 3),
+                                         ((64, 64, 64), 2), ((1, 3, 9), 4),
+                                         ((20, 130, 121), 1)])
+def test_temporal_blocking_bit_exact(rt, oracle, k, warps, rows, ns, shape, iters):
+    init = synth.uniform(shape, 8)
+    ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, k, warps=warps, rows=rows, ns=ns)
+    try:
+        a, b = run_pingpong(ps.PS_KERNEL_DIFFUSION7, init, ps.full_domain(shape),
+                            DIFF_COEF, iters)
+    finally:
+        ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 1)
+    r1, r2 = init.copy(), np.zeros_like(init)
+    nz, ny, nx = shape
+    oracle.run7(oracle.V_DIFFUSION7, r1, r2, (0, nx, 0, ny, 0, nz), DIFF_COEF,
+                iter=iters)
+    assert np.array_equal(_bits(a), _bits(r1))
+    assert np.array_equal(_bits(b), _bits(r2))
+
+
+@pytest.mark.parametrize("k", [2, 3])
+def test_temporal_blocking_double(rt, oracle, k):
+    shape = (19, 33, 70)
+    init = synth.uniform(shape, 9).astype(np.float64)
+    ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, k, warps=8, rows=2, ns=3)
+    try:
+        a, b = run_pingpong(ps.PS_KERNEL_DIFFUSION7, init, ps.full_domain(shape),
+                            DIFF_COEF, 4, np.float64)
+    finally:
+        ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 1)
+    r1, r2 = init.copy(), np.zeros_like(init)
+    nz, ny, nx = shape
+    oracle.run7(oracle.V_DIFFUSION7, r1, r2, (0, nx, 0, ny, 0, nz), DIFF_COEF, iter=4)
+    assert np.array_equal(_bits(a), _bits(r1))
+    assert np.array_equal(_bits(b), _bits(r2))
+
+
+def test_temporal_blocking_not_used_for_subdomains(rt, oracle):
+    # an interior domain keeps the plain path (cells outside stay untouched)
+    shape = (21, 31, 41)
+    init, other = synth.uniform(shape, 4), synth.uniform(shape, 5)
+    dom = (1, 40, 2, 30, 3, 20)
+    ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 3, warps=8, rows=2, ns=3)
+    try:
+        a, b = run_pingpong(ps.PS_KERNEL_DIFFUSION7, init, ps.domain(*dom),
+                            DIFF_COEF, 3, out0=other)
+    finally:
+        ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 1)
+    r1, r2 = init.copy(), other.copy()
+    oracle.run7(oracle.V_DIFFUSION7, r1, r2, dom, DIFF_COEF, iter=3)
+    assert np.array_equal(_bits(a), _bits(r1))
+    assert np.array_equal(_bits(b), _bits(r2))
+
+
+def test_temporal_blocking_rejects_bad_shapes(rt):
+    with pytest.raises(ps.PSError):
+        ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 9)
+    with pytest.raises(ps.PSError):
+        ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 5, warps=1, rows=4)  # tile too short
+    with pytest.raises(ps.PSError):
+        ps.set_temporal(ps.PS_KERNEL_SUM7, 2)
+    assert ps.get_temporal(ps.PS_KERNEL_DIFFUSION7)[0] == 1
