@@ -139,6 +139,25 @@ void PSGetLaunchShape(int kernel, PSLaunchShape *shape);
 void PSSetTemporalBlocking(int kernel, int k, const PSLaunchShape *shape);
 void PSGetTemporalBlocking(int kernel, int *k, PSLaunchShape *shape);
 
+/* Autotuner (replaces the reference's online trial of OPT_* variants and
+ * block sizes, translator/reference_translator.cc:610-935).  When on
+ * (PSSetAutotune(1) or PS_AUTOTUNE=1 at PSInit), the first iterations of a
+ * PSStencilRun whose signature (kernels, grid size, type, domains, GPU) has
+ * no tuned plan are spent trying launch shapes and, for full-grid diffusion
+ * pairs, temporal depths; every candidate computes bit-identical results, so
+ * the trials are ordinary iterations of the run.  Trials continue across
+ * runs until all candidates are timed; the fastest becomes the signature's
+ * plan.  With PS_TUNE_CACHE=<file> (or PSSetTuneCachePath) plans are
+ * appended to that file as JSON lines and loaded at PSInit, so later
+ * processes skip the trials.  A malformed cache line is ignored and
+ * reported as PS_ERR_IO. */
+void PSSetAutotune(int on);
+void PSSetTuneCachePath(const char *path);
+int PSLoadTuneCache(const char *path);  /* returns the number of plans loaded */
+void PSClearTuning(void);               /* forgets all plans (not the file) */
+/* The plan a stencil runs with: returns 1 if tuned, 0 if the defaults. */
+int PSGetStencilPlan(PSStencil s, PSLaunchShape *shape, int *k, PSLaunchShape *tshape);
+
 /* ---- 5. Reduction for callers that cannot allocate --------------------- */
 
 /* No counterpart in the reference.  PSReduce over a grid that the caller

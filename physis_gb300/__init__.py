@@ -50,7 +50,8 @@ PSGridDevicePtr PSGridPitch PSGridElemSize PSGridType PSGridCopyinAsync
 PSGridCopyoutAsync PSHostAlloc PSHostFree PSSynchronize PSGetStream
 PSEventRecord PSEventElapsedMs PSGetLaunchCount PSGetSMCount PSSetLaunchShape
 PSGetLaunchShape PSTestFailNextAllocs PSTestDeviceWaitTimeout PSReduceNoAlloc
-PSSetTemporalBlocking PSGetTemporalBlocking""".split()
+PSSetTemporalBlocking PSGetTemporalBlocking PSSetAutotune PSSetTuneCachePath
+PSLoadTuneCache PSClearTuning PSGetStencilPlan""".split()
 
 
 class PSDomain(ctypes.Structure):
@@ -138,6 +139,13 @@ def lib():
     L.PSTestDeviceWaitTimeout.argtypes = [ctypes.c_uint]
     L.PSSetTemporalBlocking.argtypes = [i, i, ctypes.POINTER(PSLaunchShape)]
     L.PSGetTemporalBlocking.argtypes = [i, ctypes.POINTER(i), ctypes.POINTER(PSLaunchShape)]
+    L.PSSetAutotune.argtypes = [i]
+    L.PSSetTuneCachePath.argtypes = [ctypes.c_char_p]
+    L.PSLoadTuneCache.argtypes = [ctypes.c_char_p]
+    L.PSLoadTuneCache.restype = i
+    L.PSGetStencilPlan.argtypes = [i, ctypes.POINTER(PSLaunchShape), ctypes.POINTER(i),
+                                   ctypes.POINTER(PSLaunchShape)]
+    L.PSGetStencilPlan.restype = i
     L.PSReduceNoAlloc.argtypes = [vp, ctypes.c_size_t, i, i, i, i, i, vp, vp]
     L.PSReduceNoAlloc.restype = i
     _lib = L
@@ -299,6 +307,24 @@ def get_temporal(kernel):
     sh = PSLaunchShape()
     lib().PSGetTemporalBlocking(kernel, ctypes.byref(k), ctypes.byref(sh))
     return k.value, (sh.warps, sh.rows, sh.ns, sh.ctas_per_sm)
+
+
+def set_autotune(on=True, cache_path=None):
+    L = lib()
+    if cache_path is not None:
+        L.PSSetTuneCachePath(cache_path.encode())
+    L.PSSetAutotune(1 if on else 0)
+    check()
+
+
+def stencil_plan(s):
+    """(tuned?, (warps, rows, ns, ns2, ctas), k, temporal shape) of a stencil."""
+    sh, tsh, k = PSLaunchShape(), PSLaunchShape(), ctypes.c_int(0)
+    tuned = lib().PSGetStencilPlan(s, ctypes.byref(sh), ctypes.byref(k),
+                                   ctypes.byref(tsh))
+    check()
+    return (bool(tuned), (sh.warps, sh.rows, sh.ns, sh.ns2, sh.ctas_per_sm), k.value,
+            (tsh.warps, tsh.rows, tsh.ns))
 
 
 def launch_count():

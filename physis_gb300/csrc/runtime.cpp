@@ -22,6 +22,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <string>
 #include <unordered_set>
 #include <vector>
@@ -59,11 +60,21 @@ struct Grid {
   void *dev;
 };
 
+// How a run executes: the sweep's launch shape and, for temporal-eligible
+// pairs, the temporal depth and the passes' shape.
+struct Plan {
+  MarchConfig shape;
+  int k;
+  MarchConfig tshape;
+};
+
 struct Map {
   int kernel;
   __PSDomain dom;
   std::vector<Grid *> grids;
   std::vector<double> scalars;
+  bool has_plan = false;  // set by the autotuner (or its cache)
+  Plan plan;
 };
 
 struct Runtime {
@@ -84,6 +95,9 @@ struct Runtime {
   MarchConfig tshapes[kNumKernels];        // launch shape of temporal passes
   std::vector<TmapEntry> tmaps;
   int fail_allocs = 0;
+  bool autotune = false;
+  std::string tune_path;  // JSON-lines cache file ("" = in memory only)
+  std::string gpu_name;
 };
 
 Runtime *rt = nullptr;
@@ -314,7 +328,7 @@ bool launch_s7(const Map &m, const GridView &in, const GridView &out) {
     return true;
   for (int i = 0; i < 7; ++i) a.coef[i] = i < (int)m.scalars.size() ? m.scalars[i] : 0.0;
   const int vec = 16 / in.esz;
-  const MarchConfig cfg = rt->shapes[shape_slot(m.kernel)];
+  const MarchConfig cfg = m.has_plan ? m.plan.shape : rt->shapes[shape_slot(m.kernel)];
   CUtensorMap t;
   if (!tmap_for(in, 34 * vec, cfg.warps * cfg.rows + 2, &t)) return false;
   cudaError_t e = psg::launch_stencil7(a, cfg, &t, rt->dev_err, rt->sm_count, rt->stream);
@@ -339,7 +353,7 @@ bool launch_map(const Map &m, bool want_gosa) {
     a.dom = box;
     a.omega = (float)m.scalars[0];
     a.gosa = want_gosa;
-    const MarchConfig cfg = rt->shapes[shape_slot(m.kernel)];
+    const MarchConfig cfg = m.has_plan ? m.plan.shape : rt->shapes[shape_slot(m.kernel)];
     CUtensorMap maps[13];
     if (!tmap_for(view(m.grids[0]), 136, cfg.warps + 2, &maps[0])) return false;
     for (int i = 0; i < 12; ++i)
@@ -365,7 +379,7 @@ bool launch_t7(const Map &m, const GridView &in, const GridView &out, int k) {
   a.out = out;
   a.k = k;
   for (int i = 0; i < 7; ++i) a.coef[i] = m.scalars[i];
-  const MarchConfig cfg = rt->tshapes[shape_slot(m.kernel)];
+  const MarchConfig cfg = m.has_plan ? m.plan.tshape : rt->tshapes[shape_slot(m.kernel)];
   const int vec = 16 / in.esz;
   CUtensorMap t;
   if (!tmap_for(in, 34 * vec, cfg.warps * cfg.rows + 2, &t)) return false;
@@ -377,14 +391,17 @@ bool launch_t7(const Map &m, const GridView &in, const GridView &out, int k) {
 
 // A pair of maps (g1 -> g2, g2 -> g1) of the same full-grid DIFFUSION7
 // stencil can run `iter` iterations as temporal passes.
-bool temporal_pair(const Map &a, const Map &b) {
+int temporal_depth(const Map &a) {
+  return a.has_plan ? a.plan.k : rt->tblock[shape_slot(a.kernel)];
+}
+
+// True if (a, b) is a ping-pong pair of one full-grid DIFFUSION7 stencil
+// (the shape temporal blocking applies to), whatever the current depth.
+bool pair_eligible(const Map &a, const Map &b) {
   if (a.kernel != PS_KERNEL_DIFFUSION7 || b.kernel != PS_KERNEL_DIFFUSION7) return false;
-  const int k = rt->tblock[shape_slot(a.kernel)];
-  if (k < 2) return false;
   const Grid *g1 = a.grids[0], *g2 = a.grids[1];
   if (b.grids[0] != g2 || b.grids[1] != g1) return false;
   if (g1->type != PS_FLOAT && g1->type != PS_DOUBLE) return false;
-  if (k > psg::temporal7_max_k(g1->esz)) return false;
   for (int i = 0; i < 7; ++i)
     if (a.scalars[i] != b.scalars[i]) return false;
   for (int d = 0; d < 3; ++d)
@@ -392,6 +409,11 @@ bool temporal_pair(const Map &a, const Map &b) {
         b.dom.max[d] != g1->dim[d])
       return false;
   return true;
+}
+
+bool temporal_pair(const Map &a, const Map &b) {
+  const int k = temporal_depth(a);
+  return k >= 2 && k <= psg::temporal7_max_k(a.grids[0]->esz) && pair_eligible(a, b);
 }
 
 // Runs (a, b) x iter as temporal passes.  Both maps cover the whole grid, so
@@ -402,7 +424,7 @@ bool run_temporal(const Map &a, int iter) {
   Grid *g1 = a.grids[0], *g2 = a.grids[1];
   const int total = 2 * iter;
   if (total <= 0) return true;
-  const int k = rt->tblock[shape_slot(a.kernel)];
+  const int k = temporal_depth(a);
   GridView cur = view(g1), oth = view(g2);
   int t = 0;
   // Temporal passes up to step total-1; the last step is a plain sweep so
@@ -527,13 +549,191 @@ bool map_from(int kernel, const __PSDomain &dom, int ngrids, void *const *grids,
   return true;
 }
 
+// ---- Autotuner ------------------------------------------------------------
+//
+// Replaces the reference's online trial (translator/reference_translator.cc:
+// 610-935: each OPT_* / block-size variant times one iteration of the run
+// during its first calls, nothing persists).  Here the candidates are launch
+// shapes and temporal depths; because every candidate computes bit-identical
+// results, the trials are simply the run's first iterations.  The winner is
+// kept per run signature (kernels, grid size, type, domains, GPU) in memory
+// and, when PS_TUNE_CACHE names a file, as one JSON object per line there.
+
+struct TuneState {
+  std::vector<Plan> cands;
+  std::vector<double> ms;  // per-iteration time of each tried candidate
+  size_t next = 0;
+};
+
+std::map<std::string, Plan> g_tuned;
+std::map<std::string, TuneState> g_tuning;
+
+std::string run_key(const std::vector<Map *> &ms) {
+  std::string k;
+  char buf[256];
+  for (const Map *m : ms) {
+    const Grid *g = m->grids[0];
+    snprintf(buf, sizeof(buf), "k%d t%d g%dx%dx%d d%d:%d,%d:%d,%d:%d;", m->kernel, g->type,
+             g->dim[0], g->dim[1], g->dim[2], m->dom.min[0], m->dom.max[0], m->dom.min[1],
+             m->dom.max[1], m->dom.min[2], m->dom.max[2]);
+    k += buf;
+  }
+  if (ms.size() == 2 && pair_eligible(*ms[0], *ms[1])) k += "pair;";
+  snprintf(buf, sizeof(buf), "%s/%dsm", rt->gpu_name.c_str(), rt->sm_count);
+  return k + buf;
+}
+
+std::vector<Plan> candidates(const std::vector<Map *> &ms) {
+  std::vector<Plan> out;
+  const Map &m0 = *ms[0];
+  const bool him = m0.kernel == PS_KERNEL_HIMENO19 || m0.kernel == PS_KERNEL_HIMENO19_GOSA;
+  const MarchConfig tdef = rt->tshapes[shape_slot(m0.kernel)];
+  if (him) {
+    const int sh[][3] = {{4, 5, 2}, {2, 5, 2}, {8, 4, 2}, {4, 4, 3}, {4, 6, 2}, {2, 6, 3},
+                         {8, 3, 2}, {4, 3, 1}};
+    for (auto &c : sh) out.push_back(Plan{MarchConfig{c[0], 1, c[1], c[2], 0}, 1, tdef});
+    return out;
+  }
+  const int sh[][3] = {{8, 2, 4}, {4, 2, 3}, {2, 2, 3}, {8, 4, 4}, {4, 4, 4},
+                       {16, 4, 4}, {16, 2, 6}, {8, 8, 3}, {8, 1, 4}, {4, 1, 4}};
+  for (auto &c : sh) out.push_back(Plan{MarchConfig{c[0], c[1], c[2], 0, 0}, 1, tdef});
+  if (ms.size() == 2 && pair_eligible(*ms[0], *ms[1])) {
+    const int maxk = psg::temporal7_max_k(m0.grids[0]->esz);
+    const int tc[][4] = {{2, 8, 2, 3}, {2, 8, 4, 3}, {2, 4, 4, 4}, {3, 8, 2, 4},
+                         {3, 8, 4, 3}, {4, 8, 4, 3}};
+    for (auto &c : tc) {
+      if (c[0] > maxk) continue;
+      out.push_back(Plan{MarchConfig{8, 2, 4, 0, 0}, c[0], MarchConfig{c[1], c[2], c[3], 0, 0}});
+    }
+  }
+  return out;
+}
+
+void apply_plan(const std::vector<Map *> &ms, const Plan &p) {
+  for (Map *m : ms) {
+    m->has_plan = true;
+    m->plan = p;
+  }
+}
+
+void save_tuned(const std::string &key, const Plan &p, double ms) {
+  if (rt->tune_path.empty()) return;
+  FILE *f = fopen(rt->tune_path.c_str(), "a");
+  if (!f) {
+    fail(PS_ERR_IO, "cannot append to the tune cache %s", rt->tune_path.c_str());
+    return;
+  }
+  fprintf(f,
+          "{\"key\": \"%s\", \"warps\": %d, \"rows\": %d, \"ns\": %d, \"ns2\": %d, "
+          "\"ctas\": %d, \"k\": %d, \"twarps\": %d, \"trows\": %d, \"tns\": %d, "
+          "\"ms\": %.6f}\n",
+          key.c_str(), p.shape.warps, p.shape.rows, p.shape.ns, p.shape.ns2,
+          p.shape.ctas_per_sm, p.k, p.tshape.warps, p.tshape.rows, p.tshape.ns, ms);
+  fclose(f);
+}
+
+// Loads a JSON-lines tune cache written by save_tuned; malformed lines are
+// skipped (and reported once as PS_ERR_IO).  Returns the entries loaded.
+int load_tuned(const char *path) {
+  FILE *f = fopen(path, "r");
+  if (!f) return 0;
+  char line[1024], key[512];
+  int n = 0, bad = 0;
+  while (fgets(line, sizeof(line), f)) {
+    Plan p{};
+    double ms = 0;
+    const int got = sscanf(line,
+                           "{\"key\": \"%511[^\"]\", \"warps\": %d, \"rows\": %d, \"ns\": %d, "
+                           "\"ns2\": %d, \"ctas\": %d, \"k\": %d, \"twarps\": %d, \"trows\": %d, "
+                           "\"tns\": %d, \"ms\": %lf}",
+                           key, &p.shape.warps, &p.shape.rows, &p.shape.ns, &p.shape.ns2,
+                           &p.shape.ctas_per_sm, &p.k, &p.tshape.warps, &p.tshape.rows,
+                           &p.tshape.ns, &ms);
+    const bool sane = got == 11 && p.shape.warps >= 1 && p.shape.warps <= 16 &&
+                      p.shape.rows >= 1 && p.shape.rows <= 8 && p.shape.ns >= 2 &&
+                      p.shape.ns <= 16 && p.k >= 1 && p.k <= 5 && p.tshape.warps >= 1 &&
+                      p.tshape.warps <= 8 && p.tshape.ns >= 2 && p.tshape.ns <= 16;
+    if (!sane) {
+      ++bad;
+      continue;
+    }
+    g_tuned[key] = p;
+    ++n;
+  }
+  fclose(f);
+  if (bad) fail(PS_ERR_IO, "tune cache %s: %d malformed line(s) ignored", path, bad);
+  return n;
+}
+
+// Runs `iter` iterations of the maps, spending the first ones on tuning
+// trials while the run's signature has no tuned plan.  Returns the number of
+// iterations it ran (all of them unless an error occurs).
+bool run_tuning(const std::vector<Map *> &ms, int &iter) {
+  const std::string key = run_key(ms);
+  auto hit = g_tuned.find(key);
+  if (hit != g_tuned.end()) {
+    apply_plan(ms, hit->second);
+    return true;
+  }
+  if (!rt->autotune) return true;  // no plan: defaults
+  TuneState &st = g_tuning[key];
+  if (st.cands.empty()) st.cands = candidates(ms);
+  const bool pair = ms.size() == 2 && pair_eligible(*ms[0], *ms[1]);
+  while (iter > 0 && st.next < st.cands.size()) {
+    const Plan &c = st.cands[st.next];
+    apply_plan(ms, c);
+    // temporal candidates need several iterations for the passes to dominate
+    int reps = (pair && c.k > 1) ? 6 : 2;
+    if (reps > iter) reps = iter;
+    cudaEventRecord(rt->events[kNumEvents - 2], rt->stream);
+    bool ok = true;
+    if (pair && c.k > 1) {
+      ok = run_temporal(*ms[0], reps);
+    } else {
+      for (int i = 0; i < reps && ok; ++i)
+        for (Map *m : ms)
+          if (!launch_map(*m, m->kernel == PS_KERNEL_HIMENO19_GOSA)) {
+            ok = false;
+            break;
+          }
+    }
+    cudaEventRecord(rt->events[kNumEvents - 1], rt->stream);
+    iter -= reps;
+    float t = 0;
+    if (!ok || cudaEventSynchronize(rt->events[kNumEvents - 1]) != cudaSuccess ||
+        cudaEventElapsedTime(&t, rt->events[kNumEvents - 2], rt->events[kNumEvents - 1]) !=
+            cudaSuccess) {
+      // a candidate that cannot launch is skipped (the launch error is kept)
+      cudaGetLastError();
+      st.ms.push_back(1e30);
+    } else {
+      st.ms.push_back((double)t / reps);
+    }
+    ++st.next;
+  }
+  if (st.next < st.cands.size()) return true;  // continue in a later run
+  size_t best = 0;
+  for (size_t i = 1; i < st.ms.size(); ++i)
+    if (st.ms[i] < st.ms[best]) best = i;
+  const Plan p = st.cands[best];
+  const double best_ms = st.ms[best];
+  g_tuned[key] = p;
+  g_tuning.erase(key);
+  apply_plan(ms, p);
+  save_tuned(key, p, best_ms);
+  return true;
+}
+
 bool run_maps(const std::vector<Map *> &ms, int iter) {
   std::chrono::steady_clock::time_point t0;
   if (rt->trace) {
     fprintf(stderr, "Physis: Stencil started\n");
     t0 = std::chrono::steady_clock::now();
   }
-  if (ms.size() == 2 && temporal_pair(*ms[0], *ms[1])) {
+  if ((rt->autotune || !g_tuned.empty()) && !run_tuning(ms, iter)) return false;
+  if (iter <= 0) {
+    // every iteration went into tuning trials
+  } else if (ms.size() == 2 && temporal_pair(*ms[0], *ms[1])) {
     if (!run_temporal(*ms[0], iter)) return false;
   } else {
     for (int i = 0; i < iter; ++i)
@@ -598,6 +798,10 @@ bool reduce_kernel_form(void *v, int op, int kernel, const __PSDomain &dom, int 
   Map m;
   if (!map_from(kernel, dom, ngrids, grids, nscalars, scalars, &m)) return false;
   if (!validate_map(m)) return false;
+  if (!g_tuned.empty()) {  // a plan tuned for this sweep's PSStencilRun form
+    auto hit = g_tuned.find(run_key({&m}));
+    if (hit != g_tuned.end()) apply_plan({&m}, hit->second);
+  }
   if (!launch_map(m, true)) return false;
   uint64_t bits = 0;
   if (!read_result(1, &bits)) return false;
@@ -694,7 +898,14 @@ void PSInitV(int trace) {
     return;
   }
   r->sm_count = prop.multiProcessorCount;
+  r->gpu_name = prop.name;
+  for (char &ch : r->gpu_name)
+    if (ch == '"' || ch == ' ') ch = '_';
   r->trace = trace != 0;
+  const char *at = getenv("PS_AUTOTUNE");
+  r->autotune = at && at[0] == '1';
+  const char *tc = getenv("PS_TUNE_CACHE");
+  if (tc && tc[0]) r->tune_path = tc;
   if (!g_encode) {
     void *fn = nullptr;
     cudaDriverEntryPointQueryResult q;
@@ -731,6 +942,7 @@ void PSInitV(int trace) {
   r->shapes[PS_KERNEL_HIMENO19_GOSA] = MarchConfig{4, 1, 5, 2, 0};
   cudaDeviceSynchronize();
   rt = r;
+  if (!rt->tune_path.empty()) load_tuned(rt->tune_path.c_str());
 }
 
 void PSFinalize(void) {
@@ -1162,6 +1374,41 @@ int PSReduceNoAlloc(const void *data, size_t pitch, int nx, int ny, int nz, int 
                                        static_cast<cudaStream_t>(stream), &why);
   if (code != PS_OK) fail(code, "PSReduceNoAlloc: %s", why);
   return code;
+}
+
+void PSSetAutotune(int on) {
+  if (need_rt("PSSetAutotune")) rt->autotune = on != 0;
+}
+
+int PSLoadTuneCache(const char *path) {
+  if (!need_rt("PSLoadTuneCache") || !path) return 0;
+  return load_tuned(path);
+}
+
+void PSSetTuneCachePath(const char *path) {
+  if (need_rt("PSSetTuneCachePath")) rt->tune_path = path ? path : "";
+}
+
+void PSClearTuning(void) {
+  g_tuned.clear();
+  g_tuning.clear();
+  if (!rt) return;
+  for (Map &m : rt->maps) m.has_plan = false;
+}
+
+int PSGetStencilPlan(PSStencil s, PSLaunchShape *shape, int *k, PSLaunchShape *tshape) {
+  if (!need_rt("PSGetStencilPlan")) return 0;
+  Map *m = lookup_map(s);
+  if (!m) {
+    fail(PS_ERR_BAD_HANDLE, "PSGetStencilPlan: %d is not a stencil", s);
+    return 0;
+  }
+  const MarchConfig c = m->has_plan ? m->plan.shape : rt->shapes[shape_slot(m->kernel)];
+  const MarchConfig t = m->has_plan ? m->plan.tshape : rt->tshapes[shape_slot(m->kernel)];
+  if (shape) *shape = PSLaunchShape{c.warps, c.rows, c.ns, c.ns2, c.ctas_per_sm};
+  if (tshape) *tshape = PSLaunchShape{t.warps, t.rows, t.ns, t.ns2, t.ctas_per_sm};
+  if (k) *k = temporal_depth(*m);
+  return m->has_plan ? 1 : 0;
 }
 
 void PSTestFailNextAllocs(int n) {

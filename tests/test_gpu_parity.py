@@ -465,3 +465,61 @@ def test_temporal_blocking_rejects_bad_shapes(rt):
     with pytest.raises(ps.PSError):
         ps.set_temporal(ps.PS_KERNEL_SUM7, 2)
     assert ps.get_temporal(ps.PS_KERNEL_DIFFUSION7)[0] == 1
+
+
+# ---- autotuner ---------------------------------------------------------------
+
+def test_autotuner_trials_are_ordinary_iterations(rt, oracle, tmp_path):
+    # Tuning spends the run's first iterations on candidate shapes/depths;
+    # every candidate is bit-identical, so the run's result must equal the
+    # oracle's, and the signature ends with a tuned plan saved to the cache.
+    shape = (40, 70, 300)
+    init = synth.uniform(shape, 12)
+    cache = str(tmp_path / "tune.jsonl")
+    ps.lib().PSClearTuning()
+    ps.set_autotune(True, cache)
+    try:
+        g1, g2 = ps.Grid(shape), ps.Grid(shape)
+        g1.copyin(init)
+        dom = ps.full_domain(shape)
+        m1 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g1, g2], DIFF_COEF)
+        m2 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g2, g1], DIFF_COEF)
+        ps.stencil_run([m1, m2], 30)   # tuning continues across runs
+        ps.stencil_run([m1, m2], 40)
+        a, b = g1.copyout(), g2.copyout()
+        tuned, sh, k, tsh = ps.stencil_plan(m1)
+        assert tuned
+    finally:
+        ps.set_autotune(False, "")
+    r1, r2 = init.copy(), np.zeros_like(init)
+    nz, ny, nx = shape
+    oracle.run7(oracle.V_DIFFUSION7, r1, r2, (0, nx, 0, ny, 0, nz), DIFF_COEF,
+                iter=70, nthreads=0)
+    assert np.array_equal(_bits(a), _bits(r1))
+    assert np.array_equal(_bits(b), _bits(r2))
+    # the plan persists: a fresh tuning table loads it and applies it
+    lines = open(cache).read().splitlines()
+    assert len(lines) == 1 and '"key": "k2 t2 g300x70x40' in lines[0]
+    ps.lib().PSClearTuning()
+    assert ps.lib().PSLoadTuneCache(cache.encode()) == 1
+    m3 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g1, g2], DIFF_COEF)
+    m4 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g2, g1], DIFF_COEF)
+    ps.stencil_run([m3, m4], 1)
+    assert ps.stencil_plan(m3)[0]
+    assert ps.stencil_plan(m3)[1:] == (sh, k, tsh)
+    ps.lib().PSClearTuning()
+    g1.free()
+    g2.free()
+
+
+def test_corrupt_tune_cache_is_skipped(rt, tmp_path):
+    p = tmp_path / "bad.jsonl"
+    good = ('{"key": "k2 t2 g8x8x8 d0:8,0:8,0:8;x/1sm", "warps": 4, "rows": 2, '
+            '"ns": 3, "ns2": 0, "ctas": 0, "k": 1, "twarps": 8, "trows": 4, '
+            '"tns": 3, "ms": 0.1}')
+    p.write_text("garbage\n" + good + "\n{\"key\": \"x\", \"warps\": 99}\n")
+    ps.clear_error()
+    assert ps.lib().PSLoadTuneCache(str(p).encode()) == 1
+    assert ps.last_error()[0] == ps.PS_ERR_IO
+    ps.clear_error()
+    ps.lib().PSClearTuning()
