@@ -22,6 +22,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <string>
 #include <unordered_set>
@@ -88,7 +89,7 @@ struct Runtime {
   uint64_t *results = nullptr;  // slot 0: reductions, slot 1: residuals
   cudaEvent_t events[kNumEvents] = {};
   long long launches = 0;
-  std::vector<Map> maps;
+  std::deque<Map> maps;  // deque: references stay valid as maps are added
   std::unordered_set<Grid *> grids;
   MarchConfig shapes[kNumKernels];
   int tblock[kNumKernels] = {};            // temporal steps per pass (<= 1: off)
@@ -724,6 +725,140 @@ bool run_tuning(const std::vector<Map *> &ms, int &iter) {
   return true;
 }
 
+// ---- CUDA graphs for launch-bound runs -----------------------------------
+//
+// A plain (non-temporal) run re-launches the same kernels with the same
+// arguments every iteration.  For small grids the launch overhead rivals the
+// sweep itself, so after one ordinary iteration the runtime captures
+// kGraphUnroll iterations into a CUDA graph and replays it; the remainder
+// runs as ordinary launches.  Graphs are cached per map list and rebuilt
+// when a grid's storage or a map's plan changes.  PS_GRAPH=0 disables them.
+
+constexpr int kGraphUnroll = 16;
+
+struct GraphEntry {
+  std::vector<const Map *> maps;   // elements of rt->maps (a deque: stable)
+  std::vector<const Grid *> grids; // every grid the maps touch
+  std::vector<void *> ptrs;        // grid storage at capture
+  std::vector<MarchConfig> cfgs;   // launch shapes at capture
+  cudaGraphExec_t exec = nullptr;
+};
+std::vector<GraphEntry> g_graphs;
+
+void graph_signature(const std::vector<Map *> &ms, std::vector<void *> *ptrs,
+                     std::vector<MarchConfig> *cfgs) {
+  for (const Map *m : ms) {
+    for (const Grid *g : m->grids) ptrs->push_back(g->dev);
+    cfgs->push_back(m->has_plan ? m->plan.shape : rt->shapes[shape_slot(m->kernel)]);
+  }
+}
+
+bool same_cfg(const MarchConfig &a, const MarchConfig &b) {
+  return a.warps == b.warps && a.rows == b.rows && a.ns == b.ns && a.ns2 == b.ns2 &&
+         a.ctas_per_sm == b.ctas_per_sm;
+}
+
+void drop_graphs_for(const Grid *g) {
+  for (size_t i = 0; i < g_graphs.size();) {
+    bool uses = false;
+    for (const Grid *x : g_graphs[i].grids) uses = uses || x == g;
+    if (uses) {
+      cudaGraphExecDestroy(g_graphs[i].exec);
+      g_graphs[i] = g_graphs.back();
+      g_graphs.pop_back();
+    } else {
+      ++i;
+    }
+  }
+}
+
+bool launch_iteration(const std::vector<Map *> &ms) {
+  for (Map *m : ms)
+    if (!launch_map(*m, m->kernel == PS_KERNEL_HIMENO19_GOSA)) return false;
+  return true;
+}
+
+// Returns the cached or newly captured graph of kGraphUnroll iterations, or
+// nullptr if capture is not possible (the caller then launches normally).
+cudaGraphExec_t graph_for(const std::vector<Map *> &ms) {
+  std::vector<void *> ptrs;
+  std::vector<MarchConfig> cfgs;
+  graph_signature(ms, &ptrs, &cfgs);
+  for (size_t i = 0; i < g_graphs.size(); ++i) {
+    GraphEntry &e = g_graphs[i];
+    if (e.maps.size() != ms.size()) continue;
+    bool same = true;
+    for (size_t j = 0; j < ms.size(); ++j) same = same && e.maps[j] == ms[j];
+    if (!same) continue;
+    bool fresh = e.ptrs == ptrs && e.cfgs.size() == cfgs.size();
+    for (size_t j = 0; fresh && j < cfgs.size(); ++j) fresh = same_cfg(e.cfgs[j], cfgs[j]);
+    if (fresh) return e.exec;
+    cudaGraphExecDestroy(e.exec);
+    g_graphs[i] = g_graphs.back();
+    g_graphs.pop_back();
+    break;
+  }
+  const long long launches0 = rt->launches;
+  cudaGraph_t graph = nullptr;
+  if (cudaStreamBeginCapture(rt->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  bool ok = true;
+  for (int u = 0; u < kGraphUnroll && ok; ++u) ok = launch_iteration(ms);
+  const cudaError_t ee = cudaStreamEndCapture(rt->stream, &graph);
+  rt->launches = launches0;  // captured launches run when the graph does
+  if (!ok || ee != cudaSuccess || !graph) {
+    cudaGetLastError();
+    if (graph) cudaGraphDestroy(graph);
+    return nullptr;
+  }
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ie != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  GraphEntry e;
+  e.maps.assign(ms.begin(), ms.end());
+  for (const Map *m : ms) e.grids.insert(e.grids.end(), m->grids.begin(), m->grids.end());
+  e.ptrs = ptrs;
+  e.cfgs = cfgs;
+  e.exec = exec;
+  g_graphs.push_back(e);
+  return exec;
+}
+
+bool graphs_enabled() {
+  const char *e = getenv("PS_GRAPH");
+  return !(e && e[0] == '0');
+}
+
+bool run_plain(const std::vector<Map *> &ms, int iter) {
+  int i = 0;
+  if (graphs_enabled() && iter > kGraphUnroll) {
+    // one ordinary iteration first: sets kernel attributes and caches
+    if (!launch_iteration(ms)) return false;
+    ++i;
+    cudaGraphExec_t g = graph_for(ms);
+    if (g) {
+      long long per = 0;
+      for (const Map *m : ms) {
+        const __PSDomain &d = m->dom;
+        if (d.min[0] < d.max[0] && d.min[1] < d.max[1] && d.min[2] < d.max[2]) ++per;
+      }
+      for (; i + kGraphUnroll <= iter; i += kGraphUnroll) {
+        if (!cuda_ok(cudaGraphLaunch(g, rt->stream), "cudaGraphLaunch")) return false;
+        rt->launches += per * kGraphUnroll;
+      }
+    }
+  }
+  for (; i < iter; ++i)
+    if (!launch_iteration(ms)) return false;
+  return true;
+}
+
 bool run_maps(const std::vector<Map *> &ms, int iter) {
   std::chrono::steady_clock::time_point t0;
   if (rt->trace) {
@@ -736,9 +871,7 @@ bool run_maps(const std::vector<Map *> &ms, int iter) {
   } else if (ms.size() == 2 && temporal_pair(*ms[0], *ms[1])) {
     if (!run_temporal(*ms[0], iter)) return false;
   } else {
-    for (int i = 0; i < iter; ++i)
-      for (Map *m : ms)
-        if (!launch_map(*m, m->kernel == PS_KERNEL_HIMENO19_GOSA)) return false;
+    if (!run_plain(ms, iter)) return false;
   }
   if (rt->trace) {
     if (!sync_rt()) return false;
@@ -954,6 +1087,8 @@ void PSFinalize(void) {
     delete g;
   }
   rt->grids.clear();
+  for (GraphEntry &e : g_graphs) cudaGraphExecDestroy(e.exec);
+  g_graphs.clear();
   cudaFree(rt->dev_err);
   cudaFree(rt->partials);
   cudaFree(rt->ticket);
@@ -1037,6 +1172,7 @@ void PSGridFree(void *g) {
   if (!p) return;
   cudaStreamSynchronize(rt->stream);
   drop_tmaps(p->dev);
+  drop_graphs_for(p);
   cudaFree(p->dev);
   rt->grids.erase(p);
   p->magic = 0;
@@ -1131,6 +1267,11 @@ void PSStencilRunV(int n, const PSStencil *stencils, int iter) {
       fail(PS_ERR_BAD_HANDLE, "PSStencilRun: %d is not a stencil", stencils[i]);
       return;
     }
+    for (const Grid *g : m->grids)
+      if (!rt->grids.count(const_cast<Grid *>(g))) {
+        fail(PS_ERR_BAD_HANDLE, "PSStencilRun: stencil %d uses a freed grid", stencils[i]);
+        return;
+      }
     ms.push_back(m);
   }
   run_maps(ms, iter);

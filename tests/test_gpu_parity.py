@@ -523,3 +523,31 @@ def test_corrupt_tune_cache_is_skipped(rt, tmp_path):
     assert ps.last_error()[0] == ps.PS_ERR_IO
     ps.clear_error()
     ps.lib().PSClearTuning()
+
+
+# ---- CUDA graph replay of launch-bound runs ----------------------------------
+
+def test_graph_replay_matches_and_survives_reallocation(rt, oracle):
+    # 37 iterations: one ordinary, two 16-iteration graph replays, 4 ordinary
+    shape = (16, 24, 40)
+    for seed in (30, 31):  # second round: new grids at possibly reused addresses
+        init = synth.uniform(shape, seed)
+        n0 = ps.launch_count()
+        a, b = run_pingpong(ps.PS_KERNEL_DIFFUSION7, init, ps.full_domain(shape),
+                            DIFF_COEF, 37)
+        assert ps.launch_count() - n0 == 74
+        r1, r2 = init.copy(), np.zeros_like(init)
+        oracle.run7(oracle.V_DIFFUSION7, r1, r2, (0, 40, 0, 24, 0, 16), DIFF_COEF,
+                    iter=37)
+        assert np.array_equal(_bits(a), _bits(r1))
+        assert np.array_equal(_bits(b), _bits(r2))
+
+
+def test_run_with_freed_grid_is_rejected(rt):
+    g1, g2 = ps.Grid((8, 8, 8)), ps.Grid((8, 8, 8))
+    m = ps.stencil_map(ps.PS_KERNEL_COPY, ps.full_domain((8, 8, 8)), [g1, g2])
+    g2.free()
+    with pytest.raises(ps.PSError) as e:
+        ps.stencil_run([m])
+    assert e.value.code == ps.PS_ERR_BAD_HANDLE
+    g1.free()
