@@ -158,6 +158,22 @@ void PSClearTuning(void);               /* forgets all plans (not the file) */
 /* The plan a stencil runs with: returns 1 if tuned, 0 if the defaults. */
 int PSGetStencilPlan(PSStencil s, PSLaunchShape *shape, int *k, PSLaunchShape *tshape);
 
+/* ---- 4b. Batches of independent runs ------------------------------------ */
+
+/* No counterpart in the reference (Physis runs each PSStencilRun alone).
+ * Many independent runs of uneven sizes advance together, one persistent
+ * launch per time step over a (problem, z-chunk, tile) work list; runs of
+ * more than 16 iterations replay a CUDA graph of 16.  maps holds nruns x
+ * maps_per_run stencils (maps_per_run 1 or 2; the maps of one run share
+ * kernel and domain, e.g. the g1->g2 / g2->g1 pair).  Float grids of
+ * PS_KERNEL_DIFFUSION7, SUM7, COPY or HIMENO19.  A 7-point run uses the rows
+ * per thread of its tuned plan (PSGetStencilPlan) when it has one.
+ * Returns a batch id or -1. */
+int PSBatchCreate(int nruns, int maps_per_run, const PSStencil *maps);
+/* Runs `iter` iterations: every run executes its maps in order each time. */
+void PSBatchRun(int batch, int iter);
+void PSBatchFree(int batch);
+
 /* ---- 5. Reduction for callers that cannot allocate --------------------- */
 
 /* No counterpart in the reference.  PSReduce over a grid that the caller

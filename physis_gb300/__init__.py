@@ -51,7 +51,7 @@ PSGridCopyoutAsync PSHostAlloc PSHostFree PSSynchronize PSGetStream
 PSEventRecord PSEventElapsedMs PSGetLaunchCount PSGetSMCount PSSetLaunchShape
 PSGetLaunchShape PSTestFailNextAllocs PSTestDeviceWaitTimeout PSReduceNoAlloc
 PSSetTemporalBlocking PSGetTemporalBlocking PSSetAutotune PSSetTuneCachePath
-PSLoadTuneCache PSClearTuning PSGetStencilPlan""".split()
+PSLoadTuneCache PSClearTuning PSGetStencilPlan PSBatchCreate PSBatchRun PSBatchFree""".split()
 
 
 class PSDomain(ctypes.Structure):
@@ -146,6 +146,10 @@ def lib():
     L.PSGetStencilPlan.argtypes = [i, ctypes.POINTER(PSLaunchShape), ctypes.POINTER(i),
                                    ctypes.POINTER(PSLaunchShape)]
     L.PSGetStencilPlan.restype = i
+    L.PSBatchCreate.argtypes = [i, i, ctypes.POINTER(i)]
+    L.PSBatchCreate.restype = i
+    L.PSBatchRun.argtypes = [i, i]
+    L.PSBatchFree.argtypes = [i]
     L.PSReduceNoAlloc.argtypes = [vp, ctypes.c_size_t, i, i, i, i, i, vp, vp]
     L.PSReduceNoAlloc.restype = i
     _lib = L
@@ -325,6 +329,26 @@ def stencil_plan(s):
     check()
     return (bool(tuned), (sh.warps, sh.rows, sh.ns, sh.ns2, sh.ctas_per_sm), k.value,
             (tsh.warps, tsh.rows, tsh.ns))
+
+
+def batch_create(runs):
+    """runs: list of stencil lists (all of the same length, 1 or 2)."""
+    m = len(runs[0])
+    flat = [s for r in runs for s in r]
+    arr = (ctypes.c_int * len(flat))(*flat)
+    b = lib().PSBatchCreate(len(runs), m, arr)
+    check()
+    return b
+
+
+def batch_run(b, iter):
+    lib().PSBatchRun(b, iter)
+    check()
+
+
+def batch_free(b):
+    lib().PSBatchFree(b)
+    check()
 
 
 def launch_count():

@@ -25,53 +25,15 @@
 // * residual: FP32 per thread, FP32 warp-shuffle + block tree, one FP64
 //   partial per CTA, and the last CTA to finish (atomic ticket) adds the
 //   partials in FP64 in a fixed order (deterministic run to run).
-#include "ps_device.cuh"
-#include "ps_internal.h"
+#include "himeno_body.cuh"
 
 namespace psg {
 namespace {
 
-constexpr int kTX = 128;      // tile width in cells (32 lanes x float4)
-constexpr int kW = kTX + 8;   // shared p row width (4-cell halo each side)
-constexpr int kNumCoef = 12;  // a0 a1 a2 a3 b0 b1 b2 c0 c1 c2 bnd wrk1
-
 struct HimenoMaps {
-  CUtensorMap p;               // p0 with halo box {kW, TY+2, 1}
-  CUtensorMap coef[kNumCoef];  // box {kTX, TY, 1}
+  CUtensorMap p;               // p0 with halo box {kHimW, TY+2, 1}
+  CUtensorMap coef[kHimCoef];  // box {kHimTX, TY, 1}
 };
-
-struct HParams {
-  float *out;
-  int64_t row, plane;  // out pitch / plane in elements
-  int dmin0, dmin1, dmin2, dmax0, dmax1, dmax2;
-  int xbase, tiles_x, tiles, zlen;
-  int64_t items;
-  int nsp, nsc;
-  float omega;
-  double *partials;
-  unsigned *ticket;
-  double *result;
-  int *err;
-};
-
-__host__ __device__ constexpr int h_bar_bytes(int n) { return 128 * ((8 * n + 127) / 128); }
-// Every TMA destination starts on a 128-byte boundary.
-__host__ __device__ constexpr uint32_t h_align128(uint32_t b) { return (b + 127u) & ~127u; }
-
-__device__ __forceinline__ void row6(const float *pl, int idx, int lane, float (&r)[6]) {
-  float v[4];
-  ld16_shared<float>(v, pl + idx);
-  float l = shfl_up1(v[3]);
-  float rr = shfl_down1(v[0]);
-  if (lane == 0) l = pl[idx - 1];
-  if (lane == 31) rr = pl[idx + 4];
-  r[0] = l;
-  r[1] = v[0];
-  r[2] = v[1];
-  r[3] = v[2];
-  r[4] = v[3];
-  r[5] = rr;
-}
 
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
@@ -84,29 +46,14 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Position in a ring of mbarrier-signalled stages used in issue order.
-struct Ring {
-  int stage = 0;
-  uint32_t phase = 0;
-  __device__ __forceinline__ void advance(int n) {
-    if (++stage == n) {
-      stage = 0;
-      phase ^= 1u;
-    }
-  }
-};
-
 template <bool GOSA>
 __global__ void __launch_bounds__(256, 1)
 himeno19_kernel(const __grid_constant__ HimenoMaps maps, const HParams p) {
   typedef RN<float> R;
   const int TY = blockDim.y;
   const int nsp = p.nsp, nsc = p.nsc;
-  const uint32_t p_bytes = (uint32_t)(kW * (TY + 2) * 4);
+  const uint32_t p_bytes = (uint32_t)(kHimW * (TY + 2) * 4);
   const int p_elems = (int)(h_align128(p_bytes) / 4);  // stage stride
-  const int c_tile = kTX * TY;                         // elements per coefficient tile
-  const int c_elems = kNumCoef * c_tile;               // elements per coefficient stage
-  const uint32_t c_bytes = (uint32_t)(c_elems * 4);
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
@@ -127,127 +74,16 @@ himeno19_kernel(const __grid_constant__ HimenoMaps maps, const HParams p) {
   }
   __syncthreads();
 
-  Ring pprod, pcons, cprod, ccons;
+  HRing pprod, pcons, cprod, ccons;
   bool ok = true;
   float acc = 0.0f;
-  const int cen = (row + 1) * kW + 4 + lane * 4;
-  const int cidx = row * kTX + lane * 4;
-
   for (int64_t item = blockIdx.x; item < p.items && ok; item += gridDim.x) {
     const int chunk = (int)(item / p.tiles);
     const int tile = (int)(item - (int64_t)chunk * p.tiles);
     const int zs = p.dmin2 + chunk * p.zlen;
     const int ze = min(zs + p.zlen, p.dmax2);
-    const int x0 = p.xbase + (tile % p.tiles_x) * kTX;
-    const int y0 = p.dmin1 + (tile / p.tiles_x) * TY;
-    const int nplanes = ze - zs + 2;  // p planes zs-1 .. ze
-    const int ncoef = ze - zs;        // coefficient planes zs .. ze-1
-
-    auto issue_p = [&](int q) {
-      const int s = pprod.stage;
-      mbar_arrive_expect_tx(&pfull[s], p_bytes);
-      tma_load_3d(pring + s * p_elems, &maps.p, x0 - 4, y0 - 1, zs - 1 + q, &pfull[s]);
-      pprod.advance(nsp);
-    };
-    auto issue_c = [&](int r) {
-      const int s = cprod.stage;
-      mbar_arrive_expect_tx(&cfull[s], c_bytes);
-      float *dst = cring + s * c_elems;
-#pragma unroll 1
-      for (int a = 0; a < kNumCoef; ++a)
-        tma_load_3d(dst + a * c_tile, &maps.coef[a], x0, y0, zs + r, &cfull[s]);
-      cprod.advance(nsc);
-    };
-    auto wait_p = [&]() -> const float * {
-      if (!mbar_wait(&pfull[pcons.stage], pcons.phase, p.err)) ok = false;
-      const float *pl = pring + pcons.stage * p_elems;
-      pcons.advance(nsp);
-      return pl;
-    };
-    auto wait_c = [&]() -> const float * {
-      if (!mbar_wait(&cfull[ccons.stage], ccons.phase, p.err)) ok = false;
-      const float *pl = cring + ccons.stage * c_elems;
-      ccons.advance(nsc);
-      return pl;
-    };
-
-    if (tid == 0) {
-      for (int q = 0; q < min(nsp, nplanes); ++q) issue_p(q);
-      for (int r = 0; r < min(nsc, ncoef); ++r) issue_c(r);
-    }
-    const int y = y0 + row;
-    const int x = x0 + lane * 4;
-    const bool row_in = (y < p.dmax1);
-    const bool vec_in = (x >= p.dmin0) && (x + 4 <= p.dmax0);
-
-    const float *pm = wait_p();  // plane zs-1
-    const float *pc = wait_p();  // plane zs
-    for (int z = zs; z < ze; ++z) {
-      const int r = z - zs;
-      const float *pp = wait_p();  // plane z+1
-      const float *cf = wait_c();  // coefficients of plane z
-
-      float Zc[6], Zym[6], Zyp[6], Zpc[6], Zmc[6];
-      float Zpyp[4], Zpym[4], Zmyp[4], Zmym[4];
-      row6(pc, cen, lane, Zc);
-      row6(pc, cen - kW, lane, Zym);
-      row6(pc, cen + kW, lane, Zyp);
-      row6(pp, cen, lane, Zpc);
-      row6(pm, cen, lane, Zmc);
-      ld16_shared<float>(Zpyp, pp + cen + kW);
-      ld16_shared<float>(Zpym, pp + cen - kW);
-      ld16_shared<float>(Zmyp, pm + cen + kW);
-      ld16_shared<float>(Zmym, pm + cen - kW);
-      float co[kNumCoef][4];
-#pragma unroll
-      for (int a = 0; a < kNumCoef; ++a) ld16_shared<float>(co[a], cf + a * c_tile + cidx);
-
-      float o[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        // s0 = a0*p(k+1) + a1*p(j+1) + a2*p(i+1) + b0*(..) + b1*(..) + b2*(..)
-        //    + c0*p(k-1) + c1*p(j-1) + c2*p(i-1) + wrk1   (left to right)
-        float s0 = R::mul(co[0][i], Zpc[i + 1]);
-        s0 = R::add(s0, R::mul(co[1][i], Zyp[i + 1]));
-        s0 = R::add(s0, R::mul(co[2][i], Zc[i + 2]));
-        float t0 = R::add(R::sub(R::sub(Zpyp[i], Zpym[i]), Zmyp[i]), Zmym[i]);
-        s0 = R::add(s0, R::mul(co[4][i], t0));
-        float t1 = R::add(R::sub(R::sub(Zyp[i + 2], Zym[i + 2]), Zyp[i]), Zym[i]);
-        s0 = R::add(s0, R::mul(co[5][i], t1));
-        float t2 = R::add(R::sub(R::sub(Zpc[i + 2], Zmc[i + 2]), Zpc[i]), Zmc[i]);
-        s0 = R::add(s0, R::mul(co[6][i], t2));
-        s0 = R::add(s0, R::mul(co[7][i], Zmc[i + 1]));
-        s0 = R::add(s0, R::mul(co[8][i], Zym[i + 1]));
-        s0 = R::add(s0, R::mul(co[9][i], Zc[i]));
-        s0 = R::add(s0, co[11][i]);
-        // ss = (s0*a3 - p) * bnd ; p1 = p + omega*ss
-        const float ss = R::mul(R::sub(R::mul(s0, co[3][i]), Zc[i + 1]), co[10][i]);
-        o[i] = R::add(Zc[i + 1], R::mul(p.omega, ss));
-        if (GOSA) {
-          const bool in = row_in && (x + i >= p.dmin0) && (x + i < p.dmax0);
-          if (in) acc = R::add(acc, R::mul(ss, ss));
-        }
-      }
-      if (ok && row_in) {
-        float *dst = p.out + (int64_t)z * p.plane + (int64_t)y * p.row + x;
-        if (vec_in) {
-          st16_global<float>(dst, o);
-        } else {
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-            if (x + i >= p.dmin0 && x + i < p.dmax0) dst[i] = o[i];
-        }
-      }
-      pm = pc;
-      pc = pp;
-      ok = __syncthreads_and(ok);
-      if (!ok) break;
-      // p plane r (z-1) and coefficient plane r are consumed by every thread.
-      if (tid == 0) {
-        if (r + nsp < nplanes) issue_p(r + nsp);
-        if (r + nsc < ncoef) issue_c(r + nsc);
-      }
-    }
+    ok = himeno_item<GOSA>(&maps.p, maps.coef, p, pfull, cfull, pring, cring, tile, zs, ze,
+                           pprod, pcons, cprod, ccons, acc);
   }
   if (!ok) {
     if (tid == 0) {
@@ -289,8 +125,8 @@ himeno19_kernel(const __grid_constant__ HimenoMaps maps, const HParams p) {
 size_t himeno19_smem_bytes(const MarchConfig &cfg) {
   // 128 bytes of slack for aligning the dynamic shared-memory base
   return 128 + (size_t)h_bar_bytes(cfg.ns + cfg.ns2) +
-         (size_t)cfg.ns * h_align128((uint32_t)(kW * (cfg.warps + 2) * 4)) +
-         (size_t)cfg.ns2 * kNumCoef * kTX * cfg.warps * 4;
+         (size_t)cfg.ns * h_align128((uint32_t)(kHimW * (cfg.warps + 2) * 4)) +
+         (size_t)cfg.ns2 * kHimCoef * kHimTX * cfg.warps * 4;
 }
 
 cudaError_t launch_himeno19(const Himeno19Args &a, const MarchConfig &cfg,
@@ -298,7 +134,7 @@ cudaError_t launch_himeno19(const Himeno19Args &a, const MarchConfig &cfg,
                             int *dev_err, int sm_count, cudaStream_t s) {
   HimenoMaps maps;
   maps.p = tmaps[0];
-  for (int i = 0; i < kNumCoef; ++i) maps.coef[i] = tmaps[1 + i];
+  for (int i = 0; i < kHimCoef; ++i) maps.coef[i] = tmaps[1 + i];
   HParams p;
   const GridView &out = a.g[1];
   p.out = static_cast<float *>(out.ptr);
@@ -325,7 +161,7 @@ cudaError_t launch_himeno19(const Himeno19Args &a, const MarchConfig &cfg,
   if (cfg.warps < 1 || cfg.warps > 8 || cfg.ns < 3 || cfg.ns > 16 || cfg.ns2 < 1 ||
       cfg.ns2 > 8)
     return cudaErrorInvalidConfiguration;
-  p.tiles_x = (ex + kTX - 1) / kTX;
+  p.tiles_x = (ex + kHimTX - 1) / kHimTX;
   p.tiles = p.tiles_x * ((ey + cfg.warps - 1) / cfg.warps);
   const size_t smem = himeno19_smem_bytes(cfg);
   // Opt in to the dynamic shared memory this launch needs (the kernel also

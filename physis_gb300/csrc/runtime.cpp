@@ -31,6 +31,7 @@
 #include "physis_gb300/physis_gb300.h"
 #undef PSStencilRun
 #include "ps_internal.h"
+#include "batch.h"
 
 using psg::GridView;
 using psg::MarchConfig;
@@ -859,6 +860,175 @@ bool run_plain(const std::vector<Map *> &ms, int iter) {
   return true;
 }
 
+// ---- Batches of independent runs (batch.cu) --------------------------------
+
+struct Batch {
+  bool live = false;
+  int nruns = 0, maps_per_run = 0;
+  std::vector<const Map *> maps;      // nruns x maps_per_run (deque elements: stable)
+  std::vector<const Grid *> grids;    // every grid the batch touches
+  std::vector<void *> ptrs;           // their storage when the device tables were built
+  psg::BatchShape shape{};
+  psg::BatchProblem *probs_dev = nullptr;
+  CUtensorMap *tmaps_dev = nullptr;
+  int64_t total_items = 0;
+  int grid = 0;
+  cudaGraphExec_t graph = nullptr;    // maps_per_run x kGraphUnroll launches
+};
+std::vector<Batch> g_batches;
+
+void batch_release(Batch &b) {
+  if (b.graph) cudaGraphExecDestroy(b.graph);
+  if (b.probs_dev) cudaFree(b.probs_dev);
+  if (b.tmaps_dev) cudaFree(b.tmaps_dev);
+  b.graph = nullptr;
+  b.probs_dev = nullptr;
+  b.tmaps_dev = nullptr;
+}
+
+bool batch_kind_ok(int k) {
+  return k == PS_KERNEL_DIFFUSION7 || k == PS_KERNEL_SUM7 || k == PS_KERNEL_COPY ||
+         k == PS_KERNEL_HIMENO19;
+}
+
+// (Re)builds the device tables of a batch from its maps' current grids.
+bool batch_build(Batch &b) {
+  batch_release(b);
+  b.ptrs.clear();
+  for (const Grid *g : b.grids) b.ptrs.push_back(g->dev);
+  const int M = b.maps_per_run;
+  b.shape = psg::BatchShape{4, 1, 4, 5, 2};
+  std::vector<int> rows(b.nruns, 2);
+  for (int r = 0; r < b.nruns; ++r) {
+    const Map *m = b.maps[(size_t)r * M];
+    if (m->kernel != PS_KERNEL_HIMENO19 && m->has_plan &&
+        (m->plan.shape.rows == 1 || m->plan.shape.rows == 2 || m->plan.shape.rows == 4))
+      rows[r] = m->plan.shape.rows;
+    if (m->kernel != PS_KERNEL_HIMENO19 && rows[r] > b.shape.max_rows)
+      b.shape.max_rows = rows[r];
+  }
+  const int occ = psg::batch_occupancy(b.shape);
+  if (occ < 1) return fail(PS_ERR_CUDA, "batch kernel does not fit on an SM");
+  const int resident = rt->sm_count * occ;
+  std::vector<psg::BatchProblem> probs(b.nruns);
+  std::vector<CUtensorMap> tmaps;
+  int64_t item = 0;
+  for (int r = 0; r < b.nruns; ++r) {
+    psg::BatchProblem &bp = probs[r];
+    memset(&bp, 0, sizeof(bp));
+    const Map *m0 = b.maps[(size_t)r * M];
+    const Grid *g = m0->grids[0];
+    bp.kind = m0->kernel;
+    bp.rows = rows[r];
+    const int tyy = bp.kind == PS_KERNEL_HIMENO19 ? b.shape.warps : b.shape.warps * bp.rows;
+    const int xbase = (m0->dom.min[0] / 4) * 4;
+    const int tiles_x = (m0->dom.max[0] - xbase + 127) / 128;
+    bp.tiles = tiles_x * ((m0->dom.max[1] - m0->dom.min[1] + tyy - 1) / tyy);
+    const int nzd = m0->dom.max[2] - m0->dom.min[2];
+    bp.zlen = psg::choose_zchunk(bp.tiles, nzd, resident);
+    bp.items = (int64_t)bp.tiles * ((nzd + bp.zlen - 1) / bp.zlen);
+    bp.item_begin = item;
+    item += bp.items;
+    bp.dmin2 = m0->dom.min[2];
+    bp.dmax2 = m0->dom.max[2];
+    for (int par = 0; par < 2; ++par) {
+      const Map *m = b.maps[(size_t)r * M + (par % M)];
+      const GridView in = view(m->grids[0]), out = view(m->grids[1]);
+      CUtensorMap t;
+      const int box_h = (bp.kind == PS_KERNEL_HIMENO19 ? b.shape.warps : tyy) + 2;
+      if (!tmap_for(in, 136, box_h, &t)) return false;
+      bp.tmap[par] = (int)tmaps.size();
+      tmaps.push_back(t);
+      if (bp.kind == PS_KERNEL_HIMENO19) {
+        psg::HParams &h = bp.him[par];
+        h.out = static_cast<float *>(out.ptr);
+        h.row = out.pitch / 4;
+        h.plane = h.row * out.ny;
+        h.dmin0 = m->dom.min[0];
+        h.dmin1 = m->dom.min[1];
+        h.dmin2 = m->dom.min[2];
+        h.dmax0 = m->dom.max[0];
+        h.dmax1 = m->dom.max[1];
+        h.dmax2 = m->dom.max[2];
+        h.xbase = xbase;
+        h.tiles_x = tiles_x;
+        h.tiles = bp.tiles;
+        h.zlen = bp.zlen;
+        h.items = bp.items;
+        h.nsp = b.shape.nsp;
+        h.nsc = b.shape.nsc;
+        h.omega = (float)m->scalars[0];
+        h.err = rt->dev_err;
+        if (par == 0) {
+          bp.cmap = (int)tmaps.size();
+          for (int i = 0; i < 12; ++i) {
+            if (!tmap_for(view(m->grids[2 + i]), 128, b.shape.warps, &t)) return false;
+            tmaps.push_back(t);
+          }
+        }
+      } else {
+        psg::S7Params<float> &q = bp.s7[par];
+        q.out = static_cast<float *>(out.ptr);
+        q.row = out.pitch / 4;
+        q.plane = q.row * out.ny;
+        q.nx = g->dim[0];
+        q.ny = g->dim[1];
+        q.nz = g->dim[2];
+        q.dmin0 = m->dom.min[0];
+        q.dmin1 = m->dom.min[1];
+        q.dmin2 = m->dom.min[2];
+        q.dmax0 = m->dom.max[0];
+        q.dmax1 = m->dom.max[1];
+        q.dmax2 = m->dom.max[2];
+        q.xbase = xbase;
+        q.tiles_x = tiles_x;
+        q.tiles = bp.tiles;
+        q.zlen = bp.zlen;
+        q.items = bp.items;
+        q.ns = b.shape.ns7;
+        const double *c = m->scalars.data();
+        const bool has = m->scalars.size() >= 7;
+        q.ce = has ? (float)c[0] : 0.f;
+        q.cw = has ? (float)c[1] : 0.f;
+        q.cn = has ? (float)c[2] : 0.f;
+        q.cs = has ? (float)c[3] : 0.f;
+        q.ct = has ? (float)c[4] : 0.f;
+        q.cb = has ? (float)c[5] : 0.f;
+        q.cc = has ? (float)c[6] : 0.f;
+        q.err = rt->dev_err;
+      }
+    }
+  }
+  b.total_items = item;
+  b.grid = (int)std::min<int64_t>(resident, std::max<int64_t>(item, 1));
+  if (!cuda_ok(cudaMalloc(&b.probs_dev, sizeof(psg::BatchProblem) * probs.size()), "cudaMalloc") ||
+      !cuda_ok(cudaMalloc(&b.tmaps_dev, sizeof(CUtensorMap) * tmaps.size()), "cudaMalloc") ||
+      !cuda_ok(cudaMemcpyAsync(b.probs_dev, probs.data(), sizeof(psg::BatchProblem) * probs.size(),
+                               cudaMemcpyHostToDevice, rt->stream), "batch table copy") ||
+      !cuda_ok(cudaMemcpyAsync(b.tmaps_dev, tmaps.data(), sizeof(CUtensorMap) * tmaps.size(),
+                               cudaMemcpyHostToDevice, rt->stream), "batch map copy") ||
+      !cuda_ok(cudaStreamSynchronize(rt->stream), "cudaStreamSynchronize")) {
+    batch_release(b);
+    return false;
+  }
+  return true;
+}
+
+bool batch_launch(Batch &b, int parity) {
+  cudaError_t e = psg::launch_batch(b.probs_dev, b.nruns, b.tmaps_dev, b.total_items, parity,
+                                    b.shape, b.grid, rt->stream);
+  if (!cuda_ok(e, "batch launch")) return false;
+  ++rt->launches;
+  return true;
+}
+
+bool batch_stale(const Batch &b) {
+  if (!b.probs_dev) return true;
+  for (size_t i = 0; i < b.grids.size(); ++i)
+    if (b.grids[i]->dev != b.ptrs[i]) return true;
+  return false;
+}
+
 bool run_maps(const std::vector<Map *> &ms, int iter) {
   std::chrono::steady_clock::time_point t0;
   if (rt->trace) {
@@ -1089,6 +1259,8 @@ void PSFinalize(void) {
   rt->grids.clear();
   for (GraphEntry &e : g_graphs) cudaGraphExecDestroy(e.exec);
   g_graphs.clear();
+  for (Batch &b : g_batches) batch_release(b);
+  g_batches.clear();
   cudaFree(rt->dev_err);
   cudaFree(rt->partials);
   cudaFree(rt->ticket);
@@ -1515,6 +1687,111 @@ int PSReduceNoAlloc(const void *data, size_t pitch, int nx, int ny, int nz, int 
                                        static_cast<cudaStream_t>(stream), &why);
   if (code != PS_OK) fail(code, "PSReduceNoAlloc: %s", why);
   return code;
+}
+
+int PSBatchCreate(int nruns, int maps_per_run, const PSStencil *maps) {
+  if (!need_rt("PSBatchCreate")) return -1;
+  if (nruns < 1 || maps_per_run < 1 || maps_per_run > 2 || !maps) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSBatchCreate: %d runs of %d maps", nruns, maps_per_run);
+    return -1;
+  }
+  Batch b;
+  b.nruns = nruns;
+  b.maps_per_run = maps_per_run;
+  for (int r = 0; r < nruns; ++r) {
+    const Map *first = nullptr;
+    for (int j = 0; j < maps_per_run; ++j) {
+      const Map *m = lookup_map(maps[r * maps_per_run + j]);
+      if (!m) {
+        fail(PS_ERR_BAD_HANDLE, "PSBatchCreate: %d is not a stencil", maps[r * maps_per_run + j]);
+        return -1;
+      }
+      if (!batch_kind_ok(m->kernel) || m->grids[0]->type != PS_FLOAT) {
+        fail(PS_ERR_UNSUPPORTED,
+             "PSBatchCreate: batches take float maps of DIFFUSION7, SUM7, COPY or HIMENO19");
+        return -1;
+      }
+      const __PSDomain &d = m->dom;
+      if (d.min[0] >= d.max[0] || d.min[1] >= d.max[1] || d.min[2] >= d.max[2]) {
+        fail(PS_ERR_INVALID_ARGUMENT, "PSBatchCreate: empty domain");
+        return -1;
+      }
+      if (first) {
+        bool same = first->kernel == m->kernel;
+        for (int k = 0; k < 3; ++k)
+          same = same && first->dom.min[k] == d.min[k] && first->dom.max[k] == d.max[k];
+        if (!same) {
+          fail(PS_ERR_INVALID_ARGUMENT,
+               "PSBatchCreate: the maps of one run must share kernel and domain");
+          return -1;
+        }
+      }
+      first = first ? first : m;
+      b.maps.push_back(m);
+      for (const Grid *g : m->grids) b.grids.push_back(g);
+    }
+  }
+  if (!batch_build(b)) return -1;
+  b.live = true;
+  g_batches.push_back(b);
+  return (int)g_batches.size() - 1;
+}
+
+void PSBatchRun(int batch, int iter) {
+  if (!need_rt("PSBatchRun")) return;
+  if (batch < 0 || batch >= (int)g_batches.size() || !g_batches[batch].live) {
+    fail(PS_ERR_BAD_HANDLE, "PSBatchRun: %d is not a batch", batch);
+    return;
+  }
+  Batch &b = g_batches[batch];
+  for (const Grid *g : b.grids)
+    if (!rt->grids.count(const_cast<Grid *>(g))) {
+      fail(PS_ERR_BAD_HANDLE, "PSBatchRun: the batch uses a freed grid");
+      return;
+    }
+  if (batch_stale(b) && !batch_build(b)) return;
+  const int M = b.maps_per_run;
+  int i = 0;
+  if (graphs_enabled() && iter > kGraphUnroll) {
+    for (int p = 0; p < M; ++p)
+      if (!batch_launch(b, p)) return;
+    ++i;
+    if (!b.graph) {
+      cudaGraph_t graph = nullptr;
+      const long long l0 = rt->launches;
+      if (cudaStreamBeginCapture(rt->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        bool ok = true;
+        for (int u = 0; u < kGraphUnroll && ok; ++u)
+          for (int p = 0; p < M && ok; ++p) ok = batch_launch(b, p);
+        if (cudaStreamEndCapture(rt->stream, &graph) == cudaSuccess && ok && graph &&
+            cudaGraphInstantiate(&b.graph, graph, 0) != cudaSuccess)
+          b.graph = nullptr;
+        if (graph) cudaGraphDestroy(graph);
+      }
+      cudaGetLastError();
+      rt->launches = l0;
+    }
+    if (b.graph) {
+      for (; i + kGraphUnroll <= iter; i += kGraphUnroll) {
+        if (!cuda_ok(cudaGraphLaunch(b.graph, rt->stream), "cudaGraphLaunch")) return;
+        rt->launches += (long long)M * kGraphUnroll;
+      }
+    }
+  }
+  for (; i < iter; ++i)
+    for (int p = 0; p < M; ++p)
+      if (!batch_launch(b, p)) return;
+}
+
+void PSBatchFree(int batch) {
+  if (!need_rt("PSBatchFree")) return;
+  if (batch < 0 || batch >= (int)g_batches.size() || !g_batches[batch].live) {
+    fail(PS_ERR_BAD_HANDLE, "PSBatchFree: %d is not a batch", batch);
+    return;
+  }
+  cudaStreamSynchronize(rt->stream);
+  batch_release(g_batches[batch]);
+  g_batches[batch].live = false;
 }
 
 void PSSetAutotune(int on) {

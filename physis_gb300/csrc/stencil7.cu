@@ -32,228 +32,49 @@
 //   expression order, so every cell is bit-identical to the REF target.
 #include <type_traits>
 
-#include "ps_device.cuh"
-#include "ps_internal.h"
+#include "s7_body.cuh"
 
 namespace psg {
 namespace {
-
-template <typename T>
-struct S7Params {
-  T *out;
-  int64_t row;    // out pitch in elements
-  int64_t plane;  // out elements per z-plane
-  int nx, ny, nz;
-  int dmin0, dmin1, dmin2, dmax0, dmax1, dmax2;
-  int xbase;      // x of the first tile (multiple of VEC)
-  int tiles_x;    // tiles per y-band
-  int tiles;      // tiles_x * tiles per x-column
-  int zlen;       // planes per z-chunk
-  int64_t items;  // tiles * chunks
-  int ns;
-  T cc, cw, ce, cs, cn, cb, ct;  // expression order of DIFFUSION7
-  int *err;
-};
-
-__host__ __device__ constexpr int s7_bar_bytes(int ns) { return 128 * ((8 * ns + 127) / 128); }
-__host__ __device__ constexpr uint32_t s7_stage_bytes(uint32_t b) { return (b + 127u) & ~127u; }
 
 template <typename T, int K, int RY>
 __global__ void __launch_bounds__(512, 1)
 s7_march_kernel(const __grid_constant__ CUtensorMap tin, const S7Params<T> p) {
   constexpr int VEC = 16 / (int)sizeof(T);
-  constexpr int TX = 32 * VEC;
-  constexpr int W = TX + 2 * VEC;  // shared row width in elements
-  constexpr bool kClamp = (K == kKernelDiffusion7);
-  typedef RN<T> R;
-
+  constexpr int W = 34 * VEC;  // shared row width in elements
   const int TY = blockDim.y * RY;
   // Each ring stage starts on a 128-byte boundary (required of the shared
   // destination of cp.async.bulk.tensor).
   const uint32_t plane_bytes = (uint32_t)(W * (TY + 2) * sizeof(T));
   const int plane_elems = (int)(s7_stage_bytes(plane_bytes) / sizeof(T));
-  const int ns = p.ns;
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);
-  T *ring = reinterpret_cast<T *>(smem + s7_bar_bytes(ns));
+  T *ring = reinterpret_cast<T *>(smem + s7_bar_bytes(p.ns));
 
-  const int lane = threadIdx.x, warp = threadIdx.y;
-  const int tid = warp * 32 + lane;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
   if (tid == 0) {
     prefetch_tmap(&tin);
-    for (int s = 0; s < ns; ++s) mbar_init(&full[s], 1);
+    for (int s = 0; s < p.ns; ++s) mbar_init(&full[s], 1);
     fence_barrier_init();
   }
   __syncthreads();
 
-  // Producer state (thread 0) and consumer state (all threads): the stage
-  // that the next issued / next awaited plane uses, and its phase parity.
-  int pstage = 0;
-  uint32_t pphase = 0;
-  int cstage = 0;
-  uint32_t cphase = 0;
+  // Producer (thread 0) and consumer (all threads) positions in the ring.
+  RingPos prod, cons;
   bool ok = true;
-
-  const int rows0 = warp * RY;                          // first own row in the tile
-  const int cen0 = (rows0 + 1) * W + VEC + lane * VEC;  // own first row, centre
-
   for (int64_t item = blockIdx.x; item < p.items && ok; item += gridDim.x) {
     const int chunk = (int)(item / p.tiles);
     const int tile = (int)(item - (int64_t)chunk * p.tiles);
     const int zs = p.dmin2 + chunk * p.zlen;
     const int ze = min(zs + p.zlen, p.dmax2);
-    const int x0 = p.xbase + (tile % p.tiles_x) * TX;
-    const int y0 = p.dmin1 + (tile / p.tiles_x) * TY;
-    const int nplanes = ze - zs + 2;  // planes zs-1 .. ze
-
-    // Issues plane q (global plane zs-1+q) into the producer's next stage.
-    auto issue = [&](int q) {
-      mbar_arrive_expect_tx(&full[pstage], plane_bytes);
-      tma_load_3d(ring + pstage * plane_elems, &tin, x0 - VEC, y0 - 1, zs - 1 + q,
-                  &full[pstage]);
-      if (++pstage == ns) {
-        pstage = 0;
-        pphase ^= 1u;
-      }
-    };
-    // Waits for the next plane in issue order; returns its stage.
-    auto wait_next = [&]() -> const T * {
-      if (!mbar_wait(&full[cstage], cphase, p.err)) ok = false;
-      const T *pl = ring + cstage * plane_elems;
-      if (++cstage == ns) {
-        cstage = 0;
-        cphase ^= 1u;
-      }
-      return pl;
-    };
-
-    if (tid == 0) {
-      const int n0 = min(ns, nplanes);
-      for (int q = 0; q < n0; ++q) issue(q);
-    }
-    T b[RY][VEC], c[RY][VEC], t[RY][VEC];
-    const T *pm = wait_next();   // plane zs-1
-    const T *cur = wait_next();  // plane zs
-#pragma unroll
-    for (int r = 0; r < RY; ++r) {
-      ld16_shared<T>(c[r], cur + cen0 + r * W);
-      ld16_shared<T>(b[r], pm + cen0 + r * W);
-      if (kClamp && zs == 0) {
-#pragma unroll
-        for (int i = 0; i < VEC; ++i) b[r][i] = c[r][i];
-      }
-    }
-    ok = __syncthreads_and(ok);
-    if (!ok) break;
-    if (tid == 0 && ns < nplanes) issue(ns);
-
-    const int x = x0 + lane * VEC;
-    const int y = y0 + rows0;  // first own row
-    const bool vec_in = (x >= p.dmin0) && (x + VEC <= p.dmax0);
-    const bool west_face = kClamp && (x == 0);            // element 0 clamps west
-    const int east_elem = kClamp ? (p.nx - 1 - x) : -1;  // element clamping east
-
-    for (int z = zs; z < ze; ++z) {
-      const int q = z - zs + 1;  // plane index of z
-      const T *nxt = wait_next();
-      T n[VEC], s[VEC];
-#pragma unroll
-      for (int r = 0; r < RY; ++r) ld16_shared<T>(t[r], nxt + cen0 + r * W);
-      if (K != kKernelCopy) {
-        ld16_shared<T>(n, cur + cen0 - W);       // row above the column
-        ld16_shared<T>(s, cur + cen0 + RY * W);  // row below the column
-      }
-      if (kClamp && z == p.nz - 1) {
-#pragma unroll
-        for (int r = 0; r < RY; ++r)
-#pragma unroll
-          for (int i = 0; i < VEC; ++i) t[r][i] = c[r][i];
-      }
-#pragma unroll
-      for (int r = 0; r < RY; ++r) {
-        T o[VEC];
-        if (K == kKernelCopy) {
-#pragma unroll
-          for (int i = 0; i < VEC; ++i) o[i] = c[r][i];
-        } else {
-          T nn[VEC], ss[VEC];
-#pragma unroll
-          for (int i = 0; i < VEC; ++i) {
-            nn[i] = (r == 0) ? n[i] : c[r - 1][i];
-            ss[i] = (r == RY - 1) ? s[i] : c[r + 1][i];
-          }
-          if (kClamp) {
-            if (y + r == 0) {
-#pragma unroll
-              for (int i = 0; i < VEC; ++i) nn[i] = c[r][i];
-            }
-            if (y + r == p.ny - 1) {
-#pragma unroll
-              for (int i = 0; i < VEC; ++i) ss[i] = c[r][i];
-            }
-          }
-          T left = shfl_up1(c[r][VEC - 1]);
-          T right = shfl_down1(c[r][0]);
-          if (lane == 0) left = cur[cen0 + r * W - 1];
-          if (lane == 31) right = cur[cen0 + r * W + VEC];
-#pragma unroll
-          for (int i = 0; i < VEC; ++i) {
-            T w = (i == 0) ? left : c[r][i - 1];
-            T e = (i == VEC - 1) ? right : c[r][i + 1];
-            if (kClamp) {
-              if (i == 0 && west_face) w = c[r][0];
-              if (i == east_elem) e = c[r][i];
-              // cc*c + cw*w + ce*e + cs*s + cn*n + cb*b + ct*t, left to right
-              T v = R::mul(p.cc, c[r][i]);
-              v = R::add(v, R::mul(p.cw, w));
-              v = R::add(v, R::mul(p.ce, e));
-              v = R::add(v, R::mul(p.cs, ss[i]));
-              v = R::add(v, R::mul(p.cn, nn[i]));
-              v = R::add(v, R::mul(p.cb, b[r][i]));
-              v = R::add(v, R::mul(p.ct, t[r][i]));
-              o[i] = v;
-            } else {
-              // c + e + w + s + n + b + t, left to right
-              T v = R::add(c[r][i], e);
-              v = R::add(v, w);
-              v = R::add(v, ss[i]);
-              v = R::add(v, nn[i]);
-              v = R::add(v, b[r][i]);
-              v = R::add(v, t[r][i]);
-              o[i] = v;
-            }
-          }
-        }
-        if (ok && y + r < p.dmax1) {
-          T *dst = p.out + (int64_t)z * p.plane + (int64_t)(y + r) * p.row + x;
-          if (vec_in) {
-            st16_global<T>(dst, o);
-          } else {
-#pragma unroll
-            for (int i = 0; i < VEC; ++i)
-              if (x + i >= p.dmin0 && x + i < p.dmax0) dst[i] = o[i];
-          }
-        }
-      }
-#pragma unroll
-      for (int r = 0; r < RY; ++r)
-#pragma unroll
-        for (int i = 0; i < VEC; ++i) {
-          b[r][i] = c[r][i];
-          c[r][i] = t[r][i];
-        }
-      cur = nxt;
-      ok = __syncthreads_and(ok);
-      if (!ok) break;
-      // Plane q is consumed by every thread: refill its stage with q + ns.
-      if (tid == 0 && q + ns < nplanes) issue(q + ns);
-    }
+    ok = s7_item<T, K, RY>(&tin, p, full, ring, plane_elems, plane_bytes, TY, tile, zs, ze,
+                           prod, cons);
   }
   if (!ok && tid == 0) {
     // Give copies still in flight a bounded chance to land before exit.
-    for (int s = 0; s < ns; ++s) mbar_wait(&full[s], 0, nullptr, 1024);
+    for (int s = 0; s < p.ns; ++s) mbar_wait(&full[s], 0, nullptr, 1024);
   }
 }
 

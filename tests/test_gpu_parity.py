@@ -551,3 +551,74 @@ def test_run_with_freed_grid_is_rejected(rt):
         ps.stencil_run([m])
     assert e.value.code == ps.PS_ERR_BAD_HANDLE
     g1.free()
+
+
+# ---- batches of independent runs --------------------------------------------
+
+@pytest.mark.parametrize("iters", [3, 21])
+def test_batch_of_uneven_runs_bit_exact(rt, oracle, iters):
+    rng = np.random.default_rng(40)
+    runs, refs, keep = [], [], []
+    for i, shape in enumerate([(24, 40, 130), (9, 17, 33), (40, 8, 300)]):
+        init = synth.uniform(shape, 50 + i)
+        g1, g2 = ps.Grid(shape), ps.Grid(shape)
+        g1.copyin(init)
+        dom = ps.full_domain(shape)
+        runs.append([ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g1, g2], DIFF_COEF),
+                     ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g2, g1], DIFF_COEF)])
+        r1, r2 = init.copy(), np.zeros_like(init)
+        nz, ny, nx = shape
+        oracle.run7(oracle.V_DIFFUSION7, r1, r2, (0, nx, 0, ny, 0, nz), DIFF_COEF,
+                    iter=iters)
+        refs.append((g1, g2, r1, r2))
+    shape = (12, 19, 37)
+    init = rng.random(shape).astype(np.float32)
+    g1, g2 = ps.Grid(shape), ps.Grid(shape)
+    g1.copyin(init)
+    g2.copyin(init)
+    domt = (1, 36, 1, 18, 1, 11)
+    runs.append([ps.stencil_map(ps.PS_KERNEL_SUM7, ps.domain(*domt), [g1, g2]),
+                 ps.stencil_map(ps.PS_KERNEL_SUM7, ps.domain(*domt), [g2, g1])])
+    r1, r2 = init.copy(), init.copy()
+    oracle.run7(oracle.V_SUM7, r1, r2, domt, iter=iters)
+    refs.append((g1, g2, r1, r2))
+    for shape in [(20, 33, 130), (9, 11, 13)]:
+        arrays = _himeno_random(shape, 60 + shape[0])
+        gs = himeno_grids(shape, arrays)
+        keep.append(gs)
+        nz, ny, nx = shape
+        domt = (1, nx - 1, 1, ny - 1, 1, nz - 1)
+        dom = ps.domain(*domt)
+        runs.append([ps.stencil_map(ps.PS_KERNEL_HIMENO19, dom, gs, [0.8]),
+                     ps.stencil_map(ps.PS_KERNEL_HIMENO19, dom, [gs[1], gs[0]] + gs[2:],
+                                    [0.8])])
+        g = [a.copy() for a in arrays]
+        for _ in range(2 * iters):
+            oracle.himeno19(g, domt, np.float32(0.8))
+            g[0], g[1] = g[1], g[0]
+        refs.append((gs[0], gs[1], g[0], g[1]))
+    b = ps.batch_create(runs)
+    n0 = ps.launch_count()
+    ps.batch_run(b, iters)
+    assert ps.launch_count() - n0 == 2 * iters  # one launch per step for all runs
+    for ga, gb, ra, rb in refs:
+        assert np.array_equal(_bits(ga.copyout()), _bits(ra))
+        assert np.array_equal(_bits(gb.copyout()), _bits(rb))
+    ps.batch_free(b)
+    for ga, gb, _, _ in refs:
+        ga.free()
+        gb.free()
+    for gs in keep:
+        for g in gs[2:]:
+            g.free()
+
+
+def test_batch_rejects_unsupported(rt):
+    g1, g2 = ps.Grid((8, 8, 8), np.float64), ps.Grid((8, 8, 8), np.float64)
+    m = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, ps.full_domain((8, 8, 8)), [g1, g2],
+                       DIFF_COEF)
+    with pytest.raises(ps.PSError) as e:
+        ps.batch_create([[m]])
+    assert e.value.code == ps.PS_ERR_UNSUPPORTED
+    g1.free()
+    g2.free()
