@@ -494,6 +494,135 @@ def run_gpu_himeno(args, dist):
         g.free()
 
 
+# ---------------------------------------------------------------------------
+# Batched uneven grids (config 4)
+# ---------------------------------------------------------------------------
+
+def batch_dims(seed=2, n=48):
+    """(nx, ny, nz) per problem: X, Y in [32, 320], Z in [32, 512], rounded
+    to multiples of 8, from the SplitMix64 stream with the given seed."""
+    from physis_gb300 import synth
+    u = synth.uniform((n, 3), seed).astype(np.float64)
+    dims = []
+    for a, b, c in u:
+        nx = int(round((32 + a * (320 - 32)) / 8)) * 8
+        ny = int(round((32 + b * (320 - 32)) / 8)) * 8
+        nz = int(round((32 + c * (512 - 32)) / 8)) * 8
+        dims.append((nx, ny, nz))
+    return dims
+
+
+def run_gpu_batch(args, dist):
+    os.environ.setdefault("PS_DEVICE", str(dist.local))
+    import physis_gb300 as ps
+    from physis_gb300 import synth
+    ps.init()
+    L = ps.lib()
+    dims = batch_dims()
+    runs, grids, inputs = [], [], []
+    lups = 0.0
+    algo_bytes = 0.0
+    for i, (nx, ny, nz) in enumerate(dims):
+        shape = (nz, ny, nx)
+        init = synth.uniform(shape, 100 + i)
+        if i % 2 == 0:  # 7-point diffusion
+            g1, g2 = ps.Grid(shape), ps.Grid(shape)
+            g1.copyin(init)
+            dom = ps.full_domain(shape)
+            runs.append([ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g1, g2], COEF),
+                         ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g2, g1], COEF)])
+            grids.append([g1, g2])
+            inputs.append([(g1, init)])
+            lups += float(nx) * ny * nz
+            algo_bytes += 8.0 * nx * ny * nz
+        else:  # Himeno 19-point, config-3 coefficients, p uniform
+            arrays = himeno_arrays(nx, ny, nz)
+            arrays[0] = init
+            arrays[1] = init.copy()
+            gs = [ps.Grid(shape) for _ in range(14)]
+            for g, a in zip(gs, arrays):
+                g.copyin(a)
+            dom = ps.domain(1, nx - 1, 1, ny - 1, 1, nz - 1)
+            runs.append([ps.stencil_map(ps.PS_KERNEL_HIMENO19, dom, gs, [0.8]),
+                         ps.stencil_map(ps.PS_KERNEL_HIMENO19, dom,
+                                        [gs[1], gs[0]] + gs[2:], [0.8])])
+            grids.append(gs)
+            inputs.append([(gs[0], init), (gs[1], init)])
+            n_in = float(nx - 2) * (ny - 2) * (nz - 2)
+            lups += n_in
+            algo_bytes += 56.0 * n_in
+    K = args.steps  # time steps per problem (even)
+    it = max(1, K // 2)
+    b = ps.batch_create(runs)
+    ps.batch_run(b, 2)  # warm-up (also builds the graph cache on longer runs)
+    ps.synchronize()
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    n0 = ps.launch_count()
+    L.PSEventRecord(0)
+    ps.batch_run(b, it)
+    L.PSEventRecord(1)
+    ps.synchronize()
+    ms_batch = L.PSEventElapsedMs(0, 1)
+    launches = ps.launch_count() - n0
+    clk = clocks.stop()
+    # the same work as 48 separate runs, one after another on the same stream
+    for r in runs:
+        ps.stencil_run(r, 2)
+    ps.synchronize()
+    L.PSEventRecord(2)
+    for r in runs:
+        ps.stencil_run(r, it)
+    L.PSEventRecord(3)
+    ps.synchronize()
+    ms_sep = L.PSEventElapsedMs(2, 3)
+    steps = 2 * it
+    value = lups * steps / (ms_batch / 1e3) / 1e9
+    # end to end: copy every problem's input in (pinned), run, copy all out
+    import ctypes
+    pinned = []
+    for lst in inputs:
+        for g, a in lst:
+            h = L.PSHostAlloc(a.nbytes)
+            ctypes.memmove(h, a.ctypes.data, a.nbytes)
+            pinned.append((g, h, a.nbytes))
+    t0 = time.perf_counter()
+    for g, h, _ in pinned:
+        L.PSGridCopyinAsync(g.handle, h)
+    ps.batch_run(b, it)
+    for g, h, _ in pinned:
+        L.PSGridCopyoutAsync(g.handle, h)
+    ps.synchronize()
+    e2e_s = time.perf_counter() - t0
+    nbytes = sum(n for _, _, n in pinned)
+    for _, h, _ in pinned:
+        L.PSHostFree(h)
+    peak, peak_kind = measured_peaks()
+    achieved = algo_bytes * steps / (ms_batch / 1e3) / 1e9
+    line = {
+        "metric": "GLUPS, 48 uneven fp32 grids (24 x 7-point diffusion, 24 x Himeno "
+                  "19-point) in one persistent launch per step",
+        "value": value, "unit": "GLUPS", "n_gpus": 1, "steps": steps, "warmup": 4,
+        "ms_per_step": ms_batch / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic uniform[0,1) fields, dims from SplitMix64 seed 2",
+        "config": {"workload": "48 grids, X,Y in [32,320], Z in [32,512] (multiples of 8)",
+                   "cells": lups, "separate_runs_glups": lups * steps / (ms_sep / 1e3) / 1e9,
+                   "batch_over_separate": ms_sep / ms_batch},
+        "e2e": {"value": lups * steps / e2e_s / 1e9, "unit": "GLUPS",
+                "h2d_bytes_per_step": nbytes / steps, "d2h_bytes_per_step": nbytes / steps},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    ps.batch_free(b)
+    for gs in grids:
+        for g in gs:
+            g.free()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -509,7 +638,7 @@ def main():
     ap.add_argument("--n", type=int, default=512,
                     help="grid edge (default 512; smaller only for profiling)")
     ap.add_argument("--workload", default="diffusion",
-                    choices=["diffusion", "himeno"],
+                    choices=["diffusion", "himeno", "batch"],
                     help="diffusion: 7-point 512^3 (the headline); himeno: "
                          "19-point Jacobi 257x257x513 with fused residual")
     args = ap.parse_args()
@@ -523,6 +652,8 @@ def main():
             run_reference(args, dist)
         elif args.workload == "himeno":
             run_gpu_himeno(args, dist)
+        elif args.workload == "batch":
+            run_gpu_batch(args, dist)
         else:
             run_gpu(args, dist)
     finally:
