@@ -51,7 +51,8 @@ PSGridCopyoutAsync PSHostAlloc PSHostFree PSSynchronize PSGetStream
 PSEventRecord PSEventElapsedMs PSGetLaunchCount PSGetSMCount PSSetLaunchShape
 PSGetLaunchShape PSTestFailNextAllocs PSTestDeviceWaitTimeout PSReduceNoAlloc
 PSSetTemporalBlocking PSGetTemporalBlocking PSSetAutotune PSSetTuneCachePath
-PSLoadTuneCache PSClearTuning PSGetStencilPlan PSBatchCreate PSBatchRun PSBatchFree""".split()
+PSLoadTuneCache PSClearTuning PSGetStencilPlan PSBatchCreate PSBatchRun PSBatchFree
+PSSetBatchShape""".split()
 
 
 class PSDomain(ctypes.Structure):
@@ -150,6 +151,7 @@ def lib():
     L.PSBatchCreate.restype = i
     L.PSBatchRun.argtypes = [i, i]
     L.PSBatchFree.argtypes = [i]
+    L.PSSetBatchShape.argtypes = [i, i, i, i]
     L.PSReduceNoAlloc.argtypes = [vp, ctypes.c_size_t, i, i, i, i, i, vp, vp]
     L.PSReduceNoAlloc.restype = i
     _lib = L

@@ -11,8 +11,8 @@
 // problem by binary search over the problems' first item indices and runs
 // the shared per-item body (s7_body.cuh / himeno_body.cuh) with that
 // problem's parameters and tensor maps, both read from global memory.
-// Problem kinds: the 7-point family (DIFFUSION7, SUM7, COPY) and the plain
-// Himeno sweep, float grids.
+// Problem kinds: the 7-point family (DIFFUSION7, SUM7, COPY; 1 or 2 rows per
+// thread) and the plain Himeno sweep, float grids.
 #include "batch.h"
 #include "himeno_body.cuh"
 #include "s7_body.cuh"
@@ -31,17 +31,11 @@ __device__ __forceinline__ bool s7_rows(const BatchProblem &bp, int parity,
   const int TY = blockDim.y * bp.rows;
   const uint32_t plane_bytes = (uint32_t)(W * (TY + 2) * 4);
   const int plane_elems = (int)(s7_stage_bytes(plane_bytes) / 4);
-  switch (bp.rows) {
-    case 1:
-      return s7_item<float, K, 1>(tin, p, full, ring, plane_elems, plane_bytes, TY, tile, zs,
-                                  ze, prod, cons);
-    case 4:
-      return s7_item<float, K, 4>(tin, p, full, ring, plane_elems, plane_bytes, TY, tile, zs,
-                                  ze, prod, cons);
-    default:
-      return s7_item<float, K, 2>(tin, p, full, ring, plane_elems, plane_bytes, TY, tile, zs,
-                                  ze, prod, cons);
-  }
+  if (bp.rows == 1)
+    return s7_item<float, K, 1>(tin, p, full, ring, plane_elems, plane_bytes, TY, tile, zs, ze,
+                                prod, cons);
+  return s7_item<float, K, 2>(tin, p, full, ring, plane_elems, plane_bytes, TY, tile, zs, ze,
+                              prod, cons);
 }
 
 __global__ void __launch_bounds__(256, 1)

@@ -876,6 +876,8 @@ struct Batch {
   cudaGraphExec_t graph = nullptr;    // maps_per_run x kGraphUnroll launches
 };
 std::vector<Batch> g_batches;
+// {warps, max rows (computed per batch), 7-point stages, Himeno p / coef stages}
+psg::BatchShape g_batch_shape{4, 2, 4, 5, 2};
 
 void batch_release(Batch &b) {
   if (b.graph) cudaGraphExecDestroy(b.graph);
@@ -897,13 +899,13 @@ bool batch_build(Batch &b) {
   b.ptrs.clear();
   for (const Grid *g : b.grids) b.ptrs.push_back(g->dev);
   const int M = b.maps_per_run;
-  b.shape = psg::BatchShape{4, 1, 4, 5, 2};
+  b.shape = g_batch_shape;
+  b.shape.max_rows = 1;
   std::vector<int> rows(b.nruns, 2);
   for (int r = 0; r < b.nruns; ++r) {
     const Map *m = b.maps[(size_t)r * M];
-    if (m->kernel != PS_KERNEL_HIMENO19 && m->has_plan &&
-        (m->plan.shape.rows == 1 || m->plan.shape.rows == 2 || m->plan.shape.rows == 4))
-      rows[r] = m->plan.shape.rows;
+    if (m->kernel != PS_KERNEL_HIMENO19 && m->has_plan && m->plan.shape.rows == 1)
+      rows[r] = 1;
     if (m->kernel != PS_KERNEL_HIMENO19 && rows[r] > b.shape.max_rows)
       b.shape.max_rows = rows[r];
   }
@@ -1781,6 +1783,19 @@ void PSBatchRun(int batch, int iter) {
   for (; i < iter; ++i)
     for (int p = 0; p < M; ++p)
       if (!batch_launch(b, p)) return;
+}
+
+void PSSetBatchShape(int warps, int ns7, int nsp, int nsc) {
+  if (!need_rt("PSSetBatchShape")) return;
+  psg::BatchShape sh{warps, 2, ns7, nsp, nsc};
+  if (warps < 1 || warps > 8 || ns7 < 2 || ns7 > 8 || nsp < 3 || nsp > 8 || nsc < 1 ||
+      nsc > 4 || psg::batch_smem_bytes(sh) > 227 * 1024) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSSetBatchShape: warps %d ns7 %d nsp %d nsc %d", warps,
+         ns7, nsp, nsc);
+    return;
+  }
+  g_batch_shape = sh;
+  for (Batch &b : g_batches) batch_release(b);  // rebuilt on the next run
 }
 
 void PSBatchFree(int batch) {
