@@ -498,16 +498,16 @@ def run_gpu_himeno(args, dist):
 # Batched uneven grids (config 4)
 # ---------------------------------------------------------------------------
 
-def batch_dims(seed=2, n=48):
-    """(nx, ny, nz) per problem: X, Y in [32, 320], Z in [32, 512], rounded
-    to multiples of 8, from the SplitMix64 stream with the given seed."""
+def batch_dims(seed=2, n=48, xy=(32, 320), z=(32, 512)):
+    """(nx, ny, nz) per problem: X, Y in xy, Z in z, rounded to multiples of
+    8, from the SplitMix64 stream with the given seed."""
     from physis_gb300 import synth
     u = synth.uniform((n, 3), seed).astype(np.float64)
     dims = []
     for a, b, c in u:
-        nx = int(round((32 + a * (320 - 32)) / 8)) * 8
-        ny = int(round((32 + b * (320 - 32)) / 8)) * 8
-        nz = int(round((32 + c * (512 - 32)) / 8)) * 8
+        nx = int(round((xy[0] + a * (xy[1] - xy[0])) / 8)) * 8
+        ny = int(round((xy[0] + b * (xy[1] - xy[0])) / 8)) * 8
+        nz = int(round((z[0] + c * (z[1] - z[0])) / 8)) * 8
         dims.append((nx, ny, nz))
     return dims
 
@@ -518,7 +518,12 @@ def run_gpu_batch(args, dist):
     from physis_gb300 import synth
     ps.init()
     L = ps.lib()
-    dims = batch_dims()
+    if args.batch_small:
+        dims = batch_dims(xy=(16, 64), z=(16, 64))
+        label = "48 small grids, X,Y,Z in [16,64] (multiples of 8)"
+    else:
+        dims = batch_dims()
+        label = "48 grids, X,Y in [32,320], Z in [32,512] (multiples of 8)"
     runs, grids, inputs = [], [], []
     lups = 0.0
     algo_bytes = 0.0
@@ -606,7 +611,7 @@ def run_gpu_batch(args, dist):
         "ms_per_step": ms_batch / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic uniform[0,1) fields, dims from SplitMix64 seed 2",
-        "config": {"workload": "48 grids, X,Y in [32,320], Z in [32,512] (multiples of 8)",
+        "config": {"workload": label,
                    "cells": lups, "separate_runs_glups": lups * steps / (ms_sep / 1e3) / 1e9,
                    "batch_over_separate": ms_sep / ms_batch},
         "e2e": {"value": lups * steps / e2e_s / 1e9, "unit": "GLUPS",
@@ -637,6 +642,8 @@ def main():
     ap.add_argument("--ctas", type=int, default=0)
     ap.add_argument("--n", type=int, default=512,
                     help="grid edge (default 512; smaller only for profiling)")
+    ap.add_argument("--batch-small", action="store_true",
+                    help="batch workload with 48 small grids (launch-bound regime)")
     ap.add_argument("--workload", default="diffusion",
                     choices=["diffusion", "himeno", "batch"],
                     help="diffusion: 7-point 512^3 (the headline); himeno: "

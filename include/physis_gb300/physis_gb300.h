@@ -166,16 +166,17 @@ int PSGetStencilPlan(PSStencil s, PSLaunchShape *shape, int *k, PSLaunchShape *t
  * more than 16 iterations replay a CUDA graph of 16.  maps holds nruns x
  * maps_per_run stencils (maps_per_run 1 or 2; the maps of one run share
  * kernel and domain, e.g. the g1->g2 / g2->g1 pair).  Float grids of
- * PS_KERNEL_DIFFUSION7, SUM7, COPY or HIMENO19.  A 7-point run uses 2 rows
- * per thread, or 1 when its tuned plan (PSGetStencilPlan) says so.
+ * PS_KERNEL_DIFFUSION7, SUM7, COPY or HIMENO19.  A 7-point run uses the
+ * rows per thread of its tuned plan (PSGetStencilPlan) if it has one.
  * Returns a batch id or -1. */
 int PSBatchCreate(int nruns, int maps_per_run, const PSStencil *maps);
 /* Runs `iter` iterations: every run executes its maps in order each time. */
 void PSBatchRun(int batch, int iter);
 void PSBatchFree(int batch);
-/* Launch shape of batch kernels (default 4 warps, 4 / 5 / 2 stages): warps
- * per CTA, 7-point ring stages, Himeno p-ring and coefficient-ring stages. */
-void PSSetBatchShape(int warps, int ns7, int nsp, int nsc);
+/* Launch shape of batch kernels (default 4 warps, 4 rows, 4 / 4 / 2
+ * stages): warps per CTA, rows per thread of untuned 7-point runs (1, 2, 4),
+ * 7-point ring stages, Himeno p-ring and coefficient-ring stages. */
+void PSSetBatchShape(int warps, int rows, int ns7, int nsp, int nsc);
 
 /* ---- 5. Reduction for callers that cannot allocate --------------------- */
 

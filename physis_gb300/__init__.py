@@ -151,7 +151,7 @@ def lib():
     L.PSBatchCreate.restype = i
     L.PSBatchRun.argtypes = [i, i]
     L.PSBatchFree.argtypes = [i]
-    L.PSSetBatchShape.argtypes = [i, i, i, i]
+    L.PSSetBatchShape.argtypes = [i, i, i, i, i]
     L.PSReduceNoAlloc.argtypes = [vp, ctypes.c_size_t, i, i, i, i, i, vp, vp]
     L.PSReduceNoAlloc.restype = i
     _lib = L

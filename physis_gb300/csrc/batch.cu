@@ -11,8 +11,8 @@
 // problem by binary search over the problems' first item indices and runs
 // the shared per-item body (s7_body.cuh / himeno_body.cuh) with that
 // problem's parameters and tensor maps, both read from global memory.
-// Problem kinds: the 7-point family (DIFFUSION7, SUM7, COPY; 1 or 2 rows per
-// thread) and the plain Himeno sweep, float grids.
+// Problem kinds: the 7-point family (DIFFUSION7, SUM7, COPY; 1, 2 or 4 rows
+// per thread) and the plain Himeno sweep, float grids.
 #include "batch.h"
 #include "himeno_body.cuh"
 #include "s7_body.cuh"
@@ -34,7 +34,10 @@ __device__ __forceinline__ bool s7_rows(const BatchProblem &bp, int parity,
   if (bp.rows == 1)
     return s7_item<float, K, 1>(tin, p, full, ring, plane_elems, plane_bytes, TY, tile, zs, ze,
                                 prod, cons);
-  return s7_item<float, K, 2>(tin, p, full, ring, plane_elems, plane_bytes, TY, tile, zs, ze,
+  if (bp.rows == 2)
+    return s7_item<float, K, 2>(tin, p, full, ring, plane_elems, plane_bytes, TY, tile, zs, ze,
+                                prod, cons);
+  return s7_item<float, K, 4>(tin, p, full, ring, plane_elems, plane_bytes, TY, tile, zs, ze,
                               prod, cons);
 }
 

@@ -877,7 +877,8 @@ struct Batch {
 };
 std::vector<Batch> g_batches;
 // {warps, max rows (computed per batch), 7-point stages, Himeno p / coef stages}
-psg::BatchShape g_batch_shape{4, 2, 4, 5, 2};
+psg::BatchShape g_batch_shape{4, 4, 4, 4, 2};
+int g_batch_rows = 4;  // rows per thread of untuned 7-point runs in a batch
 
 void batch_release(Batch &b) {
   if (b.graph) cudaGraphExecDestroy(b.graph);
@@ -901,11 +902,12 @@ bool batch_build(Batch &b) {
   const int M = b.maps_per_run;
   b.shape = g_batch_shape;
   b.shape.max_rows = 1;
-  std::vector<int> rows(b.nruns, 2);
+  std::vector<int> rows(b.nruns, g_batch_rows);
   for (int r = 0; r < b.nruns; ++r) {
     const Map *m = b.maps[(size_t)r * M];
-    if (m->kernel != PS_KERNEL_HIMENO19 && m->has_plan && m->plan.shape.rows == 1)
-      rows[r] = 1;
+    if (m->kernel != PS_KERNEL_HIMENO19 && m->has_plan &&
+        (m->plan.shape.rows == 1 || m->plan.shape.rows == 2 || m->plan.shape.rows == 4))
+      rows[r] = m->plan.shape.rows;
     if (m->kernel != PS_KERNEL_HIMENO19 && rows[r] > b.shape.max_rows)
       b.shape.max_rows = rows[r];
   }
@@ -1785,16 +1787,18 @@ void PSBatchRun(int batch, int iter) {
       if (!batch_launch(b, p)) return;
 }
 
-void PSSetBatchShape(int warps, int ns7, int nsp, int nsc) {
+void PSSetBatchShape(int warps, int rows, int ns7, int nsp, int nsc) {
   if (!need_rt("PSSetBatchShape")) return;
-  psg::BatchShape sh{warps, 2, ns7, nsp, nsc};
-  if (warps < 1 || warps > 8 || ns7 < 2 || ns7 > 8 || nsp < 3 || nsp > 8 || nsc < 1 ||
-      nsc > 4 || psg::batch_smem_bytes(sh) > 227 * 1024) {
+  psg::BatchShape sh{warps, 4, ns7, nsp, nsc};
+  if (warps < 1 || warps > 8 || !(rows == 1 || rows == 2 || rows == 4) || ns7 < 2 ||
+      ns7 > 8 || nsp < 3 || nsp > 8 || nsc < 1 || nsc > 4 ||
+      psg::batch_smem_bytes(sh) > 227 * 1024) {
     fail(PS_ERR_INVALID_ARGUMENT, "PSSetBatchShape: warps %d ns7 %d nsp %d nsc %d", warps,
          ns7, nsp, nsc);
     return;
   }
   g_batch_shape = sh;
+  g_batch_rows = rows;
   for (Batch &b : g_batches) batch_release(b);  // rebuilt on the next run
 }
 
