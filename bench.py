@@ -229,6 +229,88 @@ def run_reference(args, dist):
 
 
 # ---------------------------------------------------------------------------
+# The reference's own hand-written CUDA diffusion kernels, on the same GPU
+# ---------------------------------------------------------------------------
+
+# (label, cubin, mangled name, block, grid(n), dynamic smem, steps per launch):
+# launch geometry of examples/diffusion-benchmark/diffusion3d_cuda.cu:322-333,
+# diffusion3d_cuda_shared.cu:110-121 and diffusion3d_cuda_temporal_blocking.cu:
+# 289-309 (block sizes diffusion3d_cuda.h:15, 50-51 and
+# diffusion3d_cuda_temporal_blocking.h:16-17).
+REF_CUDA = [
+    ("diffusion_kernel (thread per x,y column, block 64x4; the translator's "
+     "CUDA target has this shape)", "diffusion3d_cuda.cubin",
+     "_ZN11diffusion3d16diffusion_kernelEPfS0_iiifffffff", (64, 4, 1),
+     lambda n: (n // 64, n // 4, 1), 0, 1),
+    ("diffusion_kernel_shared (2.5D shared memory, block 128x2)",
+     "diffusion3d_cuda_shared.cubin",
+     "_ZN11diffusion3d23diffusion_kernel_sharedEPfS0_iiifffffff", (128, 2, 1),
+     lambda n: (n // 128, n // 2, 1), 0, 1),
+    ("diffusion_kernel_temporal_blocking2 (2 steps per launch, block 32x16)",
+     "diffusion3d_cuda_temporal_blocking.cubin",
+     "_ZN11diffusion3d35diffusion_kernel_temporal_blocking2EPfS0_iiifffffff",
+     (32, 16, 1), lambda n: ((n + 29) // 30, (n + 13) // 14, 1), 3 * 32 * 16 * 4, 2),
+]
+
+
+def reference_cuda_kernels(ps, g1, g2, steps):
+    """Times the reference's hand-written CUDA diffusion kernels, compiled
+    from its sources for sm_103a (oracle/Makefile, cubins in oracle/_ref/),
+    on the same 512^3 grids and stream.  GLUPS per kernel, or why not."""
+    import ctypes
+    L = ps.lib()
+    n = N
+    if ps.lib().PSGridPitch(g1.handle) != n * 4:
+        return {"unavailable": "needs dense rows (pitch == nx*4)"}
+    try:
+        cu = ctypes.CDLL("libcuda.so.1")
+    except OSError as e:
+        return {"unavailable": f"libcuda.so.1: {e}"}
+    cu.cuInit(0)
+    out = {}
+    ptrs = [ctypes.c_void_p(L.PSGridDevicePtr(g1.handle)),
+            ctypes.c_void_p(L.PSGridDevicePtr(g2.handle))]
+    stream = ctypes.c_void_p(L.PSGetStream())
+    for label, cubin, sym, block, gridf, smem, per in REF_CUDA:
+        path = os.path.join(ROOT, "oracle", "_ref", cubin)
+        if not os.path.exists(path):
+            out[label] = "unavailable: cubin not built (needs the reference tree)"
+            continue
+        mod, fn = ctypes.c_void_p(), ctypes.c_void_p()
+        if cu.cuModuleLoad(ctypes.byref(mod), path.encode()) != 0 or \
+                cu.cuModuleGetFunction(ctypes.byref(fn), mod, sym.encode()) != 0:
+            out[label] = "unavailable: cuModuleLoad/GetFunction failed"
+            continue
+        grid = gridf(n)
+        coefs = [ctypes.c_float(c) for c in COEF]  # ce cw cn cs ct cb cc
+
+        def launch(i):
+            a = [ptrs[i % 2], ptrs[(i + 1) % 2], ctypes.c_int(n), ctypes.c_int(n),
+                 ctypes.c_int(n)] + coefs
+            params = (ctypes.c_void_p * len(a))(
+                *[ctypes.cast(ctypes.pointer(x), ctypes.c_void_p) for x in a])
+            return cu.cuLaunchKernel(fn, grid[0], grid[1], grid[2], block[0], block[1],
+                                     block[2], smem, stream, params, None)
+
+        count = max(1, steps // per)
+        rc = 0
+        for i in range(3):
+            rc |= launch(i)
+        L.PSEventRecord(4)
+        for i in range(count):
+            rc |= launch(i)
+        L.PSEventRecord(5)
+        ms = L.PSEventElapsedMs(4, 5)
+        cu.cuModuleUnload(mod)
+        if rc != 0:
+            out[label] = f"unavailable: cuLaunchKernel returned {rc}"
+            continue
+        out[label] = {"glups": float(n) ** 3 * count * per / (ms / 1e3) / 1e9,
+                      "ms_per_step": ms / (count * per)}
+    return out
+
+
+# ---------------------------------------------------------------------------
 # GPU leg
 # ---------------------------------------------------------------------------
 
@@ -308,6 +390,9 @@ def run_gpu(args, dist):
     peak, peak_kind = measured_peaks()
     achieved = cells * BYTES_PER_LUP / (ms / K / 1e3) / 1e9
     traffic = profiled_traffic()
+    ref_cuda = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        ref_cuda = reference_cuda_kernels(ps, g1, g2, min(K, 200))
     shape_used = ps.get_launch_shape(ps.PS_KERNEL_DIFFUSION7)
 
     cpu = None
@@ -345,6 +430,7 @@ def run_gpu(args, dist):
             "hbm_gbs_achieved": achieved,
             "clocks": clk,
             "cpu_baseline": cpu,
+            "reference_cuda_kernels": ref_cuda,
         }
         print(json.dumps(line), flush=True)
     g1.free()
