@@ -49,7 +49,8 @@ struct TParams {
 __host__ __device__ constexpr int t_bar_bytes(int ns) { return 128 * ((8 * ns + 127) / 128); }
 __host__ __device__ constexpr uint32_t t_align128(uint32_t b) { return (b + 127u) & ~127u; }
 
-// One clamped diffusion update of a 16-byte vector of one row.
+// One diffusion update of a 16-byte vector of one row; with CLAMP, the
+// neighbours across the grid's x faces are replaced by the centre.
 template <typename T, int VEC, bool CLAMP>
 __device__ __forceinline__ void diffuse_row(const T (&c)[VEC], const T (&n)[VEC],
                                             const T (&s)[VEC], const T (&b)[VEC],
@@ -76,15 +77,111 @@ __device__ __forceinline__ void diffuse_row(const T (&c)[VEC], const T (&n)[VEC]
   }
 }
 
-template <typename T, int RY, int KMAX>
+// Per-item constants of a pass.
+template <typename T>
+struct T7Item {
+  T *bufs;
+  int plane_elems, cen0, lane, rows0, x, y, TYO, zs, ze;
+  bool west_face, out_lane, vec_in;
+  int east_elem;
+};
+
+// One pipeline step: the TMA plane `in_t` is input plane s.  Each stage's
+// three register planes rotate roles with the step (ROT): b = slot ROT,
+// c = slot ROT+1, t = slot ROT+2 (mod 3); a stage writes its output straight
+// into the next stage's t slot, so no plane is ever copied between
+// registers.  CL: the item's extended tile touches a grid face in x or y.
+template <typename T, int RY, int K, int ROT, bool CL>
+__device__ __forceinline__ void t7_step(T (&Q)[K][3][RY][16 / sizeof(T)], const T *in_t,
+                                        const T *prev_in, int s, const TParams<T> &p,
+                                        const T7Item<T> &it, bool ok) {
+  constexpr int VEC = 16 / (int)sizeof(T);
+  constexpr int W = 34 * VEC;
+  constexpr int BS = ROT, CS = (ROT + 1) % 3, TS = (ROT + 2) % 3;
+  const int cen0 = it.cen0, lane = it.lane;
+#pragma unroll
+  for (int r = 0; r < RY; ++r) ld16_shared<T>(Q[0][TS][r], in_t + cen0 + r * W);
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    const int pz = s - 1 - j;  // plane stage j computes
+    const T *nb = (j == 0) ? prev_in : it.bufs + ((j - 1) * 2 + (pz & 1)) * it.plane_elems;
+    if (pz == 0) {  // clamp below the first plane: b = c
+#pragma unroll
+      for (int r = 0; r < RY; ++r)
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) Q[j][BS][r][i] = Q[j][CS][r][i];
+    }
+    if (pz == p.nz - 1) {  // clamp above the last plane: t = c
+#pragma unroll
+      for (int r = 0; r < RY; ++r)
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) Q[j][TS][r][i] = Q[j][CS][r][i];
+    }
+    T nrow[VEC], srow[VEC];
+    ld16_shared<T>(nrow, nb + cen0 - W);
+    ld16_shared<T>(srow, nb + cen0 + RY * W);
+#pragma unroll
+    for (int r = 0; r < RY; ++r) {
+      T nn[VEC], ss[VEC];
+#pragma unroll
+      for (int i = 0; i < VEC; ++i) {
+        nn[i] = (r == 0) ? nrow[i] : Q[j][CS][r - 1][i];
+        ss[i] = (r == RY - 1) ? srow[i] : Q[j][CS][r + 1][i];
+      }
+      if (CL) {
+        if (it.y + r == 0) {
+#pragma unroll
+          for (int i = 0; i < VEC; ++i) nn[i] = Q[j][CS][r][i];
+        }
+        if (it.y + r == p.ny - 1) {
+#pragma unroll
+          for (int i = 0; i < VEC; ++i) ss[i] = Q[j][CS][r][i];
+        }
+      }
+      T left = shfl_up1(Q[j][CS][r][VEC - 1]);
+      T right = shfl_down1(Q[j][CS][r][0]);
+      if (lane == 0) left = nb[cen0 + r * W - 1];
+      if (lane == 31) right = nb[cen0 + r * W + VEC];
+      if (j < K - 1) {
+        diffuse_row<T, VEC, CL>(Q[j][CS][r], nn, ss, Q[j][BS][r], Q[j][TS][r], left, right,
+                                it.west_face, it.east_elem, p, Q[(j + 1) % K][TS][r]);
+      } else {
+        T o[VEC];
+        diffuse_row<T, VEC, CL>(Q[j][CS][r], nn, ss, Q[j][BS][r], Q[j][TS][r], left, right,
+                                it.west_face, it.east_elem, p, o);
+        const int er = it.rows0 + r;  // row within E
+        const int gy = it.y + r;
+        if (ok && pz >= it.zs && pz < it.ze && it.out_lane && er >= K - 1 &&
+            er < K - 1 + it.TYO && gy < p.ny) {
+          T *g = p.out + (int64_t)pz * p.plane + (int64_t)gy * p.row + it.x;
+          if (it.vec_in) {
+            st16_global<T>(g, o);
+          } else {
+#pragma unroll
+            for (int i = 0; i < VEC; ++i)
+              if (it.x + i < p.nx) g[i] = o[i];
+          }
+        }
+      }
+    }
+    if (j < K - 1) {  // neighbours of this output for the next stage
+      T *dst = it.bufs + (j * 2 + (pz & 1)) * it.plane_elems;
+#pragma unroll
+      for (int r = 0; r < RY; ++r)
+        *reinterpret_cast<uint4 *>(dst + cen0 + r * W) =
+            *reinterpret_cast<const uint4 *>(Q[(j + 1) % K][TS][r]);
+    }
+  }
+}
+
+template <typename T, int RY, int K>
 __global__ void __launch_bounds__(256, 1)
 t7_kernel(const __grid_constant__ CUtensorMap tin, const TParams<T> p) {
   constexpr int VEC = 16 / (int)sizeof(T);
   constexpr int W = 34 * VEC;   // shared row width (E plus a VEC apron each side)
   constexpr int TXO = 30 * VEC; // output columns per tile
-  const int k = p.k;
   const int TYE = blockDim.y * RY;
-  const int TYO = TYE - 2 * (k - 1);
+  const int TYO = TYE - 2 * (K - 1);
   const uint32_t plane_bytes = (uint32_t)(W * (TYE + 2) * sizeof(T));
   const int plane_elems = (int)(t_align128(plane_bytes) / sizeof(T));
   const int ns = p.ns;
@@ -93,7 +190,7 @@ t7_kernel(const __grid_constant__ CUtensorMap tin, const TParams<T> p) {
   unsigned char *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem);
   T *ring = reinterpret_cast<T *>(smem + t_bar_bytes(ns));
-  T *bufs = ring + ns * plane_elems;  // (k-1) stages x 2 slots
+  T *bufs = ring + ns * plane_elems;  // (K-1) stages x 2 slots
 
   const int lane = threadIdx.x, warp = threadIdx.y;
   const int tid = warp * 32 + lane;
@@ -105,26 +202,32 @@ t7_kernel(const __grid_constant__ CUtensorMap tin, const TParams<T> p) {
   }
   // Zero the stage buffers once: their aprons are never written, and zeros
   // keep the (discarded) border cells finite.
-  for (int i = tid; i < (k - 1) * 2 * plane_elems; i += nthreads) bufs[i] = T(0);
+  for (int i = tid; i < (K - 1) * 2 * plane_elems; i += nthreads) bufs[i] = T(0);
   __syncthreads();
 
   int pstage = 0, cstage = 0;
   uint32_t pphase = 0, cphase = 0;
   bool ok = true;
-  const int rows0 = warp * RY;
-  const int cen0 = (rows0 + 1) * W + VEC + lane * VEC;
+  T7Item<T> it;
+  it.bufs = bufs;
+  it.plane_elems = plane_elems;
+  it.lane = lane;
+  it.rows0 = warp * RY;
+  it.cen0 = (it.rows0 + 1) * W + VEC + lane * VEC;
+  it.TYO = TYO;
+  it.out_lane = (lane >= 1 && lane <= 30);
 
   for (int64_t item = blockIdx.x; item < p.items && ok; item += gridDim.x) {
     const int chunk = (int)(item / p.tiles);
     const int tile = (int)(item - (int64_t)chunk * p.tiles);
-    const int zs = chunk * p.zlen;
-    const int ze = min(zs + p.zlen, p.nz);
+    it.zs = chunk * p.zlen;
+    it.ze = min(it.zs + p.zlen, p.nz);
     const int xo0 = (tile % p.tiles_x) * TXO;
     const int yo0 = (tile / p.tiles_x) * TYO;
-    const int xe0 = xo0 - VEC;          // E's first column
-    const int ye0 = yo0 - (k - 1);      // E's first row
-    const int zin0 = zs - k;            // first input plane
-    const int nplanes = ze - zs + 2 * k;
+    const int xe0 = xo0 - VEC;      // E's first column
+    const int ye0 = yo0 - (K - 1);  // E's first row
+    const int zin0 = it.zs - K;     // first input plane
+    const int nplanes = it.ze - it.zs + 2 * K;
 
     auto issue = [&](int q) {
       mbar_arrive_expect_tx(&full[pstage], plane_bytes);
@@ -148,138 +251,66 @@ t7_kernel(const __grid_constant__ CUtensorMap tin, const TParams<T> p) {
       const int n0 = min(ns, nplanes);
       for (int q = 0; q < n0; ++q) issue(q);
     }
+    it.x = xe0 + lane * VEC;
+    it.y = ye0 + it.rows0;
+    it.west_face = (it.x == 0);
+    it.east_elem = p.nx - 1 - it.x;
+    it.vec_in = it.out_lane && (it.x + VEC <= p.nx);
+    // Does E contain a cell on a grid face in x or y?  (z faces are uniform
+    // per plane and handled in every item.)
+    const bool edge = xe0 <= 0 || xe0 + 32 * VEC >= p.nx || ye0 <= 0 || ye0 + TYE >= p.ny;
 
-    // Global coordinates of this thread's cells and the clamp selectors.
-    const int x = xe0 + lane * VEC;
-    const int y = ye0 + rows0;
-    const bool west_face = (x == 0);
-    const int east_elem = p.nx - 1 - x;
-    // Output ownership: lanes 1..30, rows [k-1, k-1+TYO) of E, inside the grid.
-    const bool out_lane = (lane >= 1 && lane <= 30);
-    const bool vec_in = out_lane && (x + VEC <= p.nx);
-
-    T qb[KMAX][RY][VEC], qc[KMAX][RY][VEC];
+    T Q[K][3][RY][VEC];
     {
-      const T *p0 = wait_next();  // input plane zs-k
-      const T *p1 = wait_next();  // input plane zs-k+1
+      const T *p0 = wait_next();  // input plane zs-K
+      const T *p1 = wait_next();  // input plane zs-K+1
 #pragma unroll
       for (int r = 0; r < RY; ++r) {
-        ld16_shared<T>(qb[0][r], p0 + cen0 + r * W);
-        ld16_shared<T>(qc[0][r], p1 + cen0 + r * W);
+        ld16_shared<T>(Q[0][0][r], p0 + it.cen0 + r * W);
+        ld16_shared<T>(Q[0][1][r], p1 + it.cen0 + r * W);
       }
 #pragma unroll
-      for (int j = 1; j < KMAX; ++j)
+      for (int j = 1; j < K; ++j)
 #pragma unroll
-        for (int r = 0; r < RY; ++r)
+        for (int a = 0; a < 2; ++a)
 #pragma unroll
-          for (int i = 0; i < VEC; ++i) {
-            qb[j][r][i] = T(0);
-            qc[j][r][i] = T(0);
-          }
+          for (int r = 0; r < RY; ++r)
+#pragma unroll
+            for (int i = 0; i < VEC; ++i) Q[j][a][r][i] = T(0);
     }
     ok = __syncthreads_and(ok);
     if (!ok) break;
     if (tid == 0 && ns < nplanes) issue(ns);
-    const T *prev_in = ring + ((cstage + ns - 1) % ns) * plane_elems;  // plane q-1
+    const T *prev_in = ring + ((cstage + ns - 1) % ns) * plane_elems;  // plane 1
 
-    for (int q = 2; q < nplanes; ++q) {
-      const int s = zin0 + q;  // newest input plane
-      const T *in_t = wait_next();
-      T t[RY][VEC];
-#pragma unroll
-      for (int r = 0; r < RY; ++r) ld16_shared<T>(t[r], in_t + cen0 + r * W);
-#pragma unroll
-      for (int j = 0; j < KMAX; ++j) {
-        if (j < k) {
-          const int pz = s - 1 - j;  // plane stage j computes
-          // x/y neighbours of plane pz of this stage's input
-          const T *nb = (j == 0) ? prev_in : bufs + ((j - 1) * 2 + (pz & 1)) * plane_elems;
-          if (pz == 0) {
-#pragma unroll
-            for (int r = 0; r < RY; ++r)
-#pragma unroll
-              for (int i = 0; i < VEC; ++i) qb[j][r][i] = qc[j][r][i];
-          }
-          if (pz == p.nz - 1) {
-#pragma unroll
-            for (int r = 0; r < RY; ++r)
-#pragma unroll
-              for (int i = 0; i < VEC; ++i) t[r][i] = qc[j][r][i];
-          }
-          T nrow[VEC], srow[VEC];
-          ld16_shared<T>(nrow, nb + cen0 - W);
-          ld16_shared<T>(srow, nb + cen0 + RY * W);
-          T o[RY][VEC];
-#pragma unroll
-          for (int r = 0; r < RY; ++r) {
-            T nn[VEC], ss[VEC];
-#pragma unroll
-            for (int i = 0; i < VEC; ++i) {
-              nn[i] = (r == 0) ? nrow[i] : qc[j][r - 1][i];
-              ss[i] = (r == RY - 1) ? srow[i] : qc[j][r + 1][i];
-            }
-            if (y + r == 0) {
-#pragma unroll
-              for (int i = 0; i < VEC; ++i) nn[i] = qc[j][r][i];
-            }
-            if (y + r == p.ny - 1) {
-#pragma unroll
-              for (int i = 0; i < VEC; ++i) ss[i] = qc[j][r][i];
-            }
-            T left = shfl_up1(qc[j][r][VEC - 1]);
-            T right = shfl_down1(qc[j][r][0]);
-            if (lane == 0) left = nb[cen0 + r * W - 1];
-            if (lane == 31) right = nb[cen0 + r * W + VEC];
-            diffuse_row<T, VEC, true>(qc[j][r], nn, ss, qb[j][r], t[r], left, right,
-                                      west_face, east_elem, p, o[r]);
-          }
-          if (j < k - 1) {
-            T *dst = bufs + (j * 2 + (pz & 1)) * plane_elems;
-#pragma unroll
-            for (int r = 0; r < RY; ++r)
-              *reinterpret_cast<uint4 *>(dst + cen0 + r * W) =
-                  *reinterpret_cast<const uint4 *>(o[r]);
-          } else if (ok && pz >= zs && pz < ze) {
-#pragma unroll
-            for (int r = 0; r < RY; ++r) {
-              const int er = rows0 + r;  // row within E
-              const int gy = y + r;
-              if (out_lane && er >= k - 1 && er < k - 1 + TYO && gy < p.ny) {
-                T *g = p.out + (int64_t)pz * p.plane + (int64_t)gy * p.row + x;
-                if (vec_in) {
-                  st16_global<T>(g, o[r]);
-                } else {
-#pragma unroll
-                  for (int i = 0; i < VEC; ++i)
-                    if (x + i < p.nx) g[i] = o[r][i];
-                }
-              }
-            }
-          }
-          // Shift this stage's queue; its output is the next stage's newest plane.
-#pragma unroll
-          for (int r = 0; r < RY; ++r)
-#pragma unroll
-            for (int i = 0; i < VEC; ++i) {
-              qb[j][r][i] = qc[j][r][i];
-              qc[j][r][i] = t[r][i];
-              t[r][i] = o[r][i];
-            }
-        }
-      }
-      prev_in = in_t;
-      ok = __syncthreads_and(ok);
-      if (!ok) break;
-      // Input plane q-1 is consumed by every thread: refill its stage.
-      if (tid == 0 && q - 1 + ns < nplanes) issue(q - 1 + ns);
+    // One pipeline step for input plane q, with rotation R of the slots.
+#define PS_T7_STEP(R)                                                         \
+  {                                                                           \
+    const T *in_t = wait_next();                                              \
+    if (edge)                                                                 \
+      t7_step<T, RY, K, R, true>(Q, in_t, prev_in, zin0 + q, p, it, ok);      \
+    else                                                                      \
+      t7_step<T, RY, K, R, false>(Q, in_t, prev_in, zin0 + q, p, it, ok);     \
+    prev_in = in_t;                                                           \
+    ok = __syncthreads_and(ok);                                               \
+    if (!ok) break;                                                           \
+    if (tid == 0 && q - 1 + ns < nplanes) issue(q - 1 + ns);                  \
+    if (++q >= nplanes) break;                                                \
+  }
+    int q = 2;
+    while (q < nplanes) {
+      PS_T7_STEP(0)
+      PS_T7_STEP(1)
+      PS_T7_STEP(2)
     }
+#undef PS_T7_STEP
   }
   if (!ok && tid == 0) {
     for (int s = 0; s < ns; ++s) mbar_wait(&full[s], 0, nullptr, 1024);
   }
 }
 
-template <typename T, int RY, int KMAX>
+template <typename T, int RY, int K>
 cudaError_t launch_k(TParams<T> p, const MarchConfig &cfg, const CUtensorMap *tin,
                      int sm_count, cudaStream_t st) {
   constexpr int VEC = 16 / (int)sizeof(T);
@@ -288,7 +319,7 @@ cudaError_t launch_k(TParams<T> p, const MarchConfig &cfg, const CUtensorMap *ti
   const int tyo = tye - 2 * (p.k - 1);
   if (tyo < 1) return cudaErrorInvalidConfiguration;
   const size_t smem = temporal7_smem_bytes((int)sizeof(T), cfg, p.k);
-  auto kern = t7_kernel<T, RY, KMAX>;
+  auto kern = t7_kernel<T, RY, K>;
   static size_t attr_set = 0;
   if (smem > attr_set) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
