@@ -35,8 +35,8 @@ __device__ __forceinline__ void him_row6(const float *pl, int idx, int lane, flo
   ld16_shared<float>(v, pl + idx);
   float l = shfl_up1(v[3]);
   float rr = shfl_down1(v[0]);
-  if (lane == 0) l = pl[idx - 1];
-  if (lane == 31) rr = pl[idx + 4];
+  ld_shared_if(lane == 0, pl + idx - 1, l);
+  ld_shared_if(lane == 31, pl + idx + 4, rr);
   r[0] = l;
   r[1] = v[0];
   r[2] = v[1];

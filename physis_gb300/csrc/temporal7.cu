@@ -140,8 +140,8 @@ __device__ __forceinline__ void t7_step(T (&Q)[K][3][RY][16 / sizeof(T)], const 
       }
       T left = shfl_up1(Q[j][CS][r][VEC - 1]);
       T right = shfl_down1(Q[j][CS][r][0]);
-      if (lane == 0) left = nb[cen0 + r * W - 1];
-      if (lane == 31) right = nb[cen0 + r * W + VEC];
+      ld_shared_if(lane == 0, nb + cen0 + r * W - 1, left);
+      ld_shared_if(lane == 31, nb + cen0 + r * W + VEC, right);
       if (j < K - 1) {
         diffuse_row<T, VEC, CL>(Q[j][CS][r], nn, ss, Q[j][BS][r], Q[j][TS][r], left, right,
                                 it.west_face, it.east_elem, p, Q[(j + 1) % K][TS][r]);
@@ -175,7 +175,7 @@ __device__ __forceinline__ void t7_step(T (&Q)[K][3][RY][16 / sizeof(T)], const 
 }
 
 template <typename T, int RY, int K>
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(256, 2)
 t7_kernel(const __grid_constant__ CUtensorMap tin, const TParams<T> p) {
   constexpr int VEC = 16 / (int)sizeof(T);
   constexpr int W = 34 * VEC;   // shared row width (E plus a VEC apron each side)
