@@ -148,34 +148,32 @@ __device__ __forceinline__ void st16_global(T *dst, const T (&src)[16 / sizeof(T
 }
 
 // v = *addr if pred, else v unchanged: a predicated shared load with no
-// branch (the edge lanes of a warp fetch their halo cell this way).
+// branch (the edge lanes of a warp fetch their halo cell this way).  The
+// volatile asm stays after the mbarrier wait (also volatile asm) that made
+// the data visible.
 __device__ __forceinline__ void ld_shared_if(bool pred, const float *addr, float &v) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %1, 0;\n\t@p ld.shared.f32 %0, [%2];\n\t}"
       : "+f"(v)
-      : "r"((unsigned)pred), "r"(smem_u32(addr))
-      : "memory");
+      : "r"((unsigned)pred), "r"(smem_u32(addr)));
 }
 __device__ __forceinline__ void ld_shared_if(bool pred, const double *addr, double &v) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %1, 0;\n\t@p ld.shared.f64 %0, [%2];\n\t}"
       : "+d"(v)
-      : "r"((unsigned)pred), "r"(smem_u32(addr))
-      : "memory");
+      : "r"((unsigned)pred), "r"(smem_u32(addr)));
 }
 __device__ __forceinline__ void ld_shared_if(bool pred, const int *addr, int &v) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %1, 0;\n\t@p ld.shared.s32 %0, [%2];\n\t}"
       : "+r"(v)
-      : "r"((unsigned)pred), "r"(smem_u32(addr))
-      : "memory");
+      : "r"((unsigned)pred), "r"(smem_u32(addr)));
 }
 __device__ __forceinline__ void ld_shared_if(bool pred, const long long *addr, long long &v) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %1, 0;\n\t@p ld.shared.s64 %0, [%2];\n\t}"
       : "+l"(v)
-      : "r"((unsigned)pred), "r"(smem_u32(addr))
-      : "memory");
+      : "r"((unsigned)pred), "r"(smem_u32(addr)));
 }
 
 template <typename T>

@@ -147,8 +147,8 @@ __device__ __forceinline__ bool s7_item(const CUtensorMap *tin, const S7Params<T
         }
         T left = shfl_up1(c[r][VEC - 1]);
         T right = shfl_down1(c[r][0]);
-        ld_shared_if(lane == 0, cur + cen0 + r * W - 1, left);
-        ld_shared_if(lane == 31, cur + cen0 + r * W + VEC, right);
+        if (lane == 0) left = cur[cen0 + r * W - 1];
+        if (lane == 31) right = cur[cen0 + r * W + VEC];
 #pragma unroll
         for (int i = 0; i < VEC; ++i) {
           T w = (i == 0) ? left : c[r][i - 1];
