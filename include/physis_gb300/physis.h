@@ -107,6 +107,11 @@ typedef int PSStencil;
  * PS_KERNEL_SUM7        (in, out): out = c + e + w + s + n + b + t, no clamp
  *     (tests/system_tests/test_cases/test_7-pt.c:12-20); the domain must
  *     stay one cell inside the grid.  All four element types.
+ *
+ * Further kernel ids come from PSPointStencilNew (physis_gb300.h): weighted
+ * sums over a list of neighbour offsets with a boundary rule, taking
+ * (in, out) and no scalars -- the 27-point, 9-point 2D, 3-point 1D,
+ * periodic, asymmetric and red/black stencils of the reference's tests.
  */
 enum PSBuiltinKernel {
   PS_KERNEL_COPY = 1,
@@ -163,6 +168,22 @@ PSDomain3D PSDomain3DNew(PSIndex minx, PSIndex maxx, PSIndex miny,
  * k is a PS_KERNEL_* id; the domain is passed by value. */
 PSStencil __PSStencilMap(void *kernel, ...);
 #define PSStencilMap(k, ...) __PSStencilMap((void *)(intptr_t)(k), __VA_ARGS__)
+
+/* include/physis/physis_user.h:100-105: red/black maps.  The kernel updates
+ * its one grid in place, first the "red" cells (x + y + z even), then the
+ * "black" ones (odd) for PSStencilMapRedBlack; PSStencilMapRed / Black run
+ * one colour (translator/reference_runtime_builder.cc:585-600, 634-646,
+ * 875-890).  k is a point stencil id (PSPointStencilNew), PS_KERNEL_SUM7 or
+ * PS_KERNEL_DIFFUSION7; the arguments after the domain are the grid and
+ * then the kernel's scalars.  Every non-centre point of the stencil must lie
+ * at an odd distance (|dx|+|dy|+|dz|), so that a colour reads only cells of
+ * the other colour and the parallel sweep equals the sequential one. */
+PSStencil __PSStencilMapRedBlack(void *kernel, ...);
+PSStencil __PSStencilMapRed(void *kernel, ...);
+PSStencil __PSStencilMapBlack(void *kernel, ...);
+#define PSStencilMapRedBlack(k, ...) __PSStencilMapRedBlack((void *)(intptr_t)(k), __VA_ARGS__)
+#define PSStencilMapRed(k, ...) __PSStencilMapRed((void *)(intptr_t)(k), __VA_ARGS__)
+#define PSStencilMapBlack(k, ...) __PSStencilMapBlack((void *)(intptr_t)(k), __VA_ARGS__)
 
 /* include/physis/physis_user.h:106: PSStencilRun(s0, s1, ..., [iter]).
  * The macro appends PS_RUN_END so the runtime can find the end of the list;

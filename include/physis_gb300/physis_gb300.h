@@ -8,8 +8,11 @@
  *    runtime_common_cuda.h:16-27).
  * 3. Device-resident access, timing on the runtime's stream and launch
  *    counting, used by benchmarks.
- * 4. Launch-shape control and the autotuner.
- * 5. Test hooks that exercise failure handling without faulting a GPU.
+ * 4. Launch-shape control and the autotuner; batches of independent runs.
+ * 5. A reduction for callers that cannot allocate.
+ * 6. Test hooks that exercise failure handling without faulting a GPU.
+ * 7. Point-list stencils (the translator-free form of the reference's
+ *    neighbour-sum stencil functions) and the non-variadic red/black map.
  */
 #ifndef PHYSIS_GB300_EXT_H_
 #define PHYSIS_GB300_EXT_H_
@@ -216,6 +219,45 @@ void PSTestFailNextAllocs(int n);
  * bounded wait of `limit` tries; afterwards PSSynchronize reports
  * PS_ERR_DEVICE_TIMEOUT and the context stays usable. */
 void PSTestDeviceWaitTimeout(unsigned limit);
+
+/* ---- 7. Point-list stencils --------------------------------------------- */
+
+/* Boundary rules of a point stencil: none (the domain keeps every read inside
+ * the grid), periodic ((i + n) % n per axis, include/physis/physis_ref.h:
+ * 62-74, physis_cuda.h:247-269), clamp (the index is clamped to the grid; for
+ * unit offsets this is the `if (x == 0) w = c;` face rule of
+ * examples/diffusion-benchmark/diffusion3d_physis.c:40-54). */
+enum PSBoundary { PS_BOUNDARY_NONE = 0, PS_BOUNDARY_PERIODIC = 1, PS_BOUNDARY_CLAMP = 2 };
+#define PS_MAX_POINTS 64
+#define PS_MAX_POINT_RADIUS 4
+
+/* Registers the stencil
+ *   out(x,y,z) = w[0]*in(x+o[0],y+o[1],z+o[2]) + w[1]*in(x+o[3],...) + ...
+ * summed left to right in the given order, with `boundary` applied to each
+ * read; weights == NULL means every term is the point value itself (the
+ * plain neighbour sums of the reference's stencil functions, e.g.
+ * tests/system_tests/test_cases/test_27-pt.c).  offsets holds 3*npoints
+ * ints, each |offset| <= PS_MAX_POINT_RADIUS; 1 <= npoints <= PS_MAX_POINTS.
+ * Returns a kernel id for PSStencilMap (grids: in, out; no scalars) and the
+ * red/black maps (one grid, in place), or -1 with the error recorded.
+ * Integer grids need integral weights and wrap on overflow.  Registering the
+ * same stencil twice returns the same id.  No counterpart in the reference,
+ * whose translator compiles the stencil function instead
+ * (translator/reference_runtime_builder.cc:391-664). */
+int PSPointStencilNew(int boundary, int npoints, const int *offsets, const double *weights);
+
+/* Map colours: every cell, red (x + y + z even), black (odd), red then black. */
+enum PSMapColor {
+  PS_COLOR_ALL = -1,
+  PS_COLOR_RED = 0,
+  PS_COLOR_BLACK = 1,
+  PS_COLOR_REDBLACK = 2
+};
+
+/* __PSStencilMap / __PSStencilMapRed / Black / RedBlack(kernel, *dom,
+ * grids..., scalars...) by colour (PS_COLOR_ALL is PSStencilMapV). */
+PSStencil PSStencilMapColorV(int kernel, int color, const PSDomain3D *dom, int ngrids,
+                             void *const *grids, int nscalars, const double *scalars);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop

@@ -166,6 +166,118 @@ int pso_run7(int variant, int type, void *g1, void *g2, int nx, int ny, int nz,
 }
 
 /* ------------------------------------------------------------------------ */
+/* Point-list stencils and red/black sweeps                                  */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * out(x,y,z) = w0*in(p0) + w1*in(p1) + ... evaluated left to right, where
+ * p_i = (x+dx_i, y+dy_i, z+dz_i) is mapped per axis by the boundary mode:
+ *   0 none      every read is inside the grid (the caller's domain ensures it;
+ *               e.g. test_27-pt.manual.ref.c, test_asymmetric.manual.ref.c);
+ *   1 periodic  (i + n) % n (include/physis/physis_ref.h:62-74; the
+ *               ((x - 1) + N) % N of test_27-pt-periodic.manual.ref.c);
+ *   2 clamp     index clamped to [0, n-1] (for unit offsets this is the
+ *               `if (x == 0) w = c; else w = g(x-1)` of
+ *               test_7-pt-neumann-cond and test_16.manual.ref.c).
+ * weights == NULL: every term is the point value itself (the plain sums of
+ * the system tests; no multiply).  Integer grids wrap modulo 2^32 / 2^64.
+ *
+ * color -1: every cell of dom, out != in.  color 0 (red) / 1 (black): the
+ * cells of dom with x starting at min + ((min & 1) ^ ((y + z + color) % 2)),
+ * step 2 (translator/reference_runtime_builder.cc:585-600, 634-646), updated
+ * in place (out may equal in) in z -> y -> x order, sequentially.
+ * Returns 0, or -1 for an out-of-grid read in mode 0 or bad arguments.
+ */
+static inline int pso_map_axis(int i, int n, int boundary) {
+  if (boundary == 1) return (i + n) % n;
+  if (boundary == 2) return i < 0 ? 0 : (i >= n ? n - 1 : i);
+  return i;
+}
+
+#define DEFINE_POINTS(NAME, T, U)                                              \
+  static int NAME(int boundary, int npoints, const int *offs,                  \
+                  const double *weights, const T *in, T *out, int nx, int ny,  \
+                  int nz, const int *dom, int color, int nthreads) {           \
+    T w[64];                                                                   \
+    int i, z, bad = 0;                                                         \
+    for (i = 0; i < npoints; ++i) w[i] = weights ? (T)weights[i] : (T)1;       \
+    if (color < 0) {                                                           \
+      _Pragma("omp parallel for num_threads(nthreads) schedule(static) reduction(|:bad)") \
+      for (z = dom[4]; z < dom[5]; ++z) {                                      \
+        int y, x, k;                                                           \
+        for (y = dom[2]; y < dom[3]; ++y)                                      \
+          for (x = dom[0]; x < dom[1]; ++x) {                                  \
+            U v = 0;                                                           \
+            for (k = 0; k < npoints; ++k) {                                    \
+              int xx = pso_map_axis(x + offs[3 * k], nx, boundary);            \
+              int yy = pso_map_axis(y + offs[3 * k + 1], ny, boundary);        \
+              int zz = pso_map_axis(z + offs[3 * k + 2], nz, boundary);        \
+              if (xx < 0 || xx >= nx || yy < 0 || yy >= ny || zz < 0 || zz >= nz) { \
+                bad = 1;                                                       \
+                continue;                                                      \
+              }                                                                \
+              U t = weights ? (U)((U)w[k] * (U)in[IDX(xx, yy, zz)])            \
+                            : (U)in[IDX(xx, yy, zz)];                          \
+              v = (k == 0) ? t : (U)(v + t);                                   \
+            }                                                                  \
+            out[IDX(x, y, z)] = (T)v;                                          \
+          }                                                                    \
+      }                                                                        \
+      return bad ? -1 : 0;                                                     \
+    }                                                                          \
+    for (z = dom[4]; z < dom[5]; ++z) {                                        \
+      int y, x, k;                                                             \
+      for (y = dom[2]; y < dom[3]; ++y) {                                      \
+        const int x0 = dom[0] + ((dom[0] & 1) ^ ((y + z + color) % 2));        \
+        for (x = x0; x < dom[1]; x += 2) {                                     \
+          U v = 0;                                                             \
+          for (k = 0; k < npoints; ++k) {                                      \
+            int xx = pso_map_axis(x + offs[3 * k], nx, boundary);              \
+            int yy = pso_map_axis(y + offs[3 * k + 1], ny, boundary);          \
+            int zz = pso_map_axis(z + offs[3 * k + 2], nz, boundary);          \
+            if (xx < 0 || xx >= nx || yy < 0 || yy >= ny || zz < 0 || zz >= nz) \
+              return -1;                                                       \
+            U t = weights ? (U)((U)w[k] * (U)in[IDX(xx, yy, zz)])              \
+                          : (U)in[IDX(xx, yy, zz)];                            \
+            v = (k == 0) ? t : (U)(v + t);                                     \
+          }                                                                    \
+          out[IDX(x, y, z)] = (T)v;                                            \
+        }                                                                      \
+      }                                                                        \
+    }                                                                          \
+    return 0;                                                                  \
+  }
+
+DEFINE_POINTS(points_f32, float, float)
+DEFINE_POINTS(points_f64, double, double)
+DEFINE_POINTS(points_i32, int32_t, uint32_t)
+DEFINE_POINTS(points_i64, int64_t, uint64_t)
+
+int pso_points(int type, int boundary, int npoints, const int *offs,
+               const double *weights, const void *in, void *out, int nx, int ny,
+               int nz, const int *dom, int color, int nthreads) {
+  if (npoints < 1 || npoints > 64 || boundary < 0 || boundary > 2 || color < -1 ||
+      color > 1)
+    return -1;
+  nthreads = pick_threads(nthreads);
+  switch (type) {
+    case PSO_FLOAT:
+      return points_f32(boundary, npoints, offs, weights, (const float *)in, (float *)out,
+                        nx, ny, nz, dom, color, nthreads);
+    case PSO_DOUBLE:
+      return points_f64(boundary, npoints, offs, weights, (const double *)in,
+                        (double *)out, nx, ny, nz, dom, color, nthreads);
+    case PSO_INT:
+      return points_i32(boundary, npoints, offs, weights, (const int32_t *)in,
+                        (int32_t *)out, nx, ny, nz, dom, color, nthreads);
+    case PSO_LONG:
+      return points_i64(boundary, npoints, offs, weights, (const int64_t *)in,
+                        (int64_t *)out, nx, ny, nz, dom, color, nthreads);
+  }
+  return -1;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Himeno 19-point Jacobi sweep                                              */
 /* ------------------------------------------------------------------------ */
 

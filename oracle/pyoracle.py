@@ -48,6 +48,7 @@ def lib():
         L.pso_run7.argtypes = [i, i, vp, vp, i, i, i, ip, dp, i, i, i]
         L.pso_himeno19.argtypes = [i, ctypes.POINTER(vp), i, i, i, ip, d, i,
                                    ctypes.POINTER(ctypes.c_float), dp]
+        L.pso_points.argtypes = [i, i, i, ip, dp, vp, vp, i, i, i, ip, i, i]
         L.pso_reduce_ref.argtypes = [i, i, vp, i64, vp]
         L.pso_reduce_fp64.argtypes = [i, i, vp, i64, dp]
         L.pso_fill_uniform_f32.argtypes = [vp, i64, ctypes.c_uint64, i]
@@ -93,6 +94,28 @@ def run7(variant, g1, g2, dom, coef=(), iter=1, pingpong=True, nthreads=1):
                         1 if pingpong else 0, nthreads)
     if rc:
         raise ValueError("unsupported variant/type for the oracle")
+
+
+def points(g_in, g_out, dom, offsets, weights=None, boundary=0, color=-1,
+           nthreads=1):
+    """REF sweep of a point-list stencil: g_out = sum_i w_i * g_in(p + d_i).
+
+    offsets: sequence of (dx, dy, dz); weights None = plain sum.  boundary:
+    0 none, 1 periodic, 2 clamp.  color -1 = every cell (g_out != g_in);
+    0 red / 1 black = in-place REF red/black order (pass the same array
+    twice).  Arrays are shaped (nz, ny, nx).
+    """
+    nz, ny, nx = g_in.shape
+    assert g_in.dtype == g_out.dtype and g_in.shape == g_out.shape
+    n = len(offsets)
+    offs = (ctypes.c_int * (3 * n))(*[int(v) for o in offsets for v in o])
+    w = None if weights is None else (ctypes.c_double * n)(
+        *[float(v) for v in weights])
+    rc = lib().pso_points(TYPE_OF_NP[g_in.dtype], boundary, n, offs, w,
+                          _ptr(g_in), _ptr(g_out), nx, ny, nz, _dom(dom),
+                          color, nthreads)
+    if rc:
+        raise ValueError("point stencil reads outside the grid, or bad args")
 
 
 def himeno19(grids, dom, omega, nthreads=1):

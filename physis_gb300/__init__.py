@@ -23,6 +23,9 @@ PS_KERNEL_HIMENO19 = 3
 PS_KERNEL_HIMENO19_GOSA = 4
 PS_KERNEL_SUM7 = 5
 PS_RUN_END = -(2 ** 31)
+# enums of include/physis_gb300/physis_gb300.h (point stencils, map colours)
+BOUNDARY_NONE, BOUNDARY_PERIODIC, BOUNDARY_CLAMP = 0, 1, 2
+COLOR_ALL, COLOR_RED, COLOR_BLACK, COLOR_REDBLACK = -1, 0, 1, 2
 
 PS_OK = 0
 ERROR_NAMES = {
@@ -52,7 +55,8 @@ PSEventRecord PSEventElapsedMs PSGetLaunchCount PSGetSMCount PSSetLaunchShape
 PSGetLaunchShape PSTestFailNextAllocs PSTestDeviceWaitTimeout PSReduceNoAlloc
 PSSetTemporalBlocking PSGetTemporalBlocking PSSetAutotune PSSetTuneCachePath
 PSLoadTuneCache PSClearTuning PSGetStencilPlan PSBatchCreate PSBatchRun PSBatchFree
-PSSetBatchShape""".split()
+PSSetBatchShape __PSStencilMapRedBlack __PSStencilMapRed __PSStencilMapBlack
+PSStencilMapColorV PSPointStencilNew""".split()
 
 
 class PSDomain(ctypes.Structure):
@@ -154,6 +158,11 @@ def lib():
     L.PSSetBatchShape.argtypes = [i, i, i, i, i]
     L.PSReduceNoAlloc.argtypes = [vp, ctypes.c_size_t, i, i, i, i, i, vp, vp]
     L.PSReduceNoAlloc.restype = i
+    L.PSPointStencilNew.argtypes = [i, i, ctypes.POINTER(i), ctypes.POINTER(d)]
+    L.PSPointStencilNew.restype = i
+    L.PSStencilMapColorV.argtypes = [i, i, ctypes.POINTER(PSDomain), i,
+                                     ctypes.POINTER(vp), i, ctypes.POINTER(d)]
+    L.PSStencilMapColorV.restype = i
     _lib = L
     return L
 
@@ -247,6 +256,32 @@ def stencil_map(kernel, dom, grids, scalars=()):
     sarr = (ctypes.c_double * max(len(scalars), 1))(*[float(s) for s in scalars])
     s = lib().PSStencilMapV(kernel, ctypes.byref(dom), n, garr, len(scalars),
                             sarr)
+    check()
+    return s
+
+
+def point_stencil(points, weights=None, boundary=BOUNDARY_NONE):
+    """Registers a point-list stencil; returns its kernel id.
+
+    points: sequence of (dx, dy, dz) in summation order; weights: None for a
+    plain sum, else one weight per point.
+    """
+    n = len(points)
+    offs = (ctypes.c_int * (3 * n))(*[int(v) for p in points for v in p])
+    w = None if weights is None else (ctypes.c_double * n)(
+        *[float(v) for v in weights])
+    k = lib().PSPointStencilNew(boundary, n, offs, w)
+    check()
+    return k
+
+
+def stencil_map_color(kernel, color, dom, grids, scalars=()):
+    """A red (0) / black (1) / red-then-black (2) map, or -1 = PSStencilMapV."""
+    n = len(grids)
+    garr = (ctypes.c_void_p * max(n, 1))(*[g.handle for g in grids])
+    sarr = (ctypes.c_double * max(len(scalars), 1))(*[float(s) for s in scalars])
+    s = lib().PSStencilMapColorV(kernel, color, ctypes.byref(dom), n, garr,
+                                 len(scalars), sarr)
     check()
     return s
 

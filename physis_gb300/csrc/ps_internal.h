@@ -113,6 +113,25 @@ cudaError_t launch_himeno19(const Himeno19Args &a, const MarchConfig &cfg,
                             const ResidualSink &sink, int *dev_err, int sm_count,
                             cudaStream_t s);
 
+// ---- Point-list stencils and red/black sweeps (points.cu) -----------------
+constexpr int kMaxPoints = 64;      // points per stencil
+constexpr int kMaxPointRadius = 4;  // |offset| per axis
+enum Boundary { kBoundaryNone = 0, kBoundaryPeriodic = 1, kBoundaryClamp = 2 };
+struct PointsArgs {
+  GridView in, out;  // same type and size; out == in for red/black
+  Box dom;
+  int boundary;
+  int color;         // -1 every cell, 0 red, 1 black
+  int n;
+  int d[kMaxPoints][3];
+  double w[kMaxPoints];
+  bool unit;         // every weight is 1: terms are the point values
+};
+// cfg.warps x cfg.rows (1 or 2) rows per tile; the other fields are unused.
+size_t points_smem_bytes(const PointsArgs &a, const MarchConfig &cfg);
+cudaError_t launch_points(const PointsArgs &a, const MarchConfig &cfg, int sm_count,
+                          cudaStream_t s);
+
 // ---- Reductions (reduce.cu) ----------------------------------------------
 // Reduces every element of g with op.  The 8-byte result is written to
 // *result: FP64 for float and double grids, int64 for int (wrapped to 32

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <cstdarg>
 #include <cstdio>
@@ -45,6 +46,9 @@ constexpr int kMaxMaps = 1 << 24;
 constexpr int kNumEvents = 64;
 constexpr int kMaxPartials = 1 << 16;
 constexpr int kNumKernels = 8;
+constexpr int kSlotPoints = 7;     // launch-shape slot shared by all point stencils
+constexpr int kPointsBase = 1024;  // kernel id of the first registered point stencil
+constexpr int kMaxPointStencils = 1 << 16;
 
 // Tensor maps are cached per (device view, box); an entry is dropped when
 // its grid is freed.
@@ -70,10 +74,19 @@ struct Plan {
   MarchConfig tshape;
 };
 
+// A registered point-list stencil (PSPointStencilNew).
+struct PointStencil {
+  int boundary = 0, n = 0;
+  int d[psg::kMaxPoints][3];
+  double w[psg::kMaxPoints];
+  bool unit = true;
+};
+
 struct Map {
   int kernel;
+  int color = -1;  // -1 every cell; 0 red, 1 black, 2 red then black (in place)
   __PSDomain dom;
-  std::vector<Grid *> grids;
+  std::vector<Grid *> grids;  // red/black maps hold their one grid twice
   std::vector<double> scalars;
   bool has_plan = false;  // set by the autotuner (or its cache)
   Plan plan;
@@ -100,6 +113,7 @@ struct Runtime {
   bool autotune = false;
   std::string tune_path;  // JSON-lines cache file ("" = in memory only)
   std::string gpu_name;
+  std::vector<PointStencil> points;  // kernel id kPointsBase + index
 };
 
 Runtime *rt = nullptr;
@@ -267,6 +281,11 @@ struct KernelSig {
   const char *name;
 };
 
+const PointStencil *point_stencil(int k) {
+  if (!rt || k < kPointsBase || k - kPointsBase >= (int)rt->points.size()) return nullptr;
+  return &rt->points[k - kPointsBase];
+}
+
 bool kernel_sig(int k, KernelSig *s) {
   switch (k) {
     case PS_KERNEL_COPY: *s = {2, 0, "PS_KERNEL_COPY"}; return true;
@@ -275,7 +294,111 @@ bool kernel_sig(int k, KernelSig *s) {
     case PS_KERNEL_HIMENO19_GOSA: *s = {14, 1, "PS_KERNEL_HIMENO19_GOSA"}; return true;
     case PS_KERNEL_SUM7: *s = {2, 0, "PS_KERNEL_SUM7"}; return true;
   }
+  if (point_stencil(k)) {
+    *s = {2, 0, "point stencil"};
+    return true;
+  }
   return false;
+}
+
+// Registers ps (or finds an identical registration); returns its kernel id
+// or -1.
+int register_points(const PointStencil &ps) {
+  for (size_t i = 0; i < rt->points.size(); ++i) {
+    const PointStencil &q = rt->points[i];
+    if (q.boundary != ps.boundary || q.n != ps.n || q.unit != ps.unit) continue;
+    bool same = true;
+    for (int j = 0; j < ps.n && same; ++j)
+      same = q.d[j][0] == ps.d[j][0] && q.d[j][1] == ps.d[j][1] && q.d[j][2] == ps.d[j][2] &&
+             (ps.unit || q.w[j] == ps.w[j]);
+    if (same) return kPointsBase + (int)i;
+  }
+  if ((int)rt->points.size() >= kMaxPointStencils) {
+    fail(PS_ERR_OUT_OF_MEMORY, "more than %d point stencils", kMaxPointStencils);
+    return -1;
+  }
+  rt->points.push_back(ps);
+  return kPointsBase + (int)rt->points.size() - 1;
+}
+
+// The point-stencil equivalents of the 7-point builtins, for their red/black
+// maps.  SUM7: c + e + w + s + n + b + t unclamped (test_7-pt.c:12-20, the
+// same order as test_redblack.c).  DIFFUSION7: cc*c + cw*w + ce*e + cs*s +
+// cn*n + cb*b + ct*t clamped; scalars in map order ce cw cn cs ct cb cc.
+int builtin_as_points(int kernel, const std::vector<double> &sc) {
+  PointStencil ps;
+  ps.n = 7;
+  if (kernel == PS_KERNEL_SUM7) {
+    const int d[7][3] = {{0, 0, 0}, {1, 0, 0}, {-1, 0, 0}, {0, 1, 0},
+                         {0, -1, 0}, {0, 0, -1}, {0, 0, 1}};
+    memcpy(ps.d, d, sizeof(d));
+    ps.boundary = psg::kBoundaryNone;
+    ps.unit = true;
+    for (int i = 0; i < 7; ++i) ps.w[i] = 1.0;
+  } else {
+    const int d[7][3] = {{0, 0, 0}, {-1, 0, 0}, {1, 0, 0}, {0, 1, 0},
+                         {0, -1, 0}, {0, 0, -1}, {0, 0, 1}};
+    memcpy(ps.d, d, sizeof(d));
+    ps.boundary = psg::kBoundaryClamp;
+    ps.unit = false;
+    const double w[7] = {sc[6], sc[1], sc[0], sc[3], sc[2], sc[5], sc[4]};
+    memcpy(ps.w, w, sizeof(w));
+  }
+  return register_points(ps);
+}
+
+// Checks a point-stencil map: element type and weights, that every read of
+// boundary "none" stays inside the grid, and the red/black conditions.
+bool validate_points(const Map &m, const PointStencil &ps) {
+  const Grid *g = m.grids[0];
+  if ((g->type == PS_INT || g->type == PS_LONG) && !ps.unit) {
+    const double lim = g->type == PS_INT ? 2147483648.0 : 9223372036854775808.0;
+    for (int i = 0; i < ps.n; ++i)
+      if (ps.w[i] != std::trunc(ps.w[i]) || ps.w[i] < -lim || ps.w[i] >= lim)
+        return fail(PS_ERR_INVALID_ARGUMENT,
+                    "point stencil: weight %g of point %d is not a value of the grid's "
+                    "integer type", ps.w[i], i);
+  }
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  for (int i = 0; i < ps.n; ++i)
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = std::min(lo[d], ps.d[i][d]);
+      hi[d] = std::max(hi[d], ps.d[i][d]);
+    }
+  bool empty = false;
+  for (int d = 0; d < 3; ++d) empty = empty || m.dom.min[d] >= m.dom.max[d];
+  for (int d = 0; d < 3 && !empty; ++d) {
+    const int n = g->dim[d];
+    if (ps.boundary == psg::kBoundaryNone &&
+        (m.dom.min[d] + lo[d] < 0 || m.dom.max[d] - 1 + hi[d] > n - 1))
+      return fail(PS_ERR_INVALID_ARGUMENT,
+                  "point stencil reads outside the grid: domain [%d,%d) with offsets "
+                  "[%d,%d] in dim %d of size %d (boundary none)", m.dom.min[d],
+                  m.dom.max[d], lo[d], hi[d], d, n);
+    if (ps.boundary == psg::kBoundaryPeriodic && (-lo[d] > n || hi[d] > n))
+      return fail(PS_ERR_INVALID_ARGUMENT,
+                  "periodic point stencil: offsets [%d,%d] exceed the size %d of dim %d",
+                  lo[d], hi[d], n, d);
+  }
+  if (m.color < 0) return true;
+  for (int i = 0; i < ps.n; ++i) {
+    const int ax = std::abs(ps.d[i][0]), ay = std::abs(ps.d[i][1]), az = std::abs(ps.d[i][2]);
+    const int dist = ax + ay + az;
+    if (dist != 0 && dist % 2 == 0)
+      return fail(PS_ERR_UNSUPPORTED,
+                  "red/black map: point %d (%d,%d,%d) has the colour of the cell it "
+                  "updates", i, ps.d[i][0], ps.d[i][1], ps.d[i][2]);
+    if (ps.boundary == psg::kBoundaryClamp && dist > 1)
+      return fail(PS_ERR_UNSUPPORTED,
+                  "red/black map with clamped faces needs unit axis offsets (point %d)", i);
+  }
+  if (ps.boundary == psg::kBoundaryPeriodic)
+    for (int d = 0; d < 3; ++d)
+      if ((lo[d] != 0 || hi[d] != 0) && g->dim[d] % 2 != 0)
+        return fail(PS_ERR_UNSUPPORTED,
+                    "periodic red/black map needs an even grid size in dim %d (got %d)", d,
+                    g->dim[d]);
+  return true;
 }
 
 // Validates a map's grids, scalars and domain against its builtin.
@@ -290,9 +413,19 @@ bool validate_map(const Map &m) {
       return fail(PS_ERR_INVALID_ARGUMENT,
                   "%s: all grids of a map must have the same type and size", sig.name);
   }
-  if (m.grids[0] == m.grids[1])
+  if (m.color < 0 && m.grids[0] == m.grids[1])
     return fail(PS_ERR_INVALID_ARGUMENT, "%s: input and output grid are the same",
                 sig.name);
+  if (m.color >= 0 && m.grids[0] != m.grids[1])
+    return fail(PS_ERR_INVALID_ARGUMENT, "%s: a red/black map updates one grid", sig.name);
+  if (const PointStencil *ps = point_stencil(m.kernel)) {
+    for (int d = 0; d < 3; ++d)
+      if (m.dom.min[d] < 0 || m.dom.max[d] > g0->dim[d] || m.dom.min[d] > m.dom.max[d])
+        return fail(PS_ERR_INVALID_ARGUMENT,
+                    "%s: domain [%d,%d) in dim %d outside grid of size %d", sig.name,
+                    m.dom.min[d], m.dom.max[d], d, g0->dim[d]);
+    return validate_points(m, *ps);
+  }
   const bool is_float = g0->type == PS_FLOAT, is_fp = is_float || g0->type == PS_DOUBLE;
   if ((m.kernel == PS_KERNEL_DIFFUSION7 && !is_fp) ||
       ((m.kernel == PS_KERNEL_HIMENO19 || m.kernel == PS_KERNEL_HIMENO19_GOSA) && !is_float))
@@ -313,7 +446,44 @@ bool validate_map(const Map &m) {
   return true;
 }
 
-int shape_slot(int kernel) { return (kernel > 0 && kernel < kNumKernels) ? kernel : 0; }
+int shape_slot(int kernel) {
+  if (kernel >= kPointsBase) return kSlotPoints;
+  return (kernel > 0 && kernel < kNumKernels) ? kernel : 0;
+}
+
+// One point-stencil map: one launch per colour it runs.
+bool launch_points_map(const Map &m, const PointStencil &ps) {
+  psg::PointsArgs a;
+  a.in = view(m.grids[0]);
+  a.out = view(m.grids[1]);
+  for (int d = 0; d < 3; ++d) {
+    a.dom.min[d] = m.dom.min[d];
+    a.dom.max[d] = m.dom.max[d];
+  }
+  if (a.dom.min[0] >= a.dom.max[0] || a.dom.min[1] >= a.dom.max[1] ||
+      a.dom.min[2] >= a.dom.max[2])
+    return true;
+  a.boundary = ps.boundary;
+  a.n = ps.n;
+  memcpy(a.d, ps.d, sizeof(a.d));
+  memcpy(a.w, ps.w, sizeof(a.w));
+  a.unit = ps.unit;
+  MarchConfig cfg = m.has_plan ? m.plan.shape : rt->shapes[kSlotPoints];
+  // the widest stencils need a shorter tile to fit their plane ring
+  while (psg::points_smem_bytes(a, cfg) > 220 * 1024 && (cfg.rows > 1 || cfg.warps > 1)) {
+    if (cfg.rows > 1) cfg.rows = 1;
+    else cfg.warps /= 2;
+  }
+  const int colors[2] = {m.color == 2 ? 0 : m.color, 1};
+  const int ncol = m.color == 2 ? 2 : 1;
+  for (int c = 0; c < ncol; ++c) {
+    a.color = colors[c];
+    cudaError_t e = psg::launch_points(a, cfg, rt->sm_count, rt->stream);
+    if (!cuda_ok(e, "point stencil launch")) return false;
+    ++rt->launches;
+  }
+  return true;
+}
 
 // One plain sweep of a 7-point-family map with explicit input/output views.
 bool launch_s7(const Map &m, const GridView &in, const GridView &out) {
@@ -340,6 +510,7 @@ bool launch_s7(const Map &m, const GridView &in, const GridView &out) {
 }
 
 bool launch_map(const Map &m, bool want_gosa) {
+  if (const PointStencil *ps = point_stencil(m.kernel)) return launch_points_map(m, *ps);
   const Grid *g0 = m.grids[0];
   psg::Box box;
   for (int d = 0; d < 3; ++d) {
@@ -531,15 +702,31 @@ Map *lookup_map(PSStencil s) {
   return &rt->maps[idx];
 }
 
+// Kernels a red/black map accepts: point stencils and the 7-point builtins
+// (run as their point-stencil equivalents).
+bool colorable(int kernel) {
+  return point_stencil(kernel) || kernel == PS_KERNEL_SUM7 || kernel == PS_KERNEL_DIFFUSION7;
+}
+
+// Grids a map of `kernel` with `color` takes: a red/black map updates its one
+// grid in place.
+int map_ngrids(const KernelSig &sig, int color) { return color >= 0 ? 1 : sig.ngrids; }
+
 bool map_from(int kernel, const __PSDomain &dom, int ngrids, void *const *grids,
-              int nscalars, const double *scalars, Map *out) {
+              int nscalars, const double *scalars, Map *out, int color = -1) {
   KernelSig sig;
   if (!kernel_sig(kernel, &sig))
     return fail(PS_ERR_UNKNOWN_KERNEL, "unknown builtin stencil id %d", kernel);
-  if (ngrids != sig.ngrids || nscalars != sig.nscalars)
+  if (color < -1 || color > 2)
+    return fail(PS_ERR_INVALID_ARGUMENT, "unknown map colour %d", color);
+  if (color >= 0 && !colorable(kernel))
+    return fail(PS_ERR_UNSUPPORTED, "%s has no red/black form", sig.name);
+  const int want = map_ngrids(sig, color);
+  if (ngrids != want || nscalars != sig.nscalars)
     return fail(PS_ERR_INVALID_ARGUMENT, "%s takes %d grids and %d scalars, got %d and %d",
-                sig.name, sig.ngrids, sig.nscalars, ngrids, nscalars);
+                sig.name, want, sig.nscalars, ngrids, nscalars);
   out->kernel = kernel;
+  out->color = color;
   out->dom = dom;
   out->grids.clear();
   for (int i = 0; i < ngrids; ++i) {
@@ -547,7 +734,14 @@ bool map_from(int kernel, const __PSDomain &dom, int ngrids, void *const *grids,
     if (!g) return false;
     out->grids.push_back(g);
   }
+  if (color >= 0) out->grids.push_back(out->grids[0]);
   out->scalars.assign(scalars, scalars + nscalars);
+  if (color >= 0 && !point_stencil(kernel)) {
+    const int id = builtin_as_points(kernel, out->scalars);
+    if (id < 0) return false;
+    out->kernel = id;
+    out->scalars.clear();
+  }
   return true;
 }
 
@@ -579,6 +773,22 @@ std::string run_key(const std::vector<Map *> &ms) {
              g->dim[0], g->dim[1], g->dim[2], m->dom.min[0], m->dom.max[0], m->dom.min[1],
              m->dom.max[1], m->dom.min[2], m->dom.max[2]);
     k += buf;
+    if (const PointStencil *ps = point_stencil(m->kernel)) {
+      // kernel ids are per process: name the stencil by its contents
+      uint64_t h = 1469598103934665603ull;  // FNV-1a over boundary, colour, points
+      auto mix = [&h](int v) {
+        for (int b = 0; b < 4; ++b) {
+          h ^= (uint64_t)((v >> (8 * b)) & 0xff);
+          h *= 1099511628211ull;
+        }
+      };
+      mix(ps->boundary);
+      mix(m->color);
+      mix(ps->unit ? 1 : 0);
+      for (int i = 0; i < ps->n; ++i) mix(ps->d[i][0] * 81 + ps->d[i][1] * 9 + ps->d[i][2]);
+      snprintf(buf, sizeof(buf), "pts%d:%016llx;", ps->n, (unsigned long long)h);
+      k += buf;
+    }
   }
   if (ms.size() == 2 && pair_eligible(*ms[0], *ms[1])) k += "pair;";
   snprintf(buf, sizeof(buf), "%s/%dsm", rt->gpu_name.c_str(), rt->sm_count);
@@ -590,6 +800,13 @@ std::vector<Plan> candidates(const std::vector<Map *> &ms) {
   const Map &m0 = *ms[0];
   const bool him = m0.kernel == PS_KERNEL_HIMENO19 || m0.kernel == PS_KERNEL_HIMENO19_GOSA;
   const MarchConfig tdef = rt->tshapes[shape_slot(m0.kernel)];
+  bool all_points = true;
+  for (const Map *m : ms) all_points = all_points && point_stencil(m->kernel);
+  if (all_points) {  // {warps, rows} of the point-stencil tile
+    const int sh[][2] = {{8, 2}, {8, 1}, {4, 2}, {4, 1}, {16, 1}, {2, 2}};
+    for (auto &c : sh) out.push_back(Plan{MarchConfig{c[0], c[1], 4, 0, 0}, 1, tdef});
+    return out;
+  }
   if (him) {
     const int sh[][3] = {{4, 5, 2}, {2, 5, 2}, {8, 4, 2}, {4, 4, 3}, {4, 6, 2}, {2, 6, 3},
                          {8, 3, 2}, {4, 3, 1}};
@@ -1428,6 +1645,97 @@ PSStencil PSStencilMapV(int kernel, const PSDomain3D *dom, int ngrids, void *con
   Map m;
   if (!map_from(kernel, *dom, ngrids, grids, nscalars, scalars, &m)) return -1;
   return add_map(std::move(m));
+}
+
+// __PSStencilMap and its red/black forms: kernel, domain, grids, scalars.
+static PSStencil map_varargs(const char *fn, void *kernel, int color, va_list vl) {
+  if (!need_rt(fn)) return -1;
+  const int k = (int)(intptr_t)kernel;
+  KernelSig sig;
+  if (!kernel_sig(k, &sig)) {
+    fail(PS_ERR_UNKNOWN_KERNEL, "%s: unknown stencil id %d", fn, k);
+    return -1;
+  }
+  __PSDomain dom = va_arg(vl, __PSDomain);
+  void *grids[16];
+  double sc[16];
+  const int ng = map_ngrids(sig, color);
+  for (int i = 0; i < ng; ++i) grids[i] = va_arg(vl, void *);
+  for (int i = 0; i < sig.nscalars; ++i) sc[i] = va_arg(vl, double);
+  Map m;
+  if (!map_from(k, dom, ng, grids, sig.nscalars, sc, &m, color)) return -1;
+  return add_map(std::move(m));
+}
+
+PSStencil __PSStencilMapRedBlack(void *kernel, ...) {
+  va_list vl;
+  va_start(vl, kernel);
+  const PSStencil s = map_varargs("PSStencilMapRedBlack", kernel, 2, vl);
+  va_end(vl);
+  return s;
+}
+
+PSStencil __PSStencilMapRed(void *kernel, ...) {
+  va_list vl;
+  va_start(vl, kernel);
+  const PSStencil s = map_varargs("PSStencilMapRed", kernel, 0, vl);
+  va_end(vl);
+  return s;
+}
+
+PSStencil __PSStencilMapBlack(void *kernel, ...) {
+  va_list vl;
+  va_start(vl, kernel);
+  const PSStencil s = map_varargs("PSStencilMapBlack", kernel, 1, vl);
+  va_end(vl);
+  return s;
+}
+
+PSStencil PSStencilMapColorV(int kernel, int color, const PSDomain3D *dom, int ngrids,
+                             void *const *grids, int nscalars, const double *scalars) {
+  if (!need_rt("PSStencilMapColorV")) return -1;
+  if (!dom || (ngrids && !grids) || (nscalars && !scalars)) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSStencilMapColorV: NULL argument");
+    return -1;
+  }
+  Map m;
+  if (!map_from(kernel, *dom, ngrids, grids, nscalars, scalars, &m, color)) return -1;
+  return add_map(std::move(m));
+}
+
+int PSPointStencilNew(int boundary, int npoints, const int *offsets, const double *weights) {
+  if (!need_rt("PSPointStencilNew")) return -1;
+  if (boundary < PS_BOUNDARY_NONE || boundary > PS_BOUNDARY_CLAMP) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSPointStencilNew: unknown boundary rule %d", boundary);
+    return -1;
+  }
+  if (npoints < 1 || npoints > PS_MAX_POINTS || !offsets) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSPointStencilNew: %d points (1..%d, offsets non-NULL)",
+         npoints, PS_MAX_POINTS);
+    return -1;
+  }
+  PointStencil ps;
+  ps.boundary = boundary;
+  ps.n = npoints;
+  ps.unit = true;
+  for (int i = 0; i < npoints; ++i) {
+    for (int d = 0; d < 3; ++d) {
+      const int o = offsets[3 * i + d];
+      if (o < -PS_MAX_POINT_RADIUS || o > PS_MAX_POINT_RADIUS) {
+        fail(PS_ERR_INVALID_ARGUMENT, "PSPointStencilNew: offset %d of point %d beyond +-%d",
+             o, i, PS_MAX_POINT_RADIUS);
+        return -1;
+      }
+      ps.d[i][d] = o;
+    }
+    ps.w[i] = weights ? weights[i] : 1.0;
+    if (weights && !std::isfinite(weights[i])) {
+      fail(PS_ERR_INVALID_ARGUMENT, "PSPointStencilNew: weight %d is not finite", i);
+      return -1;
+    }
+    if (ps.w[i] != 1.0) ps.unit = false;
+  }
+  return register_points(ps);
 }
 
 void PSStencilRunV(int n, const PSStencil *stencils, int iter) {

@@ -41,6 +41,22 @@ MANUAL_TESTS = [
     "test_7-pt-int-type",
     "test_7-pt-periodic",
     "test_reduction-3d-sum",
+    "test_3-pt-1d",
+    "test_3-pt-periodic",
+    "test_5-pt-2d",
+    "test_5-pt-periodic",
+    "test_9-pt-2d",
+    "test_9-pt-reduction",
+    "test_9-pt-periodic-reduction",
+    "test_27-pt",
+    "test_27-pt-periodic",
+    "test_27-pt-reduction",
+    "test_asymmetric",
+    "test_asymmetric-periodic",
+    "test_stencil-hole",
+    "test_redblack",
+    "test_redblack-periodic",
+    "test_16",
 ]
 
 DIFF_N, DIFF_COUNT = 21, 6

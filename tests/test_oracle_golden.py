@@ -151,3 +151,43 @@ def test_uniform_stream_matches_python(oracle):
     b = synth.uniform((3, 5, 7), seed=1)
     assert np.array_equal(a, b)
     assert a.min() >= 0.0 and a.max() < 1.0
+
+
+@pytest.mark.parametrize("name", sorted(__import__("system_cases").CASES))
+def test_point_stencil_system_tests(oracle, name):
+    # The point-list system tests (tests/system_cases.py) through the
+    # oracle's point-stencil restatement, against the programs' stdout.
+    import system_cases as sc
+    case = dict(sc.CASES[name])
+    dom = sc.domain(case)
+    case["grids"] = sc.initial(case)
+    text = sc.run(
+        case,
+        lambda a, b: oracle.points(a, b, dom, case["points"],
+                                   boundary=case["boundary"]),
+        lambda a, color: oracle.points(a, a, dom, case["points"],
+                                       boundary=case["boundary"], color=color),
+        lambda a: oracle.reduce_ref(a.reshape(-1), oracle.PS_SUM),
+        lambda a: gio.dump_text(a, sc.fmt(case)))
+    assert text == gio.stdout_text(name)
+
+
+def test_point_stencil_matches_sweep7(oracle):
+    # The point-list form of DIFFUSION7 (clamp, weights in expression order
+    # cc cw ce cs cn cb ct) equals the dedicated 7-point restatement.
+    g = oracle.fill_uniform((9, 10, 11), seed=5)
+    ref, out = np.zeros_like(g), np.zeros_like(g)
+    coef = [0.11, 0.12, 0.13, 0.14, 0.15, 0.16, 0.4]  # ce cw cn cs ct cb cc
+    dom = (0, 11, 0, 10, 0, 9)
+    oracle.sweep7(oracle.V_DIFFUSION7, g, ref, dom, coef=coef)
+    pts = [(0, 0, 0), (-1, 0, 0), (1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, -1),
+           (0, 0, 1)]
+    w = [coef[6], coef[1], coef[0], coef[3], coef[2], coef[5], coef[4]]
+    oracle.points(g, out, dom, pts, weights=w, boundary=2)
+    assert np.array_equal(ref.view(np.uint32), out.view(np.uint32))
+
+
+def test_point_stencil_rejects_out_of_grid_reads(oracle):
+    g = np.zeros((4, 4, 4), np.float32)
+    with pytest.raises(ValueError):
+        oracle.points(g, g.copy(), (0, 4, 0, 4, 0, 4), [(1, 0, 0)], boundary=0)
