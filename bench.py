@@ -714,6 +714,93 @@ def run_gpu_batch(args, dist):
             g.free()
 
 
+# ---------------------------------------------------------------------------
+# Point-list stencils (27-point periodic sum; 7-point diffusion as points)
+# ---------------------------------------------------------------------------
+
+P27 = [(x, y, z) for z in (-1, 0, 1) for (x, y) in
+       [(0, 0), (1, 0), (-1, 0), (0, 1), (1, 1), (-1, 1), (0, -1), (1, -1), (-1, -1)]]
+P7 = [(0, 0, 0), (-1, 0, 0), (1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, -1), (0, 0, 1)]
+
+
+def run_gpu_points(args, dist):
+    """K sweeps of a point stencil over an N^3 float grid, ping-pong.
+
+    points27: the 27-point unit-weight periodic sum of
+    tests/system_tests/test_cases/test_27-pt-periodic.c at N^3.
+    points7: the clamped 7-point diffusion (cc=0.4, others 0.1) as a point
+    stencil, to compare the generic kernel with the dedicated one.
+    """
+    os.environ.setdefault("PS_DEVICE", str(dist.local))
+    import physis_gb300 as ps
+    from physis_gb300 import synth
+    ps.init()
+    L = ps.lib()
+    shape = (N, N, N)
+    init = synth.uniform(shape, 1)
+    g1, g2 = ps.Grid(shape), ps.Grid(shape)
+    g1.copyin(init)
+    g2.copyin(init)
+    dom = ps.full_domain(shape)
+    if args.workload == "points27":
+        k = ps.point_stencil(P27, boundary=ps.BOUNDARY_PERIODIC)
+        label = f"27-point periodic sum fp32 {N}^3 (point stencil)"
+    else:
+        k = ps.point_stencil(P7, weights=[0.4] + [0.1] * 6, boundary=ps.BOUNDARY_CLAMP)
+        label = f"7-point clamped diffusion fp32 {N}^3 as a point stencil"
+    if args.warps or args.rows:
+        ps.set_launch_shape(k, warps=args.warps, rows=args.rows)
+    m1 = ps.stencil_map(k, dom, [g1, g2])
+    m2 = ps.stencil_map(k, dom, [g2, g1])
+    K, W = args.steps, args.warmup
+
+    def steps(n):
+        pairs, rem = divmod(n, 2)
+        if pairs:
+            ps.stencil_run([m1, m2], pairs)
+        if rem:
+            ps.stencil_run([m1], 1)
+
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    steps(W)
+    ps.synchronize()
+    dist.barrier()
+    n0 = ps.launch_count()
+    L.PSEventRecord(0)
+    steps(K)
+    L.PSEventRecord(1)
+    ps.synchronize()
+    ms = L.PSEventElapsedMs(0, 1)
+    launches = ps.launch_count() - n0
+    dist.barrier()
+    clk = clocks.stop()
+    ps.check()
+    ms_max = dist.reduce(ms, "MAX")
+    cells = float(N) ** 3
+    value = dist.ws * cells * K / (ms_max / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    achieved = cells * BYTES_PER_LUP / (ms / K / 1e3) / 1e9
+    if dist.rank == 0:
+        line = {
+            "metric": f"GLUPS, {label}", "value": value, "unit": "GLUPS",
+            "n_gpus": dist.ws, "steps": K, "warmup": W, "ms_per_step": ms_max / K,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic uniform[0,1) seed 1 (SplitMix64)",
+            "config": {"workload": label, "grid": [N, N, N],
+                       "launch_shape": list(ps.get_launch_shape(k)[:2]),
+                       "l2": "inputs larger than L2" if N >= 256 else "fits L2"},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "peak_source": peak_kind, "bytes_per_lup": BYTES_PER_LUP},
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    g1.free()
+    g2.free()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -731,7 +818,7 @@ def main():
     ap.add_argument("--batch-small", action="store_true",
                     help="batch workload with 48 small grids (launch-bound regime)")
     ap.add_argument("--workload", default="diffusion",
-                    choices=["diffusion", "himeno", "batch"],
+                    choices=["diffusion", "himeno", "batch", "points27", "points7"],
                     help="diffusion: 7-point 512^3 (the headline); himeno: "
                          "19-point Jacobi 257x257x513 with fused residual")
     args = ap.parse_args()
@@ -747,6 +834,8 @@ def main():
             run_gpu_himeno(args, dist)
         elif args.workload == "batch":
             run_gpu_batch(args, dist)
+        elif args.workload in ("points27", "points7"):
+            run_gpu_points(args, dist)
         else:
             run_gpu(args, dist)
     finally:

@@ -246,6 +246,31 @@ enum PSBoundary { PS_BOUNDARY_NONE = 0, PS_BOUNDARY_PERIODIC = 1, PS_BOUNDARY_CL
  * (translator/reference_runtime_builder.cc:391-664). */
 int PSPointStencilNew(int boundary, int npoints, const int *offsets, const double *weights);
 
+/* Compiles a stencil function written in the reference's stencil language
+ * and returns its kernel id, or -1 with the error recorded (the compiler log
+ * for a source that does not compile; PS_ERR_UNSUPPORTED without NVRTC).
+ * `source` holds the function `void name(const int x[, const int y[, const
+ * int z]], <grids and scalars>)` -- index parameters first, then
+ * PSGrid{1,2,3}D{Float,Double,Int,Long} grids and int/long/float/double
+ * scalars in any order -- and whatever macros and helper functions it uses.
+ * The body may use PSGridGet(g, ...), PSGridGetPeriodic(g, ...),
+ * PSGridEmit(g, v) and PSGridDim(g, d) (include/physis/physis_user.h:75-81,
+ * docs/programming.md).  PSStencilMap(id, dom, args...) then takes the
+ * function's grids and scalars in its parameter order; the red/black maps
+ * run it on one colour at a time (the function is then responsible for
+ * reading only the other colour, as in the reference).  Float arithmetic
+ * is compiled without FMA contraction, so results equal a REF build of the
+ * same function (gcc -ffp-contract=off).  Compiling the same source and
+ * name again returns the same id.  Replaces the translator's lowering of
+ * stencil functions (translator/cuda_runtime_builder.cc:1099-1228). */
+int PSStencilFunctionNew(const char *source, const char *name);
+
+/* Parses and compiles a stencil function like PSStencilFunctionNew without
+ * loading it (no device or PSInit needed).  Returns PS_OK, else
+ * PS_ERR_INVALID_ARGUMENT (the reason and compiler log, truncated, in
+ * log[0..logsize)) or PS_ERR_UNSUPPORTED without NVRTC. */
+int PSStencilFunctionCheck(const char *source, const char *name, char *log, size_t logsize);
+
 /* Map colours: every cell, red (x + y + z even), black (odd), red then black. */
 enum PSMapColor {
   PS_COLOR_ALL = -1,

@@ -56,7 +56,8 @@ PSGetLaunchShape PSTestFailNextAllocs PSTestDeviceWaitTimeout PSReduceNoAlloc
 PSSetTemporalBlocking PSGetTemporalBlocking PSSetAutotune PSSetTuneCachePath
 PSLoadTuneCache PSClearTuning PSGetStencilPlan PSBatchCreate PSBatchRun PSBatchFree
 PSSetBatchShape __PSStencilMapRedBlack __PSStencilMapRed __PSStencilMapBlack
-PSStencilMapColorV PSPointStencilNew""".split()
+PSStencilMapColorV PSPointStencilNew PSStencilFunctionNew
+PSStencilFunctionCheck""".split()
 
 
 class PSDomain(ctypes.Structure):
@@ -163,6 +164,11 @@ def lib():
     L.PSStencilMapColorV.argtypes = [i, i, ctypes.POINTER(PSDomain), i,
                                      ctypes.POINTER(vp), i, ctypes.POINTER(d)]
     L.PSStencilMapColorV.restype = i
+    L.PSStencilFunctionNew.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+    L.PSStencilFunctionNew.restype = i
+    L.PSStencilFunctionCheck.argtypes = [ctypes.c_char_p, ctypes.c_char_p,
+                                         ctypes.c_char_p, ctypes.c_size_t]
+    L.PSStencilFunctionCheck.restype = i
     _lib = L
     return L
 
@@ -273,6 +279,21 @@ def point_stencil(points, weights=None, boundary=BOUNDARY_NONE):
     k = lib().PSPointStencilNew(boundary, n, offs, w)
     check()
     return k
+
+
+def stencil_function(source, name):
+    """Compiles a stencil function (the reference's stencil language) with
+    NVRTC; returns its kernel id."""
+    k = lib().PSStencilFunctionNew(source.encode(), name.encode())
+    check()
+    return k
+
+
+def stencil_function_check(source, name):
+    """(code, log) of compiling a stencil function without a device."""
+    buf = ctypes.create_string_buffer(4096)
+    code = lib().PSStencilFunctionCheck(source.encode(), name.encode(), buf, len(buf))
+    return code, buf.value.decode(errors="replace")
 
 
 def stencil_map_color(kernel, color, dom, grids, scalars=()):

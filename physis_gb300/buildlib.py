@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libphysis_gb300.so")
 SOURCES = ["runtime.cpp", "march.cpp", "stencil7.cu", "temporal7.cu", "himeno19.cu",
-           "reduce.cu", "batch.cu", "points.cu"]
+           "reduce.cu", "batch.cu", "points.cu", "jit.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -60,7 +60,7 @@ def build(verbose=False):
     if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(o)
                                    for o in objs):
         return LIB
-    cmd = [nvcc(), "-shared"] + ARCH + ["-o", LIB] + objs + ["-lcuda"] * 0
+    cmd = [nvcc(), "-shared"] + ARCH + ["-o", LIB] + objs + ["-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

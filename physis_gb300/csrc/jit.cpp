@@ -1,0 +1,457 @@
+// Stencil functions compiled at run time (NVRTC) -- the translator-free
+// front end.
+//
+// The reference turns a user stencil function such as
+//     void kernel(const int x, const int y, const int z,
+//                 PSGrid3DFloat g1, PSGrid3DFloat g2, float c) {
+//       float v = PSGridGet(g1, x, y, z) + ... ;
+//       PSGridEmit(g2, v * c);
+//     }
+// into a CUDA kernel with its source-to-source translator (physisc;
+// translator/cuda_runtime_builder.cc:1099-1228 generates the run kernel, one
+// thread per (x, y) and a loop over z; include/physis/physis_cuda.h:237-269
+// the index arithmetic).  Here the function's own source text is compiled at
+// run time: a short device prelude gives PSGridGet / PSGridGetPeriodic /
+// PSGridEmit / PSGridDim and the PSGrid* types their device meaning, every
+// unannotated function is a device function (-default-device), and a
+// generated __global__ entry walks the domain and calls the function at each
+// point.  Options --fmad=false and IEEE division/square root keep every
+// float expression exactly as the C source writes it, so results match the
+// REF target (the same source built by gcc with -ffp-contract=off) bit for
+// bit.  NVRTC is loaded with dlopen; without it the entry points report
+// PS_ERR_UNSUPPORTED.  The compiled image is loaded with the driver API into
+// the runtime's context and never inspected.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <dlfcn.h>
+
+#include <cstdio>
+#include <cstring>
+#include <regex>
+#include <string>
+#include <vector>
+
+#include "ps_internal.h"
+
+namespace psg {
+namespace {
+
+// ---- NVRTC, resolved at run time -----------------------------------------
+typedef int nvrtcResult_t;
+typedef struct _nvrtcProgram *nvrtcProgram_t;
+struct Nvrtc {
+  bool tried = false, ok = false;
+  nvrtcResult_t (*create)(nvrtcProgram_t *, const char *, const char *, int,
+                          const char *const *, const char *const *) = nullptr;
+  nvrtcResult_t (*compile)(nvrtcProgram_t, int, const char *const *) = nullptr;
+  nvrtcResult_t (*log_size)(nvrtcProgram_t, size_t *) = nullptr;
+  nvrtcResult_t (*log)(nvrtcProgram_t, char *) = nullptr;
+  nvrtcResult_t (*cubin_size)(nvrtcProgram_t, size_t *) = nullptr;
+  nvrtcResult_t (*cubin)(nvrtcProgram_t, char *) = nullptr;
+  nvrtcResult_t (*destroy)(nvrtcProgram_t *) = nullptr;
+};
+Nvrtc g_nvrtc;
+
+bool load_nvrtc(std::string *err) {
+  if (g_nvrtc.tried) {
+    if (!g_nvrtc.ok) *err = "NVRTC (libnvrtc.so) is not available";
+    return g_nvrtc.ok;
+  }
+  g_nvrtc.tried = true;
+  const char *names[] = {"libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so.13",
+                         "/usr/local/cuda/lib64/libnvrtc.so"};
+  void *h = nullptr;
+  for (const char *n : names)
+    if ((h = dlopen(n, RTLD_NOW | RTLD_LOCAL))) break;
+  if (!h) {
+    *err = "NVRTC (libnvrtc.so) is not available";
+    return false;
+  }
+#define PS_NVRTC_SYM(field, sym) \
+  g_nvrtc.field = reinterpret_cast<decltype(g_nvrtc.field)>(dlsym(h, sym))
+  PS_NVRTC_SYM(create, "nvrtcCreateProgram");
+  PS_NVRTC_SYM(compile, "nvrtcCompileProgram");
+  PS_NVRTC_SYM(log_size, "nvrtcGetProgramLogSize");
+  PS_NVRTC_SYM(log, "nvrtcGetProgramLog");
+  PS_NVRTC_SYM(cubin_size, "nvrtcGetCUBINSize");
+  PS_NVRTC_SYM(cubin, "nvrtcGetCUBIN");
+  PS_NVRTC_SYM(destroy, "nvrtcDestroyProgram");
+#undef PS_NVRTC_SYM
+  g_nvrtc.ok = g_nvrtc.create && g_nvrtc.compile && g_nvrtc.log_size && g_nvrtc.log &&
+               g_nvrtc.cubin_size && g_nvrtc.cubin && g_nvrtc.destroy;
+  if (!g_nvrtc.ok) *err = "libnvrtc.so lacks the expected entry points";
+  return g_nvrtc.ok;
+}
+
+// ---- driver API, resolved through the runtime ------------------------------
+struct Driver {
+  bool tried = false, ok = false;
+  CUresult (*load)(CUmodule *, const void *) = nullptr;
+  CUresult (*get)(CUfunction *, CUmodule, const char *) = nullptr;
+  CUresult (*launch)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
+                     unsigned, CUstream, void **, void **) = nullptr;
+  CUresult (*unload)(CUmodule) = nullptr;
+};
+Driver g_drv;
+
+bool load_driver(std::string *err) {
+  if (g_drv.tried) {
+    if (!g_drv.ok) *err = "driver entry points for module loading are unavailable";
+    return g_drv.ok;
+  }
+  g_drv.tried = true;
+  auto sym = [](const char *name) -> void * {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    return fn;
+  };
+  g_drv.load = reinterpret_cast<decltype(g_drv.load)>(sym("cuModuleLoadData"));
+  g_drv.get = reinterpret_cast<decltype(g_drv.get)>(sym("cuModuleGetFunction"));
+  g_drv.launch = reinterpret_cast<decltype(g_drv.launch)>(sym("cuLaunchKernel"));
+  g_drv.unload = reinterpret_cast<decltype(g_drv.unload)>(sym("cuModuleUnload"));
+  g_drv.ok = g_drv.load && g_drv.get && g_drv.launch && g_drv.unload;
+  if (!g_drv.ok) {
+    cudaGetLastError();
+    *err = "driver entry points for module loading are unavailable";
+  }
+  return g_drv.ok;
+}
+
+// ---- the device prelude -----------------------------------------------------
+// PSGrid{1,2,3}D{Float,Double,Int,Long} are one device struct per element
+// type; `cur` is the element the map's current point emits to.  Index
+// arithmetic as the reference's (physis_cuda.h:237-269): x fastest, periodic
+// reads wrap with (i + n) % n.
+const char *kPrelude = R"PSJIT(
+typedef int PSIndex;
+template <typename T> struct __PSGridDev {
+  T *p; long long row; long long plane; int nx; int ny; int nz; int rank; long long cur;
+};
+#define __PS_GRID_TYPES(N, T) \
+  typedef __PSGridDev<T> PSGrid1D##N; typedef __PSGridDev<T> PSGrid2D##N; \
+  typedef __PSGridDev<T> PSGrid3D##N;
+__PS_GRID_TYPES(Float, float)
+__PS_GRID_TYPES(Double, double)
+__PS_GRID_TYPES(Int, int)
+__PS_GRID_TYPES(Long, long long)
+template <typename T> __device__ __forceinline__ T __ps_get(const __PSGridDev<T> &g, int x) {
+  return g.p[x];
+}
+template <typename T> __device__ __forceinline__ T __ps_get(const __PSGridDev<T> &g, int x, int y) {
+  return g.p[(long long)y * g.row + x];
+}
+template <typename T>
+__device__ __forceinline__ T __ps_get(const __PSGridDev<T> &g, int x, int y, int z) {
+  return g.p[(long long)z * g.plane + (long long)y * g.row + x];
+}
+template <typename T> __device__ __forceinline__ T __ps_getp(const __PSGridDev<T> &g, int x) {
+  return g.p[(x + g.nx) % g.nx];
+}
+template <typename T>
+__device__ __forceinline__ T __ps_getp(const __PSGridDev<T> &g, int x, int y) {
+  return g.p[(long long)((y + g.ny) % g.ny) * g.row + (x + g.nx) % g.nx];
+}
+template <typename T>
+__device__ __forceinline__ T __ps_getp(const __PSGridDev<T> &g, int x, int y, int z) {
+  return g.p[(long long)((z + g.nz) % g.nz) * g.plane + (long long)((y + g.ny) % g.ny) * g.row +
+             (x + g.nx) % g.nx];
+}
+template <typename T> __device__ __forceinline__ int __ps_dim(const __PSGridDev<T> &g, int d) {
+  return d == 0 ? g.nx : (d == 1 ? g.ny : g.nz);
+}
+#define PSGridGet(g, ...) __ps_get((g), __VA_ARGS__)
+#define PSGridGetPeriodic(g, ...) __ps_getp((g), __VA_ARGS__)
+#define PSGridEmit(g, v) ((void)((g).p[(g).cur] = (v)))
+#define PSGridDim(g, d) __ps_dim((g), (d))
+)PSJIT";
+
+// Host mirror of __PSGridDev<T> (same layout for every T: one pointer).
+struct GridArg {
+  void *p;
+  long long row, plane;
+  int nx, ny, nz, rank;
+  long long cur;
+};
+
+std::string trim(const std::string &s) {
+  size_t a = s.find_first_not_of(" \t\r\n"), b = s.find_last_not_of(" \t\r\n");
+  return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+}
+
+// Parses one parameter declaration ("const int x", "PSGrid3DFloat g1",
+// "float c") into p; false if its type is not one the front end knows.
+bool parse_param(const std::string &decl, JitParam *p, std::string *err) {
+  static const std::regex grid_re("^PSGrid([123])D(Float|Double|Int|Long)$");
+  std::string d = " " + trim(decl) + " ";
+  for (const char *q : {" const ", " register ", " volatile "}) {
+    size_t at;
+    while ((at = d.find(q)) != std::string::npos) d.replace(at, strlen(q) - 1, "");
+  }
+  d = trim(d);
+  const size_t cut = d.find_last_of(" \t*&");
+  if (cut == std::string::npos) {
+    *err = "parameter '" + trim(decl) + "' has no name";
+    return false;
+  }
+  std::string type = trim(d.substr(0, cut));
+  std::string t;  // type with single spaces
+  for (char c : type)
+    if (!(c == ' ' && (t.empty() || t.back() == ' '))) t += (c == '\t' ? ' ' : c);
+  type = trim(t);
+  p->decl_type = type;
+  std::smatch m;
+  if (std::regex_match(type, m, grid_re)) {
+    p->grid = true;
+    p->rank = m[1].str()[0] - '0';
+    const std::string e = m[2].str();
+    p->type = e == "Float" ? kFloat : e == "Double" ? kDouble : e == "Int" ? kInt : kLong;
+    return true;
+  }
+  p->grid = false;
+  p->rank = 0;
+  if (type == "int" || type == "PSIndex" || type == "signed int") p->type = kInt;
+  else if (type == "long" || type == "long int" || type == "long long" ||
+           type == "long long int")
+    p->type = kLong;
+  else if (type == "float") p->type = kFloat;
+  else if (type == "double") p->type = kDouble;
+  else {
+    *err = "parameter type '" + type + "' is not supported (grids PSGrid{1,2,3}D{Float,"
+           "Double,Int,Long}, scalars int/long/float/double)";
+    return false;
+  }
+  return true;
+}
+
+// Finds `void name(...)` in src and parses its parameters.
+bool parse_signature(const std::string &src, const std::string &name, JitKernel *k,
+                     std::string *err) {
+  const std::regex head("\\bvoid\\s+" + name + "\\s*\\(");
+  std::smatch m;
+  if (!std::regex_search(src, m, head)) {
+    *err = "no definition 'void " + name + "(...)' in the stencil source";
+    return false;
+  }
+  size_t i = m.position(0) + m.length(0);
+  int depth = 1;
+  std::string cur;
+  std::vector<std::string> decls;
+  for (; i < src.size() && depth > 0; ++i) {
+    const char c = src[i];
+    if (c == '(') ++depth;
+    if (c == ')' && --depth == 0) break;
+    if (c == ',' && depth == 1) {
+      decls.push_back(cur);
+      cur.clear();
+    } else {
+      cur += c;
+    }
+  }
+  if (depth != 0) {
+    *err = "unbalanced parameter list of " + name;
+    return false;
+  }
+  if (!trim(cur).empty()) decls.push_back(cur);
+  k->params.clear();
+  k->nd = 0;
+  bool seen_grid = false;
+  for (const std::string &d : decls) {
+    JitParam p;
+    if (!parse_param(d, &p, err)) return false;
+    if (!p.grid && !seen_grid && p.type == kInt && k->params.empty() && k->nd < 3) {
+      ++k->nd;  // a leading index parameter
+      continue;
+    }
+    if (p.grid) seen_grid = true;
+    if (!p.grid && !seen_grid) {
+      *err = "stencil " + name + ": index parameters must come first, then the grids";
+      return false;
+    }
+    k->params.push_back(p);
+  }
+  if (k->nd < 1) {
+    *err = "stencil " + name + " has no index parameters (const int x[, y[, z]])";
+    return false;
+  }
+  k->ngrids = k->nscalars = 0;
+  for (const JitParam &p : k->params) (p.grid ? k->ngrids : k->nscalars)++;
+  if (k->ngrids < 1) {
+    *err = "stencil " + name + " takes no grid";
+    return false;
+  }
+  return true;
+}
+
+std::string scalar_ctype(int type) {
+  switch (type) {
+    case kInt: return "int";
+    case kLong: return "long long";
+    case kFloat: return "float";
+    default: return "double";
+  }
+}
+
+// The generated entry: one thread per (x, y), a z-chunk per block row in z;
+// red/black maps visit every other x from the REF start
+// min + ((min & 1) ^ ((y + z + color) % 2))
+// (translator/reference_runtime_builder.cc:585-600).
+std::string entry_source(const JitKernel &k) {
+  std::string s =
+      "\nextern \"C\" __global__ void __launch_bounds__(256) __ps_entry(int dmin0, int dmax0, "
+      "int dmin1, int dmax1, int dmin2, int dmax2, int color, int zlen";
+  for (size_t i = 0; i < k.params.size(); ++i) {
+    const JitParam &p = k.params[i];
+    s += ", " + (p.grid ? p.decl_type : scalar_ctype(p.type)) + " a" + std::to_string(i);
+  }
+  s += ") {\n"
+       "  const int tx = blockIdx.x * blockDim.x + threadIdx.x;\n"
+       "  const int y = dmin1 + blockIdx.y * blockDim.y + threadIdx.y;\n"
+       "  if (y >= dmax1) return;\n"
+       "  const int zs = dmin2 + blockIdx.z * zlen;\n"
+       "  const int ze = min(zs + zlen, dmax2);\n"
+       "  for (int z = zs; z < ze; ++z) {\n"
+       "    const int x = color < 0 ? dmin0 + tx\n"
+       "        : dmin0 + ((dmin0 & 1) ^ ((y + z + color) % 2)) + 2 * tx;\n"
+       "    if (x >= dmax0) continue;\n";
+  for (size_t i = 0; i < k.params.size(); ++i) {
+    if (!k.params[i].grid) continue;
+    const std::string a = "a" + std::to_string(i);
+    const int r = k.params[i].rank;
+    s += "    " + a + ".cur = " +
+         (r == 1 ? std::string("x")
+                 : r == 2 ? "(long long)y * " + a + ".row + x"
+                          : "(long long)z * " + a + ".plane + (long long)y * " + a +
+                                ".row + x") +
+         ";\n";
+  }
+  s += "    " + k.name + "(x";
+  if (k.nd >= 2) s += ", y";
+  if (k.nd >= 3) s += ", z";
+  for (size_t i = 0; i < k.params.size(); ++i) s += ", a" + std::to_string(i);
+  s += ");\n  }\n}\n";
+  return s;
+}
+
+}  // namespace
+
+bool jit_build(const char *source, const char *name, JitKernel *k, std::vector<char> *image,
+               std::string *err) {
+  if (!load_nvrtc(err)) return false;
+  k->name = name;
+  k->source = source;
+  if (!parse_signature(k->source, k->name, k, err)) return false;
+  const std::string program =
+      std::string(kPrelude) + "#line 1 \"stencil\"\n" + k->source + "\n" + entry_source(*k);
+  nvrtcProgram_t prog = nullptr;
+  if (g_nvrtc.create(&prog, program.c_str(), "stencil.cu", 0, nullptr, nullptr) != 0) {
+    *err = "nvrtcCreateProgram failed";
+    return false;
+  }
+  const char *opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "--fmad=false",
+                        "--prec-div=true", "--prec-sqrt=true", "--ftz=false",
+                        "--device-as-default-execution-space", "-DPS_JIT=1"};
+  const int rc = g_nvrtc.compile(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+  if (rc != 0) {
+    size_t n = 0;
+    g_nvrtc.log_size(prog, &n);
+    std::string log(n, '\0');
+    if (n) g_nvrtc.log(prog, &log[0]);
+    g_nvrtc.destroy(&prog);
+    *err = "stencil " + k->name + " does not compile: " + log.substr(0, 600);
+    return false;
+  }
+  size_t n = 0;
+  g_nvrtc.cubin_size(prog, &n);
+  image->resize(n);
+  g_nvrtc.cubin(prog, image->data());
+  g_nvrtc.destroy(&prog);
+  return true;
+}
+
+bool jit_compile(const char *source, const char *name, JitKernel *k, std::string *err) {
+  std::vector<char> image;
+  if (!jit_build(source, name, k, &image, err) || !load_driver(err)) return false;
+  CUmodule mod = nullptr;
+  CUfunction fn = nullptr;
+  if (g_drv.load(&mod, image.data()) != CUDA_SUCCESS) {
+    *err = "loading the compiled stencil failed";
+    return false;
+  }
+  if (g_drv.get(&fn, mod, "__ps_entry") != CUDA_SUCCESS) {
+    g_drv.unload(mod);
+    *err = "compiled stencil has no entry";
+    return false;
+  }
+  k->module = mod;
+  k->func = fn;
+  return true;
+}
+
+void jit_unload(JitKernel *k) {
+  if (k->module && g_drv.unload) g_drv.unload(static_cast<CUmodule>(k->module));
+  k->module = k->func = nullptr;
+}
+
+cudaError_t jit_launch(const JitKernel &k, const Box &dom, int color, const GridView *grids,
+                       const double *scalars, int sm_count, cudaStream_t s) {
+  const int nxd = dom.max[0] - dom.min[0], nyd = dom.max[1] - dom.min[1],
+            nzd = dom.max[2] - dom.min[2];
+  if (nxd <= 0 || nyd <= 0 || nzd <= 0) return cudaSuccess;
+  const unsigned bx = 64, by = 4;
+  const int xs = color < 0 ? nxd : (nxd + 1) / 2;
+  const unsigned gx = (unsigned)((xs + bx - 1) / bx), gy = (unsigned)((nyd + by - 1) / by);
+  long long want = 8LL * sm_count;  // blocks in flight: a few per SM
+  long long gz = (want + (long long)gx * gy - 1) / ((long long)gx * gy);
+  if (gz < 1) gz = 1;
+  if (gz > nzd) gz = nzd;
+  const int zlen = (int)((nzd + gz - 1) / gz);
+  gz = (nzd + zlen - 1) / zlen;
+  if (gy > 65535 || gz > 65535) return cudaErrorInvalidConfiguration;
+
+  // argument storage: 8 ints, then each parameter at its alignment
+  std::vector<unsigned char> buf(64 + 64 * k.params.size());
+  std::vector<void *> args;
+  size_t off = 0;
+  auto put = [&](const void *v, size_t n, size_t align) {
+    off = (off + align - 1) / align * align;
+    memcpy(buf.data() + off, v, n);
+    args.push_back(buf.data() + off);
+    off += n;
+  };
+  const int head[8] = {dom.min[0], dom.max[0], dom.min[1], dom.max[1],
+                       dom.min[2], dom.max[2], color, zlen};
+  for (int v : head) put(&v, 4, 4);
+  int gi = 0, si = 0;
+  for (const JitParam &p : k.params) {
+    if (p.grid) {
+      const GridView &g = grids[gi++];
+      GridArg a;
+      a.p = g.ptr;
+      a.row = g.pitch / g.esz;
+      a.plane = a.row * g.ny;
+      a.nx = g.nx;
+      a.ny = g.ny;
+      a.nz = g.nz;
+      a.rank = p.rank;
+      a.cur = 0;
+      put(&a, sizeof(a), 8);
+    } else {
+      const double v = scalars[si++];
+      switch (p.type) {
+        case kInt: { const int t = (int)v; put(&t, 4, 4); break; }
+        case kLong: { const long long t = (long long)v; put(&t, 8, 8); break; }
+        case kFloat: { const float t = (float)v; put(&t, 4, 4); break; }
+        default: put(&v, 8, 8); break;
+      }
+    }
+  }
+  const CUresult r = g_drv.launch(static_cast<CUfunction>(k.func), gx, gy, (unsigned)gz, bx,
+                                  by, 1, 0, static_cast<CUstream>(s), args.data(), nullptr);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorLaunchFailure;
+}
+
+}  // namespace psg

@@ -1,10 +1,13 @@
 // Internal interface between the host runtime (runtime.cpp) and the kernel
-// translation units.  Plain structs only; nothing here is exported.
+// translation units.  Nothing here is exported.
 #pragma once
 
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <string>
+#include <vector>
 
 namespace psg {
 
@@ -131,6 +134,32 @@ struct PointsArgs {
 size_t points_smem_bytes(const PointsArgs &a, const MarchConfig &cfg);
 cudaError_t launch_points(const PointsArgs &a, const MarchConfig &cfg, int sm_count,
                           cudaStream_t s);
+
+// ---- Stencil functions compiled at run time (jit.cpp) ---------------------
+struct JitParam {
+  bool grid;              // a PSGrid* parameter, else a scalar
+  int type;               // ElemType
+  int rank;               // grids: 1..3
+  std::string decl_type;  // the type as declared ("PSGrid3DFloat", "float")
+};
+struct JitKernel {
+  std::string name, source;
+  int nd = 0;                     // index parameters (x[, y[, z]])
+  std::vector<JitParam> params;   // after the indices, in order
+  int ngrids = 0, nscalars = 0;
+  void *module = nullptr, *func = nullptr;
+};
+// Parses `void name(...)` in source and compiles source + entry for sm_103a
+// into *image (no device needed).  false with *err on failure.
+bool jit_build(const char *source, const char *name, JitKernel *k, std::vector<char> *image,
+               std::string *err);
+// jit_build, then loads the image into the current context.
+bool jit_compile(const char *source, const char *name, JitKernel *k, std::string *err);
+void jit_unload(JitKernel *k);
+// Runs the compiled stencil over dom (color -1 every point, 0 red, 1 black):
+// grids[] and scalars[] in parameter order.
+cudaError_t jit_launch(const JitKernel &k, const Box &dom, int color, const GridView *grids,
+                       const double *scalars, int sm_count, cudaStream_t s);
 
 // ---- Reductions (reduce.cu) ----------------------------------------------
 // Reduces every element of g with op.  The 8-byte result is written to

@@ -49,6 +49,8 @@ constexpr int kNumKernels = 8;
 constexpr int kSlotPoints = 7;     // launch-shape slot shared by all point stencils
 constexpr int kPointsBase = 1024;  // kernel id of the first registered point stencil
 constexpr int kMaxPointStencils = 1 << 16;
+constexpr int kFuncBase = 1 << 20;     // kernel id of the first compiled stencil function
+constexpr int kMaxFunctions = 1 << 16;
 
 // Tensor maps are cached per (device view, box); an entry is dropped when
 // its grid is freed.
@@ -114,6 +116,7 @@ struct Runtime {
   std::string tune_path;  // JSON-lines cache file ("" = in memory only)
   std::string gpu_name;
   std::vector<PointStencil> points;  // kernel id kPointsBase + index
+  std::deque<psg::JitKernel> funcs;  // kernel id kFuncBase + index
 };
 
 Runtime *rt = nullptr;
@@ -279,6 +282,7 @@ void drop_tmaps(const void *ptr) {
 struct KernelSig {
   int ngrids, nscalars;
   const char *name;
+  const psg::JitKernel *fn = nullptr;  // compiled stencil functions: the signature
 };
 
 const PointStencil *point_stencil(int k) {
@@ -286,7 +290,16 @@ const PointStencil *point_stencil(int k) {
   return &rt->points[k - kPointsBase];
 }
 
+const psg::JitKernel *jit_kernel(int k) {
+  if (!rt || k < kFuncBase || k - kFuncBase >= (int)rt->funcs.size()) return nullptr;
+  return &rt->funcs[k - kFuncBase];
+}
+
 bool kernel_sig(int k, KernelSig *s) {
+  if (const psg::JitKernel *f = jit_kernel(k)) {
+    *s = {f->ngrids, f->nscalars, f->name.c_str(), f};
+    return true;
+  }
   switch (k) {
     case PS_KERNEL_COPY: *s = {2, 0, "PS_KERNEL_COPY"}; return true;
     case PS_KERNEL_DIFFUSION7: *s = {2, 7, "PS_KERNEL_DIFFUSION7"}; return true;
@@ -401,11 +414,40 @@ bool validate_points(const Map &m, const PointStencil &ps) {
   return true;
 }
 
+// A compiled stencil function's map: each grid has the element type and rank
+// its parameter declares, and every grid of the function's rank covers the
+// domain (the point a map emits to).  Reads at other indices are the
+// function's own business, as in the reference.
+bool validate_function_map(const Map &m, const psg::JitKernel &f) {
+  int gi = 0;
+  for (const psg::JitParam &p : f.params) {
+    if (!p.grid) continue;
+    const Grid *g = m.grids[gi++];
+    if (g->type != p.type || g->ndims != p.rank)
+      return fail(PS_ERR_INVALID_ARGUMENT,
+                  "%s: grid argument %d is a %dD grid of type %d, the parameter is %s",
+                  f.name.c_str(), gi - 1, g->ndims, g->type, p.decl_type.c_str());
+    if (p.rank != f.nd) continue;
+    for (int d = 0; d < 3; ++d)
+      if (m.dom.min[d] < m.dom.max[d] &&
+          (m.dom.min[d] < 0 || m.dom.max[d] > g->dim[d]))
+        return fail(PS_ERR_INVALID_ARGUMENT,
+                    "%s: domain [%d,%d) in dim %d outside grid argument %d of size %d",
+                    f.name.c_str(), m.dom.min[d], m.dom.max[d], d, gi - 1, g->dim[d]);
+  }
+  for (int d = 0; d < 3; ++d)
+    if (m.dom.min[d] > m.dom.max[d])
+      return fail(PS_ERR_INVALID_ARGUMENT, "%s: empty-reversed domain in dim %d",
+                  f.name.c_str(), d);
+  return true;
+}
+
 // Validates a map's grids, scalars and domain against its builtin.
 bool validate_map(const Map &m) {
   KernelSig sig;
   if (!kernel_sig(m.kernel, &sig))
     return fail(PS_ERR_UNKNOWN_KERNEL, "unknown builtin stencil id %d", m.kernel);
+  if (sig.fn) return validate_function_map(m, *sig.fn);
   const Grid *g0 = m.grids[0];
   for (const Grid *g : m.grids) {
     if (g->type != g0->type || g->dim[0] != g0->dim[0] || g->dim[1] != g0->dim[1] ||
@@ -509,8 +551,31 @@ bool launch_s7(const Map &m, const GridView &in, const GridView &out) {
   return true;
 }
 
+// One compiled-function map: one launch per colour it runs.
+bool launch_function_map(const Map &m, const psg::JitKernel &f) {
+  psg::Box box;
+  for (int d = 0; d < 3; ++d) {
+    box.min[d] = m.dom.min[d];
+    box.max[d] = m.dom.max[d];
+  }
+  if (box.min[0] >= box.max[0] || box.min[1] >= box.max[1] || box.min[2] >= box.max[2])
+    return true;
+  GridView views[64];
+  for (size_t i = 0; i < m.grids.size() && i < 64; ++i) views[i] = view(m.grids[i]);
+  const int colors[2] = {m.color == 2 ? 0 : m.color, 1};
+  const int ncol = m.color == 2 ? 2 : 1;
+  for (int c = 0; c < ncol; ++c) {
+    cudaError_t e = psg::jit_launch(f, box, colors[c], views, m.scalars.data(), rt->sm_count,
+                                    rt->stream);
+    if (!cuda_ok(e, "stencil function launch")) return false;
+    ++rt->launches;
+  }
+  return true;
+}
+
 bool launch_map(const Map &m, bool want_gosa) {
   if (const PointStencil *ps = point_stencil(m.kernel)) return launch_points_map(m, *ps);
+  if (const psg::JitKernel *f = jit_kernel(m.kernel)) return launch_function_map(m, *f);
   const Grid *g0 = m.grids[0];
   psg::Box box;
   for (int d = 0; d < 3; ++d) {
@@ -705,12 +770,15 @@ Map *lookup_map(PSStencil s) {
 // Kernels a red/black map accepts: point stencils and the 7-point builtins
 // (run as their point-stencil equivalents).
 bool colorable(int kernel) {
-  return point_stencil(kernel) || kernel == PS_KERNEL_SUM7 || kernel == PS_KERNEL_DIFFUSION7;
+  return point_stencil(kernel) || jit_kernel(kernel) || kernel == PS_KERNEL_SUM7 ||
+         kernel == PS_KERNEL_DIFFUSION7;
 }
 
 // Grids a map of `kernel` with `color` takes: a red/black map updates its one
 // grid in place.
-int map_ngrids(const KernelSig &sig, int color) { return color >= 0 ? 1 : sig.ngrids; }
+int map_ngrids(const KernelSig &sig, int color) {
+  return (color >= 0 && !sig.fn) ? 1 : sig.ngrids;
+}
 
 bool map_from(int kernel, const __PSDomain &dom, int ngrids, void *const *grids,
               int nscalars, const double *scalars, Map *out, int color = -1) {
@@ -722,6 +790,8 @@ bool map_from(int kernel, const __PSDomain &dom, int ngrids, void *const *grids,
   if (color >= 0 && !colorable(kernel))
     return fail(PS_ERR_UNSUPPORTED, "%s has no red/black form", sig.name);
   const int want = map_ngrids(sig, color);
+  if (ngrids > 64 || nscalars > 64)
+    return fail(PS_ERR_UNSUPPORTED, "%s: more than 64 grids or scalars", sig.name);
   if (ngrids != want || nscalars != sig.nscalars)
     return fail(PS_ERR_INVALID_ARGUMENT, "%s takes %d grids and %d scalars, got %d and %d",
                 sig.name, want, sig.nscalars, ngrids, nscalars);
@@ -734,7 +804,7 @@ bool map_from(int kernel, const __PSDomain &dom, int ngrids, void *const *grids,
     if (!g) return false;
     out->grids.push_back(g);
   }
-  if (color >= 0) out->grids.push_back(out->grids[0]);
+  if (color >= 0 && !sig.fn) out->grids.push_back(out->grids[0]);
   out->scalars.assign(scalars, scalars + nscalars);
   if (color >= 0 && !point_stencil(kernel)) {
     const int id = builtin_as_points(kernel, out->scalars);
@@ -888,6 +958,8 @@ int load_tuned(const char *path) {
 // trials while the run's signature has no tuned plan.  Returns the number of
 // iterations it ran (all of them unless an error occurs).
 bool run_tuning(const std::vector<Map *> &ms, int &iter) {
+  for (const Map *m : ms)
+    if (jit_kernel(m->kernel)) return true;  // one launch shape: nothing to tune
   const std::string key = run_key(ms);
   auto hit = g_tuned.find(key);
   if (hit != g_tuned.end()) {
@@ -1482,6 +1554,7 @@ void PSFinalize(void) {
   g_graphs.clear();
   for (Batch &b : g_batches) batch_release(b);
   g_batches.clear();
+  for (psg::JitKernel &k : rt->funcs) psg::jit_unload(&k);
   cudaFree(rt->dev_err);
   cudaFree(rt->partials);
   cudaFree(rt->ticket);
@@ -1614,25 +1687,14 @@ PSDomain3D PSDomain3DNew(PSIndex minx, PSIndex maxx, PSIndex miny, PSIndex maxy,
   return d;
 }
 
+static PSStencil map_varargs(const char *fn, void *kernel, int color, va_list vl);
+
 PSStencil __PSStencilMap(void *kernel, ...) {
-  if (!need_rt("PSStencilMap")) return -1;
-  const int k = (int)(intptr_t)kernel;
-  KernelSig sig;
-  if (!kernel_sig(k, &sig)) {
-    fail(PS_ERR_UNKNOWN_KERNEL, "unknown builtin stencil id %d", k);
-    return -1;
-  }
   va_list vl;
   va_start(vl, kernel);
-  __PSDomain dom = va_arg(vl, __PSDomain);
-  void *grids[16];
-  double sc[16];
-  for (int i = 0; i < sig.ngrids; ++i) grids[i] = va_arg(vl, void *);
-  for (int i = 0; i < sig.nscalars; ++i) sc[i] = va_arg(vl, double);
+  const PSStencil s = map_varargs("PSStencilMap", kernel, -1, vl);
   va_end(vl);
-  Map m;
-  if (!map_from(k, dom, sig.ngrids, grids, sig.nscalars, sc, &m)) return -1;
-  return add_map(std::move(m));
+  return s;
 }
 
 PSStencil PSStencilMapV(int kernel, const PSDomain3D *dom, int ngrids, void *const *grids,
@@ -1647,6 +1709,30 @@ PSStencil PSStencilMapV(int kernel, const PSDomain3D *dom, int ngrids, void *con
   return add_map(std::move(m));
 }
 
+// Reads a map's grid handles and scalars from C varargs.  Builtins take their
+// grids, then float scalars (promoted to double).  A compiled stencil
+// function takes them in its parameter order, each scalar with its declared
+// type's promotion (int, long, double).
+static void read_map_args(const KernelSig &sig, int ng, va_list vl, void **grids, double *sc) {
+  if (!sig.fn) {
+    for (int i = 0; i < ng; ++i) grids[i] = va_arg(vl, void *);
+    for (int i = 0; i < sig.nscalars; ++i) sc[i] = va_arg(vl, double);
+    return;
+  }
+  int gi = 0, si = 0;
+  for (const psg::JitParam &p : sig.fn->params) {
+    if (p.grid) {
+      grids[gi++] = va_arg(vl, void *);
+    } else if (p.type == psg::kInt) {
+      sc[si++] = (double)va_arg(vl, int);
+    } else if (p.type == psg::kLong) {
+      sc[si++] = (double)va_arg(vl, long);
+    } else {
+      sc[si++] = va_arg(vl, double);
+    }
+  }
+}
+
 // __PSStencilMap and its red/black forms: kernel, domain, grids, scalars.
 static PSStencil map_varargs(const char *fn, void *kernel, int color, va_list vl) {
   if (!need_rt(fn)) return -1;
@@ -1657,11 +1743,14 @@ static PSStencil map_varargs(const char *fn, void *kernel, int color, va_list vl
     return -1;
   }
   __PSDomain dom = va_arg(vl, __PSDomain);
-  void *grids[16];
-  double sc[16];
+  void *grids[64];
+  double sc[64];
   const int ng = map_ngrids(sig, color);
-  for (int i = 0; i < ng; ++i) grids[i] = va_arg(vl, void *);
-  for (int i = 0; i < sig.nscalars; ++i) sc[i] = va_arg(vl, double);
+  if (ng > 64 || sig.nscalars > 64) {
+    fail(PS_ERR_UNSUPPORTED, "%s: more than 64 grids or scalars", fn);
+    return -1;
+  }
+  read_map_args(sig, ng, vl, grids, sc);
   Map m;
   if (!map_from(k, dom, ng, grids, sig.nscalars, sc, &m, color)) return -1;
   return add_map(std::move(m));
@@ -1701,6 +1790,49 @@ PSStencil PSStencilMapColorV(int kernel, int color, const PSDomain3D *dom, int n
   Map m;
   if (!map_from(kernel, *dom, ngrids, grids, nscalars, scalars, &m, color)) return -1;
   return add_map(std::move(m));
+}
+
+int PSStencilFunctionCheck(const char *source, const char *name, char *log, size_t logsize) {
+  if (log && logsize) log[0] = '\0';
+  if (!source || !name || !name[0]) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSStencilFunctionCheck: NULL source or name");
+    return PS_ERR_INVALID_ARGUMENT;
+  }
+  psg::JitKernel k;
+  std::vector<char> image;
+  std::string why;
+  if (psg::jit_build(source, name, &k, &image, &why)) return PS_OK;
+  if (log && logsize) snprintf(log, logsize, "%s", why.c_str());
+  const bool missing = why.find("not available") != std::string::npos ||
+                       why.find("lacks") != std::string::npos;
+  return missing ? PS_ERR_UNSUPPORTED : PS_ERR_INVALID_ARGUMENT;
+}
+
+int PSStencilFunctionNew(const char *source, const char *name) {
+  if (!need_rt("PSStencilFunctionNew")) return -1;
+  if (!source || !name || !name[0]) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSStencilFunctionNew: NULL source or name");
+    return -1;
+  }
+  for (size_t i = 0; i < rt->funcs.size(); ++i)
+    if (rt->funcs[i].name == name && rt->funcs[i].source == source)
+      return kFuncBase + (int)i;
+  if ((int)rt->funcs.size() >= kMaxFunctions) {
+    fail(PS_ERR_OUT_OF_MEMORY, "more than %d stencil functions", kMaxFunctions);
+    return -1;
+  }
+  psg::JitKernel k;
+  std::string why;
+  if (!psg::jit_compile(source, name, &k, &why)) {
+    const bool missing = why.find("not available") != std::string::npos ||
+                         why.find("unavailable") != std::string::npos ||
+                         why.find("lacks") != std::string::npos;
+    fail(missing ? PS_ERR_UNSUPPORTED : PS_ERR_INVALID_ARGUMENT, "PSStencilFunctionNew: %s",
+         why.c_str());
+    return -1;
+  }
+  rt->funcs.push_back(std::move(k));
+  return kFuncBase + (int)rt->funcs.size() - 1;
 }
 
 int PSPointStencilNew(int boundary, int npoints, const int *offsets, const double *weights) {

@@ -57,6 +57,11 @@ MANUAL_TESTS = [
     "test_redblack",
     "test_redblack-periodic",
     "test_16",
+    "test_15",
+    "test_7-pt-type-mix",
+    "test_mixed-dim",
+    "test_mixed-dim2",
+    "test_mixed-dim3",
 ]
 
 DIFF_N, DIFF_COUNT = 21, 6
