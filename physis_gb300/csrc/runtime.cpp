@@ -806,7 +806,7 @@ bool map_from(int kernel, const __PSDomain &dom, int ngrids, void *const *grids,
   }
   if (color >= 0 && !sig.fn) out->grids.push_back(out->grids[0]);
   out->scalars.assign(scalars, scalars + nscalars);
-  if (color >= 0 && !point_stencil(kernel)) {
+  if (color >= 0 && (kernel == PS_KERNEL_SUM7 || kernel == PS_KERNEL_DIFFUSION7)) {
     const int id = builtin_as_points(kernel, out->scalars);
     if (id < 0) return false;
     out->kernel = id;
