@@ -723,6 +723,40 @@ P27 = [(x, y, z) for z in (-1, 0, 1) for (x, y) in
 P7 = [(0, 0, 0), (-1, 0, 0), (1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, -1), (0, 0, 1)]
 
 
+# The clamped diffusion stencil in the reference's stencil language, the way
+# examples/diffusion-benchmark/diffusion3d_physis.c:29-58 writes it
+# (neighbours replaced by the centre at the faces; scalars in map order
+# ce cw cn cs ct cb cc).
+FN_DIFFUSION = r"""
+void diffusion(const int x, const int y, const int z, PSGrid3DFloat g1, PSGrid3DFloat g2,
+               float ce, float cw, float cn, float cs, float ct, float cb, float cc) {
+  int nx = PSGridDim(g1, 0), ny = PSGridDim(g1, 1), nz = PSGridDim(g1, 2);
+  float c = PSGridGet(g1, x, y, z);
+  float w = (x == 0) ? c : PSGridGet(g1, x - 1, y, z);
+  float e = (x == nx - 1) ? c : PSGridGet(g1, x + 1, y, z);
+  float n = (y == 0) ? c : PSGridGet(g1, x, y - 1, z);
+  float s = (y == ny - 1) ? c : PSGridGet(g1, x, y + 1, z);
+  float b = (z == 0) ? c : PSGridGet(g1, x, y, z - 1);
+  float t = (z == nz - 1) ? c : PSGridGet(g1, x, y, z + 1);
+  PSGridEmit(g2, cc * c + cw * w + ce * e + cs * s + cn * n + cb * b + ct * t);
+}
+"""
+
+# The 27-point sum of tests/system_tests/test_cases/test_27-pt.c: the 27
+# terms added left to right in the test's order.
+FN27 = r"""
+void sum27(const int x, const int y, const int z, PSGrid3DFloat g1, PSGrid3DFloat g2) {
+  const int dx[9] = {0, 1, -1, 0, 1, -1, 0, 1, -1};
+  const int dy[9] = {0, 0, 0, 1, 1, 1, -1, -1, -1};
+  float v = PSGridGet(g1, x, y, z - 1);
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int i = (dz == -1) ? 1 : 0; i < 9; ++i)
+      v = v + PSGridGet(g1, x + dx[i], y + dy[i], z + dz);
+  PSGridEmit(g2, v);
+}
+"""
+
+
 def run_gpu_points(args, dist):
     """K sweeps of a point stencil over an N^3 float grid, ping-pong.
 
@@ -743,15 +777,24 @@ def run_gpu_points(args, dist):
     g2.copyin(init)
     dom = ps.full_domain(shape)
     if args.workload == "points27":
-        k = ps.point_stencil(P27, boundary=ps.BOUNDARY_PERIODIC)
-        label = f"27-point periodic sum fp32 {N}^3 (point stencil)"
-    else:
+        k = ps.point_stencil(P27, boundary=ps.BOUNDARY_NONE)
+        dom = ps.domain(1, N - 1, 1, N - 1, 1, N - 1)
+        label = f"27-point sum fp32 {N}^3 interior (point stencil)"
+    elif args.workload == "points7":
         k = ps.point_stencil(P7, weights=[0.4] + [0.1] * 6, boundary=ps.BOUNDARY_CLAMP)
         label = f"7-point clamped diffusion fp32 {N}^3 as a point stencil"
-    if args.warps or args.rows:
+    elif args.workload == "function27":
+        k = ps.stencil_function(FN27, "sum27")
+        dom = ps.domain(1, N - 1, 1, N - 1, 1, N - 1)
+        label = f"27-point sum fp32 {N}^3 interior (compiled stencil function)"
+    else:
+        k = ps.stencil_function(FN_DIFFUSION, "diffusion")
+        label = f"7-point clamped diffusion fp32 {N}^3 (compiled stencil function)"
+    if (args.warps or args.rows) and args.workload.startswith("points"):
         ps.set_launch_shape(k, warps=args.warps, rows=args.rows)
-    m1 = ps.stencil_map(k, dom, [g1, g2])
-    m2 = ps.stencil_map(k, dom, [g2, g1])
+    sc = list(COEF) if args.workload == "function7" else []
+    m1 = ps.stencil_map(k, dom, [g1, g2], sc)
+    m2 = ps.stencil_map(k, dom, [g2, g1], sc)
     K, W = args.steps, args.warmup
 
     def steps(n):
@@ -777,7 +820,7 @@ def run_gpu_points(args, dist):
     clk = clocks.stop()
     ps.check()
     ms_max = dist.reduce(ms, "MAX")
-    cells = float(N) ** 3
+    cells = float(N) ** 3 if not args.workload.endswith("27") else float(N - 2) ** 3
     value = dist.ws * cells * K / (ms_max / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
     achieved = cells * BYTES_PER_LUP / (ms / K / 1e3) / 1e9
@@ -788,7 +831,9 @@ def run_gpu_points(args, dist):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic uniform[0,1) seed 1 (SplitMix64)",
             "config": {"workload": label, "grid": [N, N, N],
-                       "launch_shape": list(ps.get_launch_shape(k)[:2]),
+                       "launch_shape": (list(ps.get_launch_shape(k)[:2])
+                                        if args.workload.startswith("points")
+                                        else "64x4 threads, one per (x, y), z-chunked"),
                        "l2": "inputs larger than L2" if N >= 256 else "fits L2"},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
@@ -818,7 +863,8 @@ def main():
     ap.add_argument("--batch-small", action="store_true",
                     help="batch workload with 48 small grids (launch-bound regime)")
     ap.add_argument("--workload", default="diffusion",
-                    choices=["diffusion", "himeno", "batch", "points27", "points7"],
+                    choices=["diffusion", "himeno", "batch", "points27", "points7",
+                             "function7", "function27"],
                     help="diffusion: 7-point 512^3 (the headline); himeno: "
                          "19-point Jacobi 257x257x513 with fused residual")
     args = ap.parse_args()
@@ -834,7 +880,7 @@ def main():
             run_gpu_himeno(args, dist)
         elif args.workload == "batch":
             run_gpu_batch(args, dist)
-        elif args.workload in ("points27", "points7"):
+        elif args.workload in ("points27", "points7", "function7", "function27"):
             run_gpu_points(args, dist)
         else:
             run_gpu(args, dist)

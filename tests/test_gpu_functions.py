@@ -362,3 +362,28 @@ def test_c_program_calls_a_function_through_varargs(rt, tmp_path):
     want = np.zeros_like(a)
     want[:, :, :7] = np.float32(0.5) * a[:, :, :7] + np.float32(3) * a[:, :, 1:]
     assert r.stdout == gio.dump_text(want)
+
+
+def test_benchmark_functions_match_oracle_and_builtin(rt, oracle):
+    # The stencil functions bench.py times: the 27-point sum against the
+    # oracle's point-stencil restatement, the clamped diffusion function
+    # against the DIFFUSION7 builtin, bit for bit.
+    import bench
+    rng = np.random.default_rng(9)
+    shape = (20, 30, 140)
+    nz, ny, nx = shape
+    src = rng.uniform(0, 1, size=shape).astype(np.float32)
+    inner = (1, nx - 1, 1, ny - 1, 1, nz - 1)
+    ref = np.zeros(shape, np.float32)
+    oracle.points(src, ref, inner, sc.P27)
+    a, b = _grid(src), _grid(np.zeros(shape, np.float32))
+    _run(ps.stencil_function(bench.FN27, "sum27"), ps.domain(*inner), [a, b])
+    assert np.array_equal(_bits(b.copyout()), _bits(ref))
+    coef = (0.1, 0.1, 0.1, 0.1, 0.1, 0.1, 0.4)
+    full = ps.full_domain(shape)
+    c = _grid(np.zeros(shape, np.float32))
+    _run(ps.stencil_function(bench.FN_DIFFUSION, "diffusion"), full, [a, b], coef)
+    _run(ps.PS_KERNEL_DIFFUSION7, full, [a, c], coef)
+    assert np.array_equal(_bits(b.copyout()), _bits(c.copyout()))
+    for g in (a, b, c):
+        g.free()
