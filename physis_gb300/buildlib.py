@@ -31,7 +31,26 @@ def nvcc():
 def common_flags():
     return ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
             "-Xcompiler", "-fvisibility=hidden", "-I", os.path.join(ROOT, "include"),
-            "-I", CSRC] + ARCH
+            "-I", CSRC, "-I", BUILD] + ARCH
+
+
+EMBEDDED = ["ps_arith.cuh", "points_body.cuh"]  # headers NVRTC compiles from memory
+
+
+def _write_embedded():
+    """BUILD/embedded_headers.inc: the headers jit.cpp hands to NVRTC, as
+    raw string literals (rewritten only when their text changes)."""
+    names = {"ps_arith.cuh": "kEmbedArith", "points_body.cuh": "kEmbedPointsBody"}
+    out = ["// Generated by buildlib.py from physis_gb300/csrc; do not edit.\n"]
+    for h in EMBEDDED:
+        text = open(os.path.join(CSRC, h)).read()
+        assert ")PSEMBED" not in text
+        out.append(f'static const char *{names[h]} = R"PSEMBED({text})PSEMBED";\n')
+    data = "".join(out)
+    path = os.path.join(BUILD, "embedded_headers.inc")
+    if not os.path.exists(path) or open(path).read() != data:
+        with open(path, "w") as f:
+            f.write(data)
 
 
 def _compile(src):
@@ -39,6 +58,7 @@ def _compile(src):
     path = os.path.join(CSRC, src)
     deps = [path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC)
                      if h.endswith((".h", ".cuh"))]
+    deps += [os.path.join(BUILD, "embedded_headers.inc")]
     deps += [os.path.join(ROOT, "include", "physis_gb300", h)
              for h in os.listdir(os.path.join(ROOT, "include", "physis_gb300"))]
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d)
@@ -55,6 +75,7 @@ def _compile(src):
 
 def build(verbose=False):
     os.makedirs(BUILD, exist_ok=True)
+    _write_embedded()
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(_compile, SOURCES))
     if os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(o)

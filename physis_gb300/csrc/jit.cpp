@@ -32,6 +32,11 @@
 #include <vector>
 
 #include "ps_internal.h"
+// kEmbedArith, kEmbedPointsBody: ps_arith.cuh and points_body.cuh as text
+// (written into the build directory by buildlib.py).
+#include "embedded_headers.inc"
+
+#include <map>
 
 namespace psg {
 namespace {
@@ -91,6 +96,8 @@ struct Driver {
   CUresult (*launch)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
                      unsigned, CUstream, void **, void **) = nullptr;
   CUresult (*unload)(CUmodule) = nullptr;
+  CUresult (*set_attr)(CUfunction, CUfunction_attribute, int) = nullptr;
+  CUresult (*occupancy)(int *, CUfunction, int, size_t) = nullptr;
 };
 Driver g_drv;
 
@@ -113,7 +120,11 @@ bool load_driver(std::string *err) {
   g_drv.get = reinterpret_cast<decltype(g_drv.get)>(sym("cuModuleGetFunction"));
   g_drv.launch = reinterpret_cast<decltype(g_drv.launch)>(sym("cuLaunchKernel"));
   g_drv.unload = reinterpret_cast<decltype(g_drv.unload)>(sym("cuModuleUnload"));
-  g_drv.ok = g_drv.load && g_drv.get && g_drv.launch && g_drv.unload;
+  g_drv.set_attr = reinterpret_cast<decltype(g_drv.set_attr)>(sym("cuFuncSetAttribute"));
+  g_drv.occupancy = reinterpret_cast<decltype(g_drv.occupancy)>(
+      sym("cuOccupancyMaxActiveBlocksPerMultiprocessor"));
+  g_drv.ok = g_drv.load && g_drv.get && g_drv.launch && g_drv.unload && g_drv.set_attr &&
+             g_drv.occupancy;
   if (!g_drv.ok) {
     cudaGetLastError();
     *err = "driver entry points for module loading are unavailable";
@@ -451,6 +462,115 @@ cudaError_t jit_launch(const JitKernel &k, const Box &dom, int color, const Grid
   }
   const CUresult r = g_drv.launch(static_cast<CUfunction>(k.func), gx, gy, (unsigned)gz, bx,
                                   by, 1, 0, static_cast<CUstream>(s), args.data(), nullptr);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorLaunchFailure;
+}
+
+namespace {
+
+const char *type_name(int type) {
+  switch (type) {
+    case kFloat: return "float";
+    case kDouble: return "double";
+    case kInt: return "int";
+    default: return "long long";
+  }
+}
+
+std::string key_string(const PtsJitKey &k) {
+  std::string s;
+  char buf[64];
+  snprintf(buf, sizeof(buf), "%d,%d,%d,%d,%d,%d,%d,%d;", k.type, k.ry, k.warps, k.n,
+           k.unit ? 1 : 0, k.w, k.nstage, k.plane_elems);
+  s += buf;
+  for (int i = 0; i < k.n; ++i) {
+    snprintf(buf, sizeof(buf), "%d:%d:%a;", k.off[i], k.lag[i], k.wt[i]);
+    s += buf;
+  }
+  return s;
+}
+
+std::string points_source(const PtsJitKey &k) {
+  std::string s = "#include \"points_body.cuh\"\nstruct GenSpec {\n"
+                  "  static constexpr bool kStatic = true;\n";
+  char buf[96];
+  snprintf(buf, sizeof(buf), "  static constexpr int kN = %d;\n", k.n);
+  s += buf;
+  s += "  static constexpr int kOff[kN] = {";
+  for (int i = 0; i < k.n; ++i) s += (i ? ", " : "") + std::to_string(k.off[i]);
+  s += "};\n  static constexpr int kLag[kN] = {";
+  for (int i = 0; i < k.n; ++i) s += (i ? ", " : "") + std::to_string(k.lag[i]);
+  s += "};\n  static constexpr double kWt[kN] = {";
+  for (int i = 0; i < k.n; ++i) {
+    snprintf(buf, sizeof(buf), "%s%a", i ? ", " : "", k.wt[i]);
+    s += buf;
+  }
+  s += "};\n";
+  snprintf(buf, sizeof(buf), "%d", k.w);
+  s += "  template <typename T> static __device__ __forceinline__ int w(const psg::PtsParams<T> &)"
+       " { return " + std::string(buf) + "; }\n";
+  s += "  template <typename T> static __device__ __forceinline__ int nstage("
+       "const psg::PtsParams<T> &) { return " + std::to_string(k.nstage) + "; }\n";
+  s += "  template <typename T> static __device__ __forceinline__ int plane_elems("
+       "const psg::PtsParams<T> &) { return " + std::to_string(k.plane_elems) + "; }\n};\n";
+  const std::string T = type_name(k.type);
+  s += "extern \"C\" __global__ void __launch_bounds__(" + std::to_string(32 * k.warps) +
+       ", 1) __ps_points(const __grid_constant__ psg::PtsParams<" + T + "> p) {\n"
+       "  extern __shared__ __align__(128) unsigned char smem[];\n"
+       "  psg::pts_body<" + T + ", " + std::to_string(k.ry) + ", " +
+       (k.unit ? "true" : "false") + ", GenSpec>(p, smem);\n}\n";
+  return s;
+}
+
+std::map<std::string, void *> g_points_jit;  // key -> CUfunction (nullptr: failed)
+
+}  // namespace
+
+void *jit_points_function(const PtsJitKey &k) {
+  const std::string key = key_string(k);
+  auto hit = g_points_jit.find(key);
+  if (hit != g_points_jit.end()) return hit->second;
+  std::string err;
+  void *fn = nullptr;
+  if (load_nvrtc(&err) && load_driver(&err)) {
+    const std::string program = points_source(k);
+    const char *hdr_src[] = {kEmbedArith, kEmbedPointsBody};
+    const char *hdr_name[] = {"ps_arith.cuh", "points_body.cuh"};
+    nvrtcProgram_t prog = nullptr;
+    if (g_nvrtc.create(&prog, program.c_str(), "points.cu", 2, hdr_src, hdr_name) == 0) {
+      const char *opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "--fmad=false"};
+      if (g_nvrtc.compile(prog, 3, opts) == 0) {
+        size_t n = 0;
+        g_nvrtc.cubin_size(prog, &n);
+        std::vector<char> image(n);
+        g_nvrtc.cubin(prog, image.data());
+        CUmodule mod = nullptr;
+        CUfunction f = nullptr;
+        if (g_drv.load(&mod, image.data()) == CUDA_SUCCESS) {
+          if (g_drv.get(&f, mod, "__ps_points") == CUDA_SUCCESS) fn = f;
+          else g_drv.unload(mod);
+        }
+      }
+      g_nvrtc.destroy(&prog);
+    }
+  }
+  g_points_jit[key] = fn;
+  return fn;
+}
+
+bool jit_prepare(void *fn, int threads, size_t smem, int *occ) {
+  CUfunction f = static_cast<CUfunction>(fn);
+  if (g_drv.set_attr(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem) !=
+      CUDA_SUCCESS)
+    return false;
+  return g_drv.occupancy(occ, f, threads, smem) == CUDA_SUCCESS;
+}
+
+cudaError_t jit_launch_raw(void *fn, int grid, dim3 block, size_t smem, cudaStream_t s,
+                           const void *params) {
+  void *args[1] = {const_cast<void *>(params)};
+  const CUresult r = g_drv.launch(static_cast<CUfunction>(fn), (unsigned)grid, 1, 1, block.x,
+                                  block.y, block.z, (unsigned)smem, static_cast<CUstream>(s),
+                                  args, nullptr);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorLaunchFailure;
 }
 

@@ -1,0 +1,201 @@
+// The point-list stencil sweep, written once for two builds:
+//  * points.cu compiles it with a run-time point table (PtsTableSpec): one
+//    kernel serves every registered stencil;
+//  * jit.cpp compiles it with NVRTC for one stencil at a time, with a
+//    generated spec whose offsets, plane lags, weights and tile geometry are
+//    compile-time constants (the point loop unrolls into shared-memory loads
+//    at immediate offsets, and loads that two rows of a thread share are
+//    issued once).
+// No header dependencies beyond ps_arith.cuh, so NVRTC can compile it from
+// memory.  See points.cu for the design.
+#pragma once
+
+#include "ps_arith.cuh"
+
+namespace psg {
+
+constexpr int kPtsTX = 128;       // tile width in cells
+constexpr int kPtsVX = 4;         // columns per lane (lane + 32*j)
+constexpr int kPtsPrefetch = 2;   // planes in flight ahead of the newest needed plane
+constexpr int kPtsMaxPoints = 64;
+// Point table in shared memory (run-time spec only): offsets, lags, weights.
+constexpr int kPtsTableBytes = kPtsMaxPoints * (4 + 4 + 8);
+enum { kPtsNone = 0, kPtsPeriodic = 1, kPtsClamp = 2 };
+
+template <typename T>
+struct PtsParams {
+  const T *in;
+  T *out;            // may equal in (red/black)
+  long long row;     // pitch in elements
+  long long plane;   // elements per z-plane
+  int nx, ny, nz;
+  int dmin0, dmin1, dmin2, dmax0, dmax1, dmax2;
+  int boundary;      // kPtsNone / kPtsPeriodic / kPtsClamp
+  int color;         // -1 every cell, 0 red, 1 black
+  int n;             // points
+  int ryl, rzl, rzh;
+  int lp, w, rows_h, nstage, plane_elems;
+  int xbase, tiles_x, tiles, zlen;
+  long long items;
+  int off[kPtsMaxPoints];  // shared offset of point i relative to the cell
+  int lag[kPtsMaxPoints];  // rzl + dz_i: the point's plane relative to z - rzl
+  T wt[kPtsMaxPoints];
+};
+
+// Grid index of coordinate i on an axis of n cells.  Periodic: i mod n, which
+// equals the reference's (i + n) % n for every i >= -n (the host admits only
+// offsets with |d| <= n, so every read that is used has i >= -n; halo cells
+// that are never read may lie further out and still land inside the grid).
+// Clamp, and the never-read halo of boundary "none": the nearest face.
+__device__ __forceinline__ int pts_map_axis(int i, int n, int boundary) {
+  if (boundary == kPtsPeriodic) {
+    const int m = i % n;
+    return m < 0 ? m + n : m;
+  }
+  return min(max(i, 0), n - 1);
+}
+
+// Issues the copies of global plane zg (tile origin x0, y0) into `dst`:
+// 16-byte copies for aligned chunks inside the grid, element copies through
+// the boundary map for chunks that cross an edge.
+template <typename T>
+__device__ __forceinline__ void pts_load_plane(const PtsParams<T> &p, T *dst, int zg, int x0,
+                                               int y0) {
+  constexpr int VEC = 16 / (int)sizeof(T);
+  const T *src_plane = p.in + (long long)pts_map_axis(zg, p.nz, p.boundary) * p.plane;
+  const int nchunk = p.w / VEC;
+  const int xs = x0 - p.lp;
+  for (int r = threadIdx.y; r < p.rows_h; r += blockDim.y) {
+    const T *src =
+        src_plane + (long long)pts_map_axis(y0 - p.ryl + r, p.ny, p.boundary) * p.row;
+    T *d = dst + r * p.w;
+    for (int c = threadIdx.x; c < nchunk; c += 32) {
+      const int x = xs + c * VEC;
+      if (x >= 0 && x + VEC <= p.nx) {
+        cp_async16(d + c * VEC, src + x);
+      } else {
+#pragma unroll
+        for (int i = 0; i < VEC; ++i)
+          cp_async_small<sizeof(T)>(d + c * VEC + i, src + pts_map_axis(x + i, p.nx, p.boundary));
+      }
+    }
+  }
+}
+
+// The run-time spec: the point table travels in the kernel parameters and is
+// copied to shared memory; the tile geometry comes from the parameters.
+struct PtsTableSpec {
+  static constexpr bool kStatic = false;
+  template <typename T>
+  static __device__ __forceinline__ int w(const PtsParams<T> &p) { return p.w; }
+  template <typename T>
+  static __device__ __forceinline__ int nstage(const PtsParams<T> &p) { return p.nstage; }
+  template <typename T>
+  static __device__ __forceinline__ int plane_elems(const PtsParams<T> &p) {
+    return p.plane_elems;
+  }
+};
+
+// acc[r][j] (+)= w * src[r*W + 32*j]; `first` starts the sum.
+template <typename T, int RY, bool UNIT>
+__device__ __forceinline__ void pts_term(T (&acc)[RY][kPtsVX], const T *src, int W, T wk,
+                                         bool first) {
+  typedef RN<T> R;
+#pragma unroll
+  for (int r = 0; r < RY; ++r)
+#pragma unroll
+    for (int j = 0; j < kPtsVX; ++j) {
+      const T v = src[r * W + 32 * j];
+      const T t = UNIT ? v : R::mul(wk, v);
+      acc[r][j] = first ? t : R::add(acc[r][j], t);
+    }
+}
+
+// The sweep: persistent (z-chunk, tile) items, a cp.async ring of planes,
+// the points summed in order, masked stores.  `smem` is the dynamic shared
+// memory (kPtsTableBytes of table, then the ring).
+template <typename T, int RY, bool UNIT, class S>
+__device__ __forceinline__ void pts_body(const PtsParams<T> &p, unsigned char *smem) {
+  int *s_off = reinterpret_cast<int *>(smem);
+  int *s_lag = s_off + kPtsMaxPoints;
+  T *s_w = reinterpret_cast<T *>(smem + kPtsMaxPoints * 8);
+  T *ring = reinterpret_cast<T *>(smem + kPtsTableBytes);
+  const int W = S::w(p), NST = S::nstage(p), PE = S::plane_elems(p);
+
+  const int lane = threadIdx.x, warp = threadIdx.y;
+  const int tid = warp * 32 + lane;
+  if (!S::kStatic) {
+    for (int i = tid; i < p.n; i += blockDim.x * blockDim.y) {
+      s_off[i] = p.off[i];
+      s_lag[i] = p.lag[i];
+      s_w[i] = p.wt[i];
+    }
+    __syncthreads();
+  }
+
+  const int TY = blockDim.y * RY;
+  const int pre = NST - 1;  // planes issued before the first compute step
+  const int cell0 = warp * RY * W + lane;
+
+  for (long long item = blockIdx.x; item < p.items; item += gridDim.x) {
+    const int chunk = (int)(item / p.tiles);
+    const int tile = (int)(item - (long long)chunk * p.tiles);
+    const int zs = p.dmin2 + chunk * p.zlen;
+    const int ze = min(zs + p.zlen, p.dmax2);
+    const int x0 = p.xbase + (tile % p.tiles_x) * kPtsTX;
+    const int y0 = p.dmin1 + (tile / p.tiles_x) * TY;
+    const int nplanes = ze - zs + p.rzl + p.rzh;  // planes zs-rzl .. ze+rzh-1
+
+    int ld = 0;  // ring slot of the next plane to issue
+    for (int q = 0; q < pre; ++q) {
+      if (q < nplanes) pts_load_plane(p, ring + ld * PE, zs - p.rzl + q, x0, y0);
+      cp_async_commit();
+      if (++ld == NST) ld = 0;
+    }
+    int cs = 0;  // ring slot of plane z - rzl
+    for (int z = zs; z < ze; ++z) {
+      const int q = z - zs + pre;
+      if (q < nplanes) pts_load_plane(p, ring + ld * PE, zs - p.rzl + q, x0, y0);
+      cp_async_commit();
+      if (++ld == NST) ld = 0;
+      cp_async_wait<kPtsPrefetch>();  // planes up to z + rzh have landed
+      __syncthreads();
+
+      T acc[RY][kPtsVX];
+      if constexpr (S::kStatic) {
+#pragma unroll
+        for (int k = 0; k < S::kN; ++k) {
+          int s = cs + S::kLag[k];
+          if (s >= NST) s -= NST;
+          pts_term<T, RY, UNIT>(acc, ring + s * PE + cell0 + S::kOff[k], W, (T)S::kWt[k],
+                                k == 0);
+        }
+      } else {
+        for (int k = 0; k < p.n; ++k) {
+          int s = cs + s_lag[k];
+          if (s >= NST) s -= NST;
+          pts_term<T, RY, UNIT>(acc, ring + s * PE + cell0 + s_off[k], W, s_w[k], k == 0);
+        }
+      }
+
+#pragma unroll
+      for (int r = 0; r < RY; ++r) {
+        const int y = y0 + warp * RY + r;
+        if (y >= p.dmax1) continue;
+        T *dst = p.out + (long long)z * p.plane + (long long)y * p.row;
+#pragma unroll
+        for (int j = 0; j < kPtsVX; ++j) {
+          const int x = x0 + lane + 32 * j;
+          const bool in_dom = x >= p.dmin0 && x < p.dmax0;
+          const bool colored = p.color < 0 || ((x + y + z + p.color) & 1) == 0;
+          if (in_dom && colored) dst[x] = acc[r][j];
+        }
+      }
+      if (++cs == NST) cs = 0;
+      __syncthreads();  // the slot of plane z - rzl is refilled next step
+    }
+    cp_async_wait<0>();  // only empty groups can remain
+  }
+}
+
+}  // namespace psg

@@ -8,6 +8,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "ps_arith.cuh"
+
 namespace psg {
 
 // Error bits written into the runtime's device error word.
@@ -21,10 +23,6 @@ enum : int {
 // sleep after the first few, so the limit bounds a wait to well under a
 // second of wall time.
 constexpr uint32_t kWaitLimit = 1u << 22;
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
 
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
@@ -87,41 +85,6 @@ __device__ __forceinline__ void prefetch_tmap(const CUtensorMap *map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map))
                : "memory");
 }
-
-// Round-to-nearest arithmetic that is never fused into an FMA.
-template <typename T>
-struct RN {
-  static __device__ __forceinline__ T add(T a, T b) { return a + b; }
-  static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
-  static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
-};
-template <>
-struct RN<float> {
-  static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
-  static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
-  static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
-};
-template <>
-struct RN<double> {
-  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
-  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
-  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
-};
-// Integer grids wrap modulo 2^32 / 2^64 like the REF target's C arithmetic
-// on two's-complement hosts; compute in unsigned to keep that defined.
-template <>
-struct RN<int> {
-  static __device__ __forceinline__ int add(int a, int b) { return (int)((unsigned)a + (unsigned)b); }
-  static __device__ __forceinline__ int sub(int a, int b) { return (int)((unsigned)a - (unsigned)b); }
-  static __device__ __forceinline__ int mul(int a, int b) { return (int)((unsigned)a * (unsigned)b); }
-};
-template <>
-struct RN<long long> {
-  typedef unsigned long long U;
-  static __device__ __forceinline__ long long add(long long a, long long b) { return (long long)((U)a + (U)b); }
-  static __device__ __forceinline__ long long sub(long long a, long long b) { return (long long)((U)a - (U)b); }
-  static __device__ __forceinline__ long long mul(long long a, long long b) { return (long long)((U)a * (U)b); }
-};
 
 // 16-byte vector of T held as VEC scalars.
 template <typename T>

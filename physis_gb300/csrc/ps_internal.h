@@ -161,6 +161,26 @@ void jit_unload(JitKernel *k);
 cudaError_t jit_launch(const JitKernel &k, const Box &dom, int color, const GridView *grids,
                        const double *scalars, int sm_count, cudaStream_t s);
 
+// Point stencils compiled per stencil (jit.cpp compiles points_body.cuh with
+// the table below as constants).  The key is everything the generated code
+// depends on; the kernel takes one PtsParams<T> by value.
+struct PtsJitKey {
+  int type;                  // ElemType
+  int ry, warps, n;
+  bool unit;
+  int w, nstage, plane_elems;
+  int off[kMaxPoints], lag[kMaxPoints];
+  double wt[kMaxPoints];
+};
+// The compiled kernel (cached; nullptr if NVRTC is missing or compiling
+// failed, after which the table kernel is used).
+void *jit_points_function(const PtsJitKey &k);
+// Sets the kernel's dynamic shared memory limit and returns its occupancy.
+bool jit_prepare(void *fn, int threads, size_t smem, int *occ);
+// Launches a kernel whose one parameter is the struct at `params`.
+cudaError_t jit_launch_raw(void *fn, int grid, dim3 block, size_t smem, cudaStream_t s,
+                           const void *params);
+
 // ---- Reductions (reduce.cu) ----------------------------------------------
 // Reduces every element of g with op.  The 8-byte result is written to
 // *result: FP64 for float and double grids, int64 for int (wrapped to 32

@@ -29,6 +29,23 @@ def rt():
     ps.clear_error()
 
 
+@pytest.fixture(params=["compiled", "table"])
+def kernel_form(request):
+    """Runs a test with the per-stencil compiled kernel (the default) and
+    with the run-time table kernel (PS_POINTS_JIT=0)."""
+    import os
+    old = os.environ.get("PS_POINTS_JIT")
+    if request.param == "table":
+        os.environ["PS_POINTS_JIT"] = "0"
+    else:
+        os.environ.pop("PS_POINTS_JIT", None)
+    yield request.param
+    if old is None:
+        os.environ.pop("PS_POINTS_JIT", None)
+    else:
+        os.environ["PS_POINTS_JIT"] = old
+
+
 def _bits(a):
     return a.view({1: np.uint8, 4: np.uint32, 8: np.uint64}[a.dtype.itemsize])
 
@@ -46,7 +63,7 @@ class _G:
 
 
 @pytest.mark.parametrize("name", sorted(sc.CASES))
-def test_point_system_tests(rt, name):
+def test_point_system_tests(rt, kernel_form, name):
     case = dict(sc.CASES[name])
     dom = _dom(sc.domain(case))
     k = ps.point_stencil(case["points"], boundary=case["boundary"])
@@ -134,8 +151,8 @@ CASES = [
 
 
 @pytest.mark.parametrize("seed,shape,dtype,boundary,npts,radius,weighted,shrink", CASES)
-def test_random_point_stencils_bit_exact(rt, oracle, seed, shape, dtype, boundary, npts,
-                                         radius, weighted, shrink):
+def test_random_point_stencils_bit_exact(rt, oracle, kernel_form, seed, shape, dtype,
+                                         boundary, npts, radius, weighted, shrink):
     rng = np.random.default_rng(seed)
     integer = np.issubdtype(dtype, np.integer)
     pts, w = _random_stencil(rng, radius, npts, boundary, shape, weighted, integer)
@@ -156,7 +173,7 @@ def test_random_point_stencils_bit_exact(rt, oracle, seed, shape, dtype, boundar
 
 
 @pytest.mark.parametrize("warps,rows", [(8, 2), (8, 1), (4, 2), (16, 1), (2, 2), (1, 1)])
-def test_point_launch_shapes_do_not_change_results(rt, oracle, warps, rows):
+def test_point_launch_shapes_do_not_change_results(rt, oracle, kernel_form, warps, rows):
     rng = np.random.default_rng(42)
     shape = (11, 45, 270)
     pts = sc.P27
@@ -195,8 +212,8 @@ RB_CASES = [
 
 @pytest.mark.parametrize("seed,shape,dtype,boundary,pts,weighted,halo", RB_CASES)
 @pytest.mark.parametrize("color", [0, 1, 2])
-def test_red_black_bit_exact(rt, oracle, seed, shape, dtype, boundary, pts, weighted,
-                             halo, color):
+def test_red_black_bit_exact(rt, oracle, kernel_form, seed, shape, dtype, boundary, pts,
+                             weighted, halo, color):
     rng = np.random.default_rng(seed)
     integer = np.issubdtype(dtype, np.integer)
     w = None
