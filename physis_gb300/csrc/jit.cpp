@@ -480,7 +480,7 @@ std::string key_string(const PtsJitKey &k) {
   std::string s;
   char buf[64];
   snprintf(buf, sizeof(buf), "%d,%d,%d,%d,%d,%d,%d,%d;", k.type, k.ry, k.warps, k.n,
-           k.unit ? 1 : 0, k.w, k.nstage, k.plane_elems);
+           k.unit ? 1 : 0, k.w, k.nstage, k.pstride);
   s += buf;
   for (int i = 0; i < k.n; ++i) {
     snprintf(buf, sizeof(buf), "%d:%d:%a;", k.off[i], k.lag[i], k.wt[i]);
@@ -510,14 +510,15 @@ std::string points_source(const PtsJitKey &k) {
        " { return " + std::string(buf) + "; }\n";
   s += "  template <typename T> static __device__ __forceinline__ int nstage("
        "const psg::PtsParams<T> &) { return " + std::to_string(k.nstage) + "; }\n";
-  s += "  template <typename T> static __device__ __forceinline__ int plane_elems("
-       "const psg::PtsParams<T> &) { return " + std::to_string(k.plane_elems) + "; }\n};\n";
+  s += "  template <typename T> static __device__ __forceinline__ int pstride("
+       "const psg::PtsParams<T> &) { return " + std::to_string(k.pstride) + "; }\n};\n";
   const std::string T = type_name(k.type);
   s += "extern \"C\" __global__ void __launch_bounds__(" + std::to_string(32 * k.warps) +
-       ", 1) __ps_points(const __grid_constant__ psg::PtsParams<" + T + "> p) {\n"
+       ", 1) __ps_points(const __grid_constant__ psg::PtsParams<" + T + "> p, "
+       "const __grid_constant__ psg::PtsTmap tm) {\n"
        "  extern __shared__ __align__(128) unsigned char smem[];\n"
        "  psg::pts_body<" + T + ", " + std::to_string(k.ry) + ", " +
-       (k.unit ? "true" : "false") + ", GenSpec>(p, smem);\n}\n";
+       (k.unit ? "true" : "false") + ", GenSpec>(p, &tm, smem);\n}\n";
   return s;
 }
 
@@ -566,8 +567,7 @@ bool jit_prepare(void *fn, int threads, size_t smem, int *occ) {
 }
 
 cudaError_t jit_launch_raw(void *fn, int grid, dim3 block, size_t smem, cudaStream_t s,
-                           const void *params) {
-  void *args[1] = {const_cast<void *>(params)};
+                           void **args) {
   const CUresult r = g_drv.launch(static_cast<CUfunction>(fn), (unsigned)grid, 1, 1, block.x,
                                   block.y, block.z, (unsigned)smem, static_cast<CUstream>(s),
                                   args, nullptr);

@@ -48,9 +48,10 @@ namespace psg {
 namespace {
 
 template <typename T, int RY, bool UNIT>
-__global__ void __launch_bounds__(512, 1) pts_kernel(const __grid_constant__ PtsParams<T> p) {
+__global__ void __launch_bounds__(512, 1)
+pts_kernel(const __grid_constant__ PtsParams<T> p, const __grid_constant__ PtsTmap tm) {
   extern __shared__ __align__(128) unsigned char smem[];
-  pts_body<T, RY, UNIT, PtsTableSpec>(p, smem);
+  pts_body<T, RY, UNIT, PtsTableSpec>(p, &tm, smem);
 }
 
 // Offsets' extent per axis: lo <= 0 <= hi.
@@ -97,6 +98,9 @@ void fill_params(const PointsArgs &a, int warps, int ry, PtsParams<T> *pp) {
   p.rows_h = TY + p.ryl + hi[1];
   p.nstage = p.rzl + p.rzh + 1 + kPtsPrefetch;
   p.plane_elems = p.rows_h * p.w;
+  p.pstride = (int)(((size_t)p.plane_elems * sizeof(T) + 127) / 128 * 128 / sizeof(T));
+  p.use_tma = a.has_tmap ? 1 : 0;
+  p.err = a.err;
   for (int i = 0; i < a.n; ++i) {
     p.off[i] = (p.ryl + a.d[i][1]) * p.w + p.lp + a.d[i][0];
     p.lag[i] = p.rzl + a.d[i][2];
@@ -121,7 +125,7 @@ int schedule(PtsParams<T> *p, int occ, int sm_count) {
 
 template <typename T>
 size_t smem_for(const PtsParams<T> &p) {
-  return (size_t)kPtsTableBytes + (size_t)p.nstage * p.plane_elems * sizeof(T);
+  return 128 + (size_t)kPtsRingOffset + (size_t)p.nstage * p.pstride * sizeof(T);
 }
 
 bool jit_enabled() {
@@ -134,6 +138,10 @@ cudaError_t launch_t(const PointsArgs &a, int warps, int sm_count, cudaStream_t 
   PtsParams<T> p;
   fill_params<T>(a, warps, RY, &p);
   const size_t smem = smem_for(p);
+  PtsTmap tm;
+  memset(&tm, 0, sizeof(tm));
+  static_assert(sizeof(PtsTmap) == sizeof(CUtensorMap), "tensor map layout");
+  if (a.has_tmap) memcpy(&tm, &a.tmap, sizeof(tm));
   if (jit_enabled()) {
     // The stencil compiled with its table as constants (cached per stencil,
     // type and tile shape); on any failure the table kernel below runs.
@@ -146,7 +154,7 @@ cudaError_t launch_t(const PointsArgs &a, int warps, int sm_count, cudaStream_t 
     key.unit = UNIT;
     key.w = p.w;
     key.nstage = p.nstage;
-    key.plane_elems = p.plane_elems;
+    key.pstride = p.pstride;
     for (int i = 0; i < a.n; ++i) {
       key.off[i] = p.off[i];
       key.lag[i] = p.lag[i];
@@ -156,7 +164,8 @@ cudaError_t launch_t(const PointsArgs &a, int warps, int sm_count, cudaStream_t 
     int occ = 0;
     if (fn && jit_prepare(fn, 32 * warps, smem, &occ) && occ >= 1) {
       const int grid = schedule(&p, occ, sm_count);
-      return jit_launch_raw(fn, grid, dim3(32, warps, 1), smem, s, &p);
+      void *args[2] = {&p, &tm};
+      return jit_launch_raw(fn, grid, dim3(32, warps, 1), smem, s, args);
     }
   }
   auto kern = pts_kernel<T, RY, UNIT>;
@@ -168,7 +177,7 @@ cudaError_t launch_t(const PointsArgs &a, int warps, int sm_count, cudaStream_t 
   if (e != cudaSuccess) return e;
   if (occ < 1) return cudaErrorInvalidConfiguration;
   const int grid = schedule(&p, occ, sm_count);
-  kern<<<grid, dim3(32, warps, 1), smem, s>>>(p);
+  kern<<<grid, dim3(32, warps, 1), smem, s>>>(p, tm);
   return cudaGetLastError();
 }
 
@@ -185,15 +194,21 @@ cudaError_t launch_type(const PointsArgs &a, const MarchConfig &cfg, int sm_coun
 
 }  // namespace
 
-size_t points_smem_bytes(const PointsArgs &a, const MarchConfig &cfg) {
-  const int esz = a.in.esz;
-  const int vec = 16 / esz;
+void points_box(const PointsArgs &a, const MarchConfig &cfg, int *w, int *h) {
+  const int vec = 16 / a.in.esz;
   int lo[3], hi[3];
   extents(a, lo, hi);
-  const int w = (-lo[0] + vec - 1) / vec * vec + kPtsTX + (hi[0] + vec - 1) / vec * vec;
-  const int rows_h = cfg.warps * (cfg.rows >= 2 ? 2 : 1) - lo[1] + hi[1];
+  *w = (-lo[0] + vec - 1) / vec * vec + kPtsTX + (hi[0] + vec - 1) / vec * vec;
+  *h = cfg.warps * (cfg.rows >= 2 ? 2 : 1) - lo[1] + hi[1];
+}
+
+size_t points_smem_bytes(const PointsArgs &a, const MarchConfig &cfg) {
+  int lo[3], hi[3], w, h;
+  extents(a, lo, hi);
+  points_box(a, cfg, &w, &h);
   const int nstage = -lo[2] + hi[2] + 1 + kPtsPrefetch;
-  return (size_t)kPtsTableBytes + (size_t)nstage * rows_h * w * esz;
+  const size_t stage = ((size_t)w * h * a.in.esz + 127) / 128 * 128;
+  return 128 + (size_t)kPtsRingOffset + (size_t)nstage * stage;
 }
 
 cudaError_t launch_points(const PointsArgs &a, const MarchConfig &cfg, int sm_count,

@@ -18,8 +18,15 @@ constexpr int kPtsTX = 128;       // tile width in cells
 constexpr int kPtsVX = 4;         // columns per lane (lane + 32*j)
 constexpr int kPtsPrefetch = 2;   // planes in flight ahead of the newest needed plane
 constexpr int kPtsMaxPoints = 64;
-// Point table in shared memory (run-time spec only): offsets, lags, weights.
+// Shared memory: point table (run-time spec only: offsets, lags, weights),
+// then the ring's mbarriers, then the ring (128-byte aligned stages).
 constexpr int kPtsTableBytes = kPtsMaxPoints * (4 + 4 + 8);
+constexpr int kPtsMaxStages = 16;
+constexpr int kPtsRingOffset = kPtsTableBytes + 8 * kPtsMaxStages;
+// Opaque TMA descriptor (the layout of CUtensorMap: 128 bytes, 64-aligned).
+struct alignas(64) PtsTmap {
+  unsigned long long opaque[16];
+};
 enum { kPtsNone = 0, kPtsPeriodic = 1, kPtsClamp = 2 };
 
 template <typename T>
@@ -35,8 +42,11 @@ struct PtsParams {
   int n;             // points
   int ryl, rzl, rzh;
   int lp, w, rows_h, nstage, plane_elems;
+  int pstride;       // ring stage stride in elements (128-byte multiple)
+  int use_tma;       // 1: the tmap parameter maps `in` with box {w, rows_h, 1}
   int xbase, tiles_x, tiles, zlen;
   long long items;
+  int *err;          // device error word (bounded waits that give up)
   int off[kPtsMaxPoints];  // shared offset of point i relative to the cell
   int lag[kPtsMaxPoints];  // rzl + dz_i: the point's plane relative to z - rzl
   T wt[kPtsMaxPoints];
@@ -91,9 +101,7 @@ struct PtsTableSpec {
   template <typename T>
   static __device__ __forceinline__ int nstage(const PtsParams<T> &p) { return p.nstage; }
   template <typename T>
-  static __device__ __forceinline__ int plane_elems(const PtsParams<T> &p) {
-    return p.plane_elems;
-  }
+  static __device__ __forceinline__ int pstride(const PtsParams<T> &p) { return p.pstride; }
 };
 
 // acc[r][j] (+)= w * src[r*W + 32*j]; `first` starts the sum.
@@ -111,33 +119,47 @@ __device__ __forceinline__ void pts_term(T (&acc)[RY][kPtsVX], const T *src, int
     }
 }
 
-// The sweep: persistent (z-chunk, tile) items, a cp.async ring of planes,
-// the points summed in order, masked stores.  `smem` is the dynamic shared
-// memory (kPtsTableBytes of table, then the ring).
+// The sweep: persistent (z-chunk, tile) items, a ring of planes, the points
+// summed in order, masked stores.  A tile whose box lies inside the grid --
+// or any tile when the boundary rule is "none", whose out-of-grid halo is
+// never read -- arrives by one TMA box load per plane (mbarrier per stage);
+// the edge tiles of periodic and clamped stencils use cp.async through the
+// boundary map (one commit group per plane).  `smem_raw` is the dynamic
+// shared memory, `tmap` the TMA descriptor of `in` (used if p.use_tma).
 template <typename T, int RY, bool UNIT, class S>
-__device__ __forceinline__ void pts_body(const PtsParams<T> &p, unsigned char *smem) {
+__device__ __forceinline__ void pts_body(const PtsParams<T> &p, const void *tmap,
+                                         unsigned char *smem_raw) {
+  unsigned char *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
   int *s_off = reinterpret_cast<int *>(smem);
   int *s_lag = s_off + kPtsMaxPoints;
   T *s_w = reinterpret_cast<T *>(smem + kPtsMaxPoints * 8);
-  T *ring = reinterpret_cast<T *>(smem + kPtsTableBytes);
-  const int W = S::w(p), NST = S::nstage(p), PE = S::plane_elems(p);
+  unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + kPtsTableBytes);
+  T *ring = reinterpret_cast<T *>(smem + kPtsRingOffset);
+  const int W = S::w(p), NST = S::nstage(p), PS = S::pstride(p);
 
   const int lane = threadIdx.x, warp = threadIdx.y;
   const int tid = warp * 32 + lane;
+  if (tid == 0) {
+    for (int s = 0; s < NST; ++s) mbar_init(&bars[s], 1);
+    fence_barrier_init();
+  }
   if (!S::kStatic) {
     for (int i = tid; i < p.n; i += blockDim.x * blockDim.y) {
       s_off[i] = p.off[i];
       s_lag[i] = p.lag[i];
       s_w[i] = p.wt[i];
     }
-    __syncthreads();
   }
+  __syncthreads();
 
   const int TY = blockDim.y * RY;
   const int pre = NST - 1;  // planes issued before the first compute step
   const int cell0 = warp * RY * W + lane;
+  const unsigned tma_bytes = (unsigned)(p.plane_elems * (int)sizeof(T));
+  unsigned phase = 0;  // bit s: parity of the next completion of stage s
+  bool ok = true;
 
-  for (long long item = blockIdx.x; item < p.items; item += gridDim.x) {
+  for (long long item = blockIdx.x; item < p.items && ok; item += gridDim.x) {
     const int chunk = (int)(item / p.tiles);
     const int tile = (int)(item - (long long)chunk * p.tiles);
     const int zs = p.dmin2 + chunk * p.zlen;
@@ -145,21 +167,57 @@ __device__ __forceinline__ void pts_body(const PtsParams<T> &p, unsigned char *s
     const int x0 = p.xbase + (tile % p.tiles_x) * kPtsTX;
     const int y0 = p.dmin1 + (tile / p.tiles_x) * TY;
     const int nplanes = ze - zs + p.rzl + p.rzh;  // planes zs-rzl .. ze+rzh-1
-
-    int ld = 0;  // ring slot of the next plane to issue
-    for (int q = 0; q < pre; ++q) {
-      if (q < nplanes) pts_load_plane(p, ring + ld * PE, zs - p.rzl + q, x0, y0);
-      cp_async_commit();
-      if (++ld == NST) ld = 0;
+    const bool tma =
+        p.use_tma && (p.boundary == kPtsNone ||
+                      (x0 - p.lp >= 0 && x0 - p.lp + W <= p.nx && y0 - p.ryl >= 0 &&
+                       y0 - p.ryl + p.rows_h <= p.ny));
+    // store masks: columns j in the domain, rows r in the domain
+    unsigned colmask = 0, rowmask = 0;
+#pragma unroll
+    for (int j = 0; j < kPtsVX; ++j) {
+      const int x = x0 + lane + 32 * j;
+      if (x >= p.dmin0 && x < p.dmax0) colmask |= 1u << j;
     }
-    int cs = 0;  // ring slot of plane z - rzl
-    for (int z = zs; z < ze; ++z) {
-      const int q = z - zs + pre;
-      if (q < nplanes) pts_load_plane(p, ring + ld * PE, zs - p.rzl + q, x0, y0);
-      cp_async_commit();
+#pragma unroll
+    for (int r = 0; r < RY; ++r)
+      if (y0 + warp * RY + r < p.dmax1) rowmask |= 1u << r;
+    const int xpar = (x0 + lane) & 1;  // parity of every column of this lane
+    T *out0 = p.out + (long long)(y0 + warp * RY) * p.row + x0 + lane;
+
+    int ld = 0, issued = 0, waited = 0, wslot = 0;
+    auto issue = [&](int q) {
+      if (tma) {
+        if (tid == 0) {
+          mbar_arrive_expect_tx(&bars[ld], tma_bytes);
+          tma_load_3d(ring + ld * PS, tmap, x0 - p.lp, y0 - p.ryl,
+                      pts_map_axis(zs - p.rzl + q, p.nz, p.boundary), &bars[ld]);
+        }
+        ++issued;
+      } else {
+        if (q < nplanes) pts_load_plane(p, ring + ld * PS, zs - p.rzl + q, x0, y0);
+        cp_async_commit();
+      }
       if (++ld == NST) ld = 0;
-      cp_async_wait<kPtsPrefetch>();  // planes up to z + rzh have landed
-      __syncthreads();
+    };
+    for (int q = 0; q < pre; ++q)
+      if (q < nplanes || !tma) issue(q);
+    int cs = 0;  // ring slot of plane z - rzl
+    for (int z = zs; z < ze && ok; ++z) {
+      const int q = z - zs + pre;
+      if (q < nplanes || !tma) issue(q);
+      if (tma) {
+        const int need = z - zs + p.rzl + p.rzh;  // newest plane this step reads
+        while (waited <= need) {
+          if (!mbar_wait(&bars[wslot], (phase >> wslot) & 1u, p.err)) ok = false;
+          phase ^= 1u << wslot;
+          ++waited;
+          if (++wslot == NST) wslot = 0;
+        }
+      } else {
+        cp_async_wait<kPtsPrefetch>();  // planes up to z + rzh have landed
+      }
+      ok = __syncthreads_and(ok);
+      if (!ok) break;
 
       T acc[RY][kPtsVX];
       if constexpr (S::kStatic) {
@@ -167,34 +225,41 @@ __device__ __forceinline__ void pts_body(const PtsParams<T> &p, unsigned char *s
         for (int k = 0; k < S::kN; ++k) {
           int s = cs + S::kLag[k];
           if (s >= NST) s -= NST;
-          pts_term<T, RY, UNIT>(acc, ring + s * PE + cell0 + S::kOff[k], W, (T)S::kWt[k],
+          pts_term<T, RY, UNIT>(acc, ring + s * PS + cell0 + S::kOff[k], W, (T)S::kWt[k],
                                 k == 0);
         }
       } else {
         for (int k = 0; k < p.n; ++k) {
           int s = cs + s_lag[k];
           if (s >= NST) s -= NST;
-          pts_term<T, RY, UNIT>(acc, ring + s * PE + cell0 + s_off[k], W, s_w[k], k == 0);
+          pts_term<T, RY, UNIT>(acc, ring + s * PS + cell0 + s_off[k], W, s_w[k], k == 0);
         }
       }
 
+      T *dst = out0 + (long long)z * p.plane;
 #pragma unroll
       for (int r = 0; r < RY; ++r) {
         const int y = y0 + warp * RY + r;
-        if (y >= p.dmax1) continue;
-        T *dst = p.out + (long long)z * p.plane + (long long)y * p.row;
+        const bool row_on = ((rowmask >> r) & 1u) &&
+                            (p.color < 0 || ((xpar + y + z + p.color) & 1) == 0);
+        if (row_on) {
 #pragma unroll
-        for (int j = 0; j < kPtsVX; ++j) {
-          const int x = x0 + lane + 32 * j;
-          const bool in_dom = x >= p.dmin0 && x < p.dmax0;
-          const bool colored = p.color < 0 || ((x + y + z + p.color) & 1) == 0;
-          if (in_dom && colored) dst[x] = acc[r][j];
+          for (int j = 0; j < kPtsVX; ++j)
+            if ((colmask >> j) & 1u) dst[r * p.row + 32 * j] = acc[r][j];
         }
       }
       if (++cs == NST) cs = 0;
       __syncthreads();  // the slot of plane z - rzl is refilled next step
     }
-    cp_async_wait<0>();  // only empty groups can remain
+    if (!tma) cp_async_wait<0>();  // only empty groups can remain
+    if (!ok && tma && tid == 0) {
+      // a wait gave up: let copies still in flight land (bounded) before exit
+      for (; waited < issued; ++waited) {
+        mbar_wait(&bars[wslot], (phase >> wslot) & 1u, nullptr, 1024);
+        phase ^= 1u << wslot;
+        if (++wslot == NST) wslot = 0;
+      }
+    }
   }
 }
 

@@ -12,75 +12,6 @@
 
 namespace psg {
 
-// Error bits written into the runtime's device error word.
-enum : int {
-  kDevErrWaitTimeout = 1,  // an mbarrier wait ran past its iteration limit
-  kDevErrBadLaunch = 2,    // a kernel found inconsistent launch parameters
-};
-
-// Iteration limit for every spin-wait in this library.  One iteration is a
-// try_wait (returns at once or after a short hardware window) plus a short
-// sleep after the first few, so the limit bounds a wait to well under a
-// second of wall time.
-constexpr uint32_t kWaitLimit = 1u << 22;
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(count)
-               : "memory");
-}
-
-// Makes initialised mbarriers visible to the async (TMA) proxy.
-__device__ __forceinline__ void fence_barrier_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar,
-                                                      uint32_t bytes) {
-  asm volatile(
-      "mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(
-          smem_u32(bar)),
-      "r"(bytes)
-      : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait for the phase with the given parity to complete.  Returns
-// false (and sets kDevErrWaitTimeout in *err) if the limit runs out.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
-                                          int *err, uint32_t limit = kWaitLimit) {
-  for (uint32_t i = 0; i < limit; ++i) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if (i >= 8) __nanosleep(64);
-  }
-  if (err) atomicOr(err, kDevErrWaitTimeout);
-  return false;
-}
-
-// 3D tiled TMA load of box {w,h,1} at element coordinates (x,y,z) into
-// shared memory, completing on `bar`.  x * sizeof(element) must be a
-// multiple of 16 bytes (callers keep x a multiple of 16/sizeof(T)).
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map,
-                                            int x, int y, int z, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z),
-      "r"(smem_u32(bar))
-      : "memory");
-}
-
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap *map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map))
                : "memory");

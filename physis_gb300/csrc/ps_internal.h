@@ -129,8 +129,13 @@ struct PointsArgs {
   int d[kMaxPoints][3];
   double w[kMaxPoints];
   bool unit;         // every weight is 1: terms are the point values
+  int *err;          // device error word
+  bool has_tmap;     // tmap maps `in` with the box points_box() gives
+  CUtensorMap tmap;
 };
 // cfg.warps x cfg.rows (1 or 2) rows per tile; the other fields are unused.
+// The TMA box of one ring plane: w cells by h rows.
+void points_box(const PointsArgs &a, const MarchConfig &cfg, int *w, int *h);
 size_t points_smem_bytes(const PointsArgs &a, const MarchConfig &cfg);
 cudaError_t launch_points(const PointsArgs &a, const MarchConfig &cfg, int sm_count,
                           cudaStream_t s);
@@ -168,7 +173,7 @@ struct PtsJitKey {
   int type;                  // ElemType
   int ry, warps, n;
   bool unit;
-  int w, nstage, plane_elems;
+  int w, nstage, pstride;
   int off[kMaxPoints], lag[kMaxPoints];
   double wt[kMaxPoints];
 };
@@ -177,9 +182,9 @@ struct PtsJitKey {
 void *jit_points_function(const PtsJitKey &k);
 // Sets the kernel's dynamic shared memory limit and returns its occupancy.
 bool jit_prepare(void *fn, int threads, size_t smem, int *occ);
-// Launches a kernel whose one parameter is the struct at `params`.
+// Launches a compiled kernel; args[i] points at its i-th parameter.
 cudaError_t jit_launch_raw(void *fn, int grid, dim3 block, size_t smem, cudaStream_t s,
-                           const void *params);
+                           void **args);
 
 // ---- Reductions (reduce.cu) ----------------------------------------------
 // Reduces every element of g with op.  The 8-byte result is written to

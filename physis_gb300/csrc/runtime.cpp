@@ -516,6 +516,11 @@ bool launch_points_map(const Map &m, const PointStencil &ps) {
     if (cfg.rows > 1) cfg.rows = 1;
     else cfg.warps /= 2;
   }
+  a.err = rt->dev_err;
+  int bw = 0, bh = 0;
+  psg::points_box(a, cfg, &bw, &bh);
+  a.has_tmap = tmap_for(a.in, bw, bh, &a.tmap);
+  if (!a.has_tmap) return false;
   const int colors[2] = {m.color == 2 ? 0 : m.color, 1};
   const int ncol = m.color == 2 ? 2 : 1;
   for (int c = 0; c < ncol; ++c) {
