@@ -92,6 +92,42 @@ __device__ __forceinline__ void pts_load_plane(const PtsParams<T> &p, T *dst, in
   }
 }
 
+// After a TMA box load of plane zg (tile origin x0, y0; zero-filled outside
+// the grid), rewrites the box cells that lie outside the grid with the
+// values the boundary rule maps them to.  Only edge tiles of periodic and
+// clamped stencils have such cells; all threads share the work.
+template <typename T>
+__device__ __forceinline__ void pts_fix_halo(const PtsParams<T> &p, T *dst, int zg, int x0,
+                                             int y0, int W) {
+  const int xs = x0 - p.lp, ys = y0 - p.ryl, H = p.rows_h;
+  const T *plane = p.in + (long long)pts_map_axis(zg, p.nz, p.boundary) * p.plane;
+  const int cl = min(max(0, -xs), W);
+  const int cr = min(max(0, xs + W - p.nx), W - cl);
+  const int rt = min(max(0, -ys), H);
+  const int rb = min(max(0, ys + H - p.ny), H - rt);
+  const int nfull = (rt + rb) * W;            // whole rows outside in y
+  const int side = cl + cr;                   // cells per inner row outside in x
+  const int total = nfull + (H - rt - rb) * side;
+  const int nthr = blockDim.x * blockDim.y;
+  for (int i = threadIdx.y * 32 + threadIdx.x; i < total; i += nthr) {
+    int r, c;
+    if (i < nfull) {
+      const int rr = i / W;
+      c = i - rr * W;
+      r = rr < rt ? rr : H - rb + (rr - rt);
+    } else {
+      const int k = i - nfull;
+      const int rr = k / side;
+      const int cc = k - rr * side;
+      r = rt + rr;
+      c = cc < cl ? cc : W - cr + (cc - cl);
+    }
+    const int x = pts_map_axis(xs + c, p.nx, p.boundary);
+    const int y = pts_map_axis(ys + r, p.ny, p.boundary);
+    dst[r * W + c] = plane[(long long)y * p.row + x];
+  }
+}
+
 // The run-time spec: the point table travels in the kernel parameters and is
 // copied to shared memory; the tile geometry comes from the parameters.
 struct PtsTableSpec {
@@ -120,12 +156,13 @@ __device__ __forceinline__ void pts_term(T (&acc)[RY][kPtsVX], const T *src, int
 }
 
 // The sweep: persistent (z-chunk, tile) items, a ring of planes, the points
-// summed in order, masked stores.  A tile whose box lies inside the grid --
-// or any tile when the boundary rule is "none", whose out-of-grid halo is
-// never read -- arrives by one TMA box load per plane (mbarrier per stage);
-// the edge tiles of periodic and clamped stencils use cp.async through the
-// boundary map (one commit group per plane).  `smem_raw` is the dynamic
-// shared memory, `tmap` the TMA descriptor of `in` (used if p.use_tma).
+// summed in order, masked stores.  Each plane of a tile arrives by one TMA
+// box load (mbarrier per stage); on the edge tiles of periodic and clamped
+// stencils the out-of-grid cells of the box are then rewritten through the
+// boundary map (with boundary "none" they are never read).  Without a TMA
+// descriptor (p.use_tma == 0) planes are copied with cp.async through the
+// boundary map instead (one commit group per plane).  `smem_raw` is the
+// dynamic shared memory, `tmap` the TMA descriptor of `in`.
 template <typename T, int RY, bool UNIT, class S>
 __device__ __forceinline__ void pts_body(const PtsParams<T> &p, const void *tmap,
                                          unsigned char *smem_raw) {
@@ -167,10 +204,10 @@ __device__ __forceinline__ void pts_body(const PtsParams<T> &p, const void *tmap
     const int x0 = p.xbase + (tile % p.tiles_x) * kPtsTX;
     const int y0 = p.dmin1 + (tile / p.tiles_x) * TY;
     const int nplanes = ze - zs + p.rzl + p.rzh;  // planes zs-rzl .. ze+rzh-1
-    const bool tma =
-        p.use_tma && (p.boundary == kPtsNone ||
-                      (x0 - p.lp >= 0 && x0 - p.lp + W <= p.nx && y0 - p.ryl >= 0 &&
-                       y0 - p.ryl + p.rows_h <= p.ny));
+    const bool tma = p.use_tma != 0;
+    const bool fix = tma && p.boundary != kPtsNone &&
+                     !(x0 - p.lp >= 0 && x0 - p.lp + W <= p.nx && y0 - p.ryl >= 0 &&
+                       y0 - p.ryl + p.rows_h <= p.ny);
     // store masks: columns j in the domain, rows r in the domain
     unsigned colmask = 0, rowmask = 0;
 #pragma unroll
@@ -209,6 +246,7 @@ __device__ __forceinline__ void pts_body(const PtsParams<T> &p, const void *tmap
         const int need = z - zs + p.rzl + p.rzh;  // newest plane this step reads
         while (waited <= need) {
           if (!mbar_wait(&bars[wslot], (phase >> wslot) & 1u, p.err)) ok = false;
+          if (fix && ok) pts_fix_halo(p, ring + wslot * PS, zs - p.rzl + waited, x0, y0, W);
           phase ^= 1u << wslot;
           ++waited;
           if (++wslot == NST) wslot = 0;
