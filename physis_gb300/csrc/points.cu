@@ -185,6 +185,9 @@ template <typename T>
 cudaError_t launch_type(const PointsArgs &a, const MarchConfig &cfg, int sm_count,
                         cudaStream_t s) {
   const int warps = cfg.warps;
+  if (cfg.rows >= 4)
+    return a.unit ? launch_t<T, 4, true>(a, warps, sm_count, s)
+                  : launch_t<T, 4, false>(a, warps, sm_count, s);
   if (cfg.rows >= 2)
     return a.unit ? launch_t<T, 2, true>(a, warps, sm_count, s)
                   : launch_t<T, 2, false>(a, warps, sm_count, s);
@@ -194,12 +197,14 @@ cudaError_t launch_type(const PointsArgs &a, const MarchConfig &cfg, int sm_coun
 
 }  // namespace
 
+int points_rows(const MarchConfig &cfg) { return cfg.rows >= 4 ? 4 : (cfg.rows >= 2 ? 2 : 1); }
+
 void points_box(const PointsArgs &a, const MarchConfig &cfg, int *w, int *h) {
   const int vec = 16 / a.in.esz;
   int lo[3], hi[3];
   extents(a, lo, hi);
   *w = (-lo[0] + vec - 1) / vec * vec + kPtsTX + (hi[0] + vec - 1) / vec * vec;
-  *h = cfg.warps * (cfg.rows >= 2 ? 2 : 1) - lo[1] + hi[1];
+  *h = cfg.warps * points_rows(cfg) - lo[1] + hi[1];
 }
 
 size_t points_smem_bytes(const PointsArgs &a, const MarchConfig &cfg) {

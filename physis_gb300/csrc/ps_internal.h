@@ -133,7 +133,9 @@ struct PointsArgs {
   bool has_tmap;     // tmap maps `in` with the box points_box() gives
   CUtensorMap tmap;
 };
-// cfg.warps x cfg.rows (1 or 2) rows per tile; the other fields are unused.
+// cfg.warps x points_rows(cfg) (1, 2 or 4) rows per tile; the other fields
+// are unused.
+int points_rows(const MarchConfig &cfg);
 // The TMA box of one ring plane: w cells by h rows.
 void points_box(const PointsArgs &a, const MarchConfig &cfg, int *w, int *h);
 size_t points_smem_bytes(const PointsArgs &a, const MarchConfig &cfg);

@@ -513,7 +513,7 @@ bool launch_points_map(const Map &m, const PointStencil &ps) {
   MarchConfig cfg = m.has_plan ? m.plan.shape : rt->shapes[kSlotPoints];
   // the widest stencils need a shorter tile to fit their plane ring
   while (psg::points_smem_bytes(a, cfg) > 220 * 1024 && (cfg.rows > 1 || cfg.warps > 1)) {
-    if (cfg.rows > 1) cfg.rows = 1;
+    if (cfg.rows > 1) cfg.rows /= 2;
     else cfg.warps /= 2;
   }
   a.err = rt->dev_err;
@@ -878,7 +878,7 @@ std::vector<Plan> candidates(const std::vector<Map *> &ms) {
   bool all_points = true;
   for (const Map *m : ms) all_points = all_points && point_stencil(m->kernel);
   if (all_points) {  // {warps, rows} of the point-stencil tile
-    const int sh[][2] = {{8, 2}, {8, 1}, {4, 2}, {4, 1}, {16, 1}, {2, 2}};
+    const int sh[][2] = {{8, 2}, {8, 4}, {4, 2}, {4, 4}, {16, 2}, {8, 1}};
     for (auto &c : sh) out.push_back(Plan{MarchConfig{c[0], c[1], 4, 0, 0}, 1, tdef});
     return out;
   }

@@ -172,7 +172,7 @@ def test_random_point_stencils_bit_exact(rt, oracle, kernel_form, seed, shape, d
     assert np.array_equal(_bits(got), _bits(ref))
 
 
-@pytest.mark.parametrize("warps,rows", [(8, 2), (8, 1), (4, 2), (16, 1), (2, 2), (1, 1)])
+@pytest.mark.parametrize("warps,rows", [(8, 2), (8, 1), (4, 2), (16, 1), (2, 2), (1, 1), (8, 4), (4, 4)])
 def test_point_launch_shapes_do_not_change_results(rt, oracle, kernel_form, warps, rows):
     rng = np.random.default_rng(42)
     shape = (11, 45, 270)
