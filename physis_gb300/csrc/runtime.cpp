@@ -1539,6 +1539,7 @@ void PSInitV(int trace) {
     r->tshapes[k] = MarchConfig{8, 4, 3, 0, 0};
     r->tblock[k] = 1;
   }
+  r->shapes[kSlotPoints] = MarchConfig{8, 4, 4, 0, 0};  // point stencils: 8 warps x 4 rows
   r->shapes[PS_KERNEL_HIMENO19] = MarchConfig{4, 1, 5, 2, 0};
   r->shapes[PS_KERNEL_HIMENO19_GOSA] = MarchConfig{4, 1, 5, 2, 0};
   cudaDeviceSynchronize();
