@@ -11,8 +11,9 @@
  * 4. Launch-shape control and the autotuner; batches of independent runs.
  * 5. A reduction for callers that cannot allocate.
  * 6. Test hooks that exercise failure handling without faulting a GPU.
- * 7. Point-list stencils (the translator-free form of the reference's
- *    neighbour-sum stencil functions) and the non-variadic red/black map.
+ * 7. Point-list stencils and compiled stencil functions (the
+ *    translator-free front ends) and the non-variadic red/black map.
+ * 8. Building blocks of the learned warm start for the Jacobi solve.
  */
 #ifndef PHYSIS_GB300_EXT_H_
 #define PHYSIS_GB300_EXT_H_
@@ -283,6 +284,64 @@ enum PSMapColor {
  * grids..., scalars...) by colour (PS_COLOR_ALL is PSStencilMapV). */
 PSStencil PSStencilMapColorV(int kernel, int color, const PSDomain3D *dom, int ngrids,
                              void *const *grids, int nscalars, const double *scalars);
+
+/* ---- 8. Learned warm start for the 19-point Jacobi solve ----------------
+ *
+ * Building blocks of a small 3D convolutional network that predicts a warm
+ * start for the Himeno Jacobi solve from its coefficient and source fields
+ * (no counterpart in the reference).  Network tensors are channels-last
+ * [batch][z][y][x][16] BF16 in device memory; weights are FP32 masters
+ * [27 taps][16 in][16 out] (tap = (dz+1)*9 + (dy+1)*3 + (dx+1)) with BF16
+ * copies for the kernels.  Every call takes device pointers and a stream
+ * (NULL: the runtime's stream), allocates nothing, and returns PS_OK or an
+ * error code (also recorded). */
+
+/* y = epilogue(conv3x3x3(x, w_fwd) + bias) with zero padding; epilogue:
+ * ReLU if relu != 0; times (mask > 0) if mask != NULL (the backward-data
+ * pass: x = dY, w = w_bwd, mask = the layer's input).  y_ch0 (optional)
+ * receives output channel 0 in FP32.  bias may be NULL. */
+int PSWarmStartConv(const void *x, const void *w, const float *bias, const void *mask, int relu,
+                    void *y, float *y_ch0, int batch, int nz, int ny, int nx, void *stream);
+
+/* dw[27][16][16] = sum over voxels of x(v + tap) dy(v)^T, db[16] = sum of dy;
+ * work holds nsplit * (27*256 + 16) floats of partial sums (reduced in a
+ * fixed order: the result is deterministic). */
+int PSWarmStartWeightGrad(const void *x, const void *dy, float *work, int nsplit, float *dw,
+                          float *db, int batch, int nz, int ny, int nx, void *stream);
+
+/* FP32 master w[27][16][16] -> BF16 w_fwd [27][out][in] and w_bwd (taps
+ * reversed, [in][out]) for PSWarmStartConv. */
+int PSWarmStartPrepareWeights(const float *w, void *w_fwd, void *w_bwd, void *stream);
+
+/* One Adam step (Kingma & Ba 2015; step counts from 1) over n parameters. */
+int PSWarmStartAdam(float *w, const float *g, float *m, float *v, long long n, float lr, float b1,
+                    float b2, float eps, int step, void *stream);
+
+/* dy (channel 0) = 2 (pred - target) / n, other channels 0; partials[i]
+ * (one per 256 values) = sum of squared errors, in FP64. */
+int PSWarmStartLoss(const float *pred, const float *target, long long n, void *dy,
+                    double *partials, void *stream);
+
+/* Instances of a Himeno batch laid out in stacked grids: instance b sits at
+ * fine origin ((b % nsx) * inx, 0, (b / nsx) * inz) of float grids with row
+ * pitch `pitch` bytes and ny rows per plane (PSGridDevicePtr / PSGridPitch
+ * of grids made with PSGrid3DFloatNew). */
+typedef struct PSWarmStartFields {
+  const float *a0, *a1, *a2, *wrk1, *bnd, *p;
+  long long pitch;
+  int ny;
+  int inx, iny, inz, nsx, factor, batch;
+  float wscale, pscale;
+} PSWarmStartFields;
+
+/* Network input: per factor^3 block of each instance, channels mean ln a0,
+ * mean ln a1, mean ln a2, mean wrk1 * wscale, mean bnd, then zeros. */
+int PSWarmStartPool(const PSWarmStartFields *f, void *out, void *stream);
+/* Training target: per block, mean p * pscale (FP32). */
+int PSWarmStartPoolTarget(const PSWarmStartFields *f, float *out, void *stream);
+/* Warm start: p = bnd * trilinear(coarse) / pscale at every fine cell, from
+ * coarse cell centres at (c + 0.5) * factor - 0.5 (clamped). */
+int PSWarmStartUpsample(const PSWarmStartFields *f, const float *coarse, float *p, void *stream);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop

@@ -1,0 +1,149 @@
+"""CPU oracle of the learned warm start's arithmetic (numpy, FP64).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/ and bench.py's checks, never by
+the product.  The learned warm start has no counterpart in the reference, so
+this oracle is pinned by its own consistency checks (the analytic gradients
+below against central finite differences, tests/test_nn_oracle.py) and the
+GPU kernels are checked against it.
+
+Tensors are channels-last, [batch, z, y, x, 16], BF16 stored as uint16.
+conv: Y[b,z,y,x,o] = bias[o] + sum_{t, i} X[b, (z,y,x) + d_t, i] * W[t, i, o]
+with the 27 taps t = (dz+1)*9 + (dy+1)*3 + (dx+1), zero padding.
+"""
+import numpy as np
+
+C = 16          # channels of every layer (inputs and the output padded)
+TAPS = [(dz, dy, dx) for dz in (-1, 0, 1) for dy in (-1, 0, 1) for dx in (-1, 0, 1)]
+
+
+def to_bf16(a):
+    """float -> bf16 bits (uint16), round to nearest even."""
+    f = np.ascontiguousarray(a, dtype=np.float32)
+    u = f.view(np.uint32).astype(np.uint64)
+    r = (u + 0x7FFF + ((u >> 16) & 1)) >> 16
+    return r.astype(np.uint16)
+
+
+def from_bf16(b):
+    return (np.asarray(b, dtype=np.uint16).astype(np.uint32) << 16).view(np.float32)
+
+
+def _shift(x, d):
+    """x[b, z+dz, y+dy, x+dx, :] with zeros outside (x: [B,Z,Y,X,C])."""
+    dz, dy, dx = d
+    out = np.zeros_like(x)
+    B, Z, Y, X, _ = x.shape
+    zs = slice(max(0, -dz), min(Z, Z - dz))
+    ys = slice(max(0, -dy), min(Y, Y - dy))
+    xs = slice(max(0, -dx), min(X, X - dx))
+    zt = slice(max(0, dz), min(Z, Z + dz))
+    yt = slice(max(0, dy), min(Y, Y + dy))
+    xt = slice(max(0, dx), min(X, X + dx))
+    out[:, zs, ys, xs, :] = x[:, zt, yt, xt, :]
+    return out
+
+
+def conv_fwd(x, w, bias=None):
+    """x [B,Z,Y,X,Ci], w [27,Ci,Co] -> [B,Z,Y,X,Co] in float64."""
+    x = np.asarray(x, np.float64)
+    w = np.asarray(w, np.float64)
+    y = np.zeros(x.shape[:4] + (w.shape[2],))
+    for t, d in enumerate(TAPS):
+        y += _shift(x, d) @ w[t]
+    if bias is not None:
+        y += np.asarray(bias, np.float64)
+    return y
+
+
+def conv_bwd_data(dy, w):
+    """dL/dx of conv_fwd given dL/dy: the conv of dy with w flipped in space
+    and transposed in channels."""
+    wt = np.asarray(w, np.float64)[::-1].transpose(0, 2, 1)
+    return conv_fwd(dy, wt)
+
+
+def conv_bwd_weight(x, dy):
+    """dL/dw [27,Ci,Co] and dL/dbias [Co]."""
+    x = np.asarray(x, np.float64)
+    dy = np.asarray(dy, np.float64)
+    ci, co = x.shape[-1], dy.shape[-1]
+    dw = np.zeros((27, ci, co))
+    for t, d in enumerate(TAPS):
+        dw[t] = _shift(x, d).reshape(-1, ci).T @ dy.reshape(-1, co)
+    return dw, dy.reshape(-1, co).sum(0)
+
+
+def relu(a):
+    return np.maximum(a, 0.0)
+
+
+def network_fwd(x, ws, bs):
+    """The 6-layer net: conv+ReLU x5, conv; returns every layer's output
+    (float64, before any BF16 rounding)."""
+    acts = [np.asarray(x, np.float64)]
+    for l, (w, b) in enumerate(zip(ws, bs)):
+        y = conv_fwd(acts[-1], w, b)
+        acts.append(relu(y) if l < len(ws) - 1 else y)
+    return acts
+
+
+def mse_loss(pred, target):
+    """Mean of (pred[..., 0] - target)^2 and its gradient wrt pred."""
+    diff = np.asarray(pred[..., 0], np.float64) - np.asarray(target, np.float64)
+    g = np.zeros(np.shape(pred))
+    g[..., 0] = 2.0 * diff / diff.size
+    return float((diff ** 2).mean()), g
+
+
+def network_grads(x, ws, bs, target):
+    """Loss and gradients of every weight and bias (float64 backprop)."""
+    acts = network_fwd(x, ws, bs)
+    loss, g = mse_loss(acts[-1], target)
+    dws, dbs = [None] * len(ws), [None] * len(ws)
+    for l in range(len(ws) - 1, -1, -1):
+        dws[l], dbs[l] = conv_bwd_weight(acts[l], g)
+        if l:
+            g = conv_bwd_data(g, ws[l]) * (acts[l] > 0)
+    return loss, dws, dbs
+
+
+def adam(w, g, m, v, step, lr, b1=0.9, b2=0.999, eps=1e-8):
+    """One Adam step (Kingma & Ba 2015), bias-corrected; returns new w, m, v."""
+    m = b1 * m + (1 - b1) * g
+    v = b2 * v + (1 - b2) * g * g
+    mh = m / (1 - b1 ** step)
+    vh = v / (1 - b2 ** step)
+    return w - lr * mh / (np.sqrt(vh) + eps), m, v
+
+
+def pool(fine, f):
+    """Mean over f x f x f blocks (partial blocks at the far edges average
+    what they hold): fine [Z,Y,X] -> [ceil(Z/f), ceil(Y/f), ceil(X/f)]."""
+    Z, Y, X = fine.shape
+    zc, yc, xc = -(-Z // f), -(-Y // f), -(-X // f)
+    s = np.zeros((zc, yc, xc))
+    n = np.zeros((zc, yc, xc))
+    iz, iy, ix = np.meshgrid(np.arange(Z) // f, np.arange(Y) // f, np.arange(X) // f,
+                             indexing="ij")
+    np.add.at(s, (iz, iy, ix), fine)
+    np.add.at(n, (iz, iy, ix), 1.0)
+    return s / n
+
+
+def upsample(coarse, shape, f):
+    """Trilinear interpolation from coarse cell centres (z_c + 0.5) * f - 0.5
+    to every fine point, clamped at the ends."""
+    out = coarse
+    for axis, n in enumerate(shape):
+        nc = coarse.shape[axis]
+        pos = (np.arange(n) + 0.5) / f - 0.5
+        pos = np.clip(pos, 0, nc - 1)
+        i0 = np.floor(pos).astype(int)
+        i1 = np.minimum(i0 + 1, nc - 1)
+        t = pos - i0
+        a = np.take(out, i0, axis=axis)
+        b = np.take(out, i1, axis=axis)
+        sh = [1] * out.ndim
+        sh[axis] = n
+        out = a * (1 - t.reshape(sh)) + b * t.reshape(sh)
+    return out

@@ -57,7 +57,9 @@ PSSetTemporalBlocking PSGetTemporalBlocking PSSetAutotune PSSetTuneCachePath
 PSLoadTuneCache PSClearTuning PSGetStencilPlan PSBatchCreate PSBatchRun PSBatchFree
 PSSetBatchShape __PSStencilMapRedBlack __PSStencilMapRed __PSStencilMapBlack
 PSStencilMapColorV PSPointStencilNew PSStencilFunctionNew
-PSStencilFunctionCheck""".split()
+PSStencilFunctionCheck PSWarmStartConv PSWarmStartWeightGrad PSWarmStartPrepareWeights
+PSWarmStartAdam PSWarmStartLoss PSWarmStartPool PSWarmStartPoolTarget
+PSWarmStartUpsample""".split()
 
 
 class PSDomain(ctypes.Structure):
@@ -71,6 +73,16 @@ class PSLaunchShape(ctypes.Structure):
     _fields_ = [("warps", ctypes.c_int), ("rows", ctypes.c_int),
                 ("ns", ctypes.c_int), ("ns2", ctypes.c_int),
                 ("ctas_per_sm", ctypes.c_int)]
+
+
+class PSWarmStartFields(ctypes.Structure):
+    """PSWarmStartFields (include/physis_gb300/physis_gb300.h)."""
+    _fields_ = [("a0", ctypes.c_void_p), ("a1", ctypes.c_void_p), ("a2", ctypes.c_void_p),
+                ("wrk1", ctypes.c_void_p), ("bnd", ctypes.c_void_p), ("p", ctypes.c_void_p),
+                ("pitch", ctypes.c_longlong), ("ny", ctypes.c_int), ("inx", ctypes.c_int),
+                ("iny", ctypes.c_int), ("inz", ctypes.c_int), ("nsx", ctypes.c_int),
+                ("factor", ctypes.c_int), ("batch", ctypes.c_int), ("wscale", ctypes.c_float),
+                ("pscale", ctypes.c_float)]
 
 
 class PSError(RuntimeError):
@@ -169,6 +181,20 @@ def lib():
     L.PSStencilFunctionCheck.argtypes = [ctypes.c_char_p, ctypes.c_char_p,
                                          ctypes.c_char_p, ctypes.c_size_t]
     L.PSStencilFunctionCheck.restype = i
+    L.PSWarmStartConv.argtypes = [vp, vp, vp, vp, i, vp, vp, i, i, i, i, vp]
+    L.PSWarmStartWeightGrad.argtypes = [vp, vp, vp, i, vp, vp, i, i, i, i, vp]
+    L.PSWarmStartPrepareWeights.argtypes = [vp, vp, vp, vp]
+    L.PSWarmStartAdam.argtypes = [vp, vp, vp, vp, ctypes.c_longlong, ctypes.c_float,
+                                  ctypes.c_float, ctypes.c_float, ctypes.c_float, i, vp]
+    L.PSWarmStartLoss.argtypes = [vp, vp, ctypes.c_longlong, vp, vp, vp]
+    fp = ctypes.POINTER(PSWarmStartFields)
+    L.PSWarmStartPool.argtypes = [fp, vp, vp]
+    L.PSWarmStartPoolTarget.argtypes = [fp, vp, vp]
+    L.PSWarmStartUpsample.argtypes = [fp, vp, vp, vp]
+    for name in ("PSWarmStartConv", "PSWarmStartWeightGrad", "PSWarmStartPrepareWeights",
+                 "PSWarmStartAdam", "PSWarmStartLoss", "PSWarmStartPool",
+                 "PSWarmStartPoolTarget", "PSWarmStartUpsample"):
+        getattr(L, name).restype = i
     _lib = L
     return L
 

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libphysis_gb300.so")
 SOURCES = ["runtime.cpp", "march.cpp", "stencil7.cu", "temporal7.cu", "himeno19.cu",
-           "reduce.cu", "batch.cu", "points.cu", "jit.cpp"]
+           "reduce.cu", "batch.cu", "points.cu", "jit.cpp", "nn.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -1,0 +1,484 @@
+// Kernels of the learned warm start for the 19-point Jacobi (Himeno) solve:
+// a 3D convolutional network of 3x3x3 layers with 16 channels, BF16 weights
+// and activations, FP32 accumulation, trained on the GPU.  No counterpart in
+// the reference.
+//
+// Tensors are channels-last, [batch, z, y, x, 16] BF16 (16 channels: 32
+// bytes per voxel).  A convolution is an implicit GEMM per tap: rows are
+// voxels, K the 16 input channels, N the 16 output channels.  Tensor cores
+// via mma.sync.m16n8k16 (BF16 in, FP32 accumulate): each warp owns 16
+// voxels and accumulates 27 taps x 2 n-tiles; the layer's weights sit in
+// shared memory in the fragment-friendly [tap][out][in] order.  The
+// backward-data pass is the same kernel with the weights flipped in space
+// and transposed in channels; the weight gradient is a K = voxels GEMM per
+// tap, split over CTAs and reduced in a fixed order (deterministic).
+// Pooling (fine grids -> coarse network input), the MSE gradient, Adam and
+// trilinear upsampling (coarse prediction -> fine warm start) complete the
+// set.  Every kernel is checked against oracle/nn_oracle.py.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ps_internal.h"
+
+namespace psg {
+namespace {
+
+constexpr int kC = 16;       // channels
+constexpr int kTaps = 27;
+constexpr int kConvWarps = 8;
+
+__device__ __forceinline__ void mma_16816(float (&d)[4], const uint32_t (&a)[4],
+                                          uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+struct Dims {
+  int B, Z, Y, X;
+  long long nvox;
+};
+
+// Voxel coordinates of flattened index v (x fastest).
+struct Vox {
+  int b, z, y, x;
+  bool ok;
+};
+__device__ __forceinline__ Vox vox_of(long long v, const Dims &d) {
+  Vox r;
+  r.ok = v < d.nvox;
+  if (!r.ok) v = 0;
+  r.x = (int)(v % d.X);
+  long long t = v / d.X;
+  r.y = (int)(t % d.Y);
+  t /= d.Y;
+  r.z = (int)(t % d.Z);
+  r.b = (int)(t / d.Z);
+  return r;
+}
+
+// Flattened index of the neighbour of `p` at tap t, or -1 outside.
+__device__ __forceinline__ long long nbr(const Vox &p, int t, const Dims &d) {
+  const int dz = t / 9 - 1, dy = (t / 3) % 3 - 1, dx = t % 3 - 1;
+  const int z = p.z + dz, y = p.y + dy, x = p.x + dx;
+  if (!p.ok || z < 0 || z >= d.Z || y < 0 || y >= d.Y || x < 0 || x >= d.X) return -1;
+  return (((long long)p.b * d.Z + z) * d.Y + y) * d.X + x;
+}
+
+__device__ __forceinline__ uint32_t ld_pair(const __nv_bfloat16 *base, long long v, int c) {
+  return v < 0 ? 0u : *reinterpret_cast<const uint32_t *>(base + v * kC + c);
+}
+__device__ __forceinline__ uint32_t pack2(const __nv_bfloat16 *base, long long v0, long long v1,
+                                          int c) {
+  const uint16_t lo = v0 < 0 ? 0 : reinterpret_cast<const uint16_t *>(base)[v0 * kC + c];
+  const uint16_t hi = v1 < 0 ? 0 : reinterpret_cast<const uint16_t *>(base)[v1 * kC + c];
+  return (uint32_t)lo | ((uint32_t)hi << 16);
+}
+
+// Y = epilogue(conv(X, W) + bias): relu, or times (mask > 0).  W is
+// [27][out][in] BF16.  yf (optional) receives channel 0 in FP32.
+__global__ void __launch_bounds__(32 * kConvWarps)
+conv_kernel(const __nv_bfloat16 *__restrict__ x, const __nv_bfloat16 *__restrict__ w,
+            const float *__restrict__ bias, const __nv_bfloat16 *__restrict__ mask,
+            int relu, __nv_bfloat16 *__restrict__ y, float *__restrict__ yf, Dims d) {
+  __shared__ __align__(16) __nv_bfloat16 ws[kTaps * kC * kC];
+  for (int i = threadIdx.x; i < kTaps * kC * kC / 8; i += blockDim.x)
+    reinterpret_cast<uint4 *>(ws)[i] = reinterpret_cast<const uint4 *>(w)[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, q = lane & 3;
+  const long long v0 = ((long long)blockIdx.x * kConvWarps + warp) * 16;
+  if (v0 >= d.nvox) return;
+  const Vox pa = vox_of(v0 + g, d), pb = vox_of(v0 + g + 8, d);
+  float acc0[4] = {0.f, 0.f, 0.f, 0.f}, acc1[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int t = 0; t < kTaps; ++t) {
+    const long long na = nbr(pa, t, d), nb = nbr(pb, t, d);
+    const uint32_t a[4] = {ld_pair(x, na, 2 * q), ld_pair(x, nb, 2 * q),
+                           ld_pair(x, na, 2 * q + 8), ld_pair(x, nb, 2 * q + 8)};
+    const uint32_t *wt = reinterpret_cast<const uint32_t *>(ws + t * kC * kC);
+    // B (k = in, n = out) from ws[t][out][in]: two consecutive in-channels
+    mma_16816(acc0, a, wt[(g * kC + 2 * q) / 2], wt[(g * kC + 2 * q + 8) / 2]);
+    mma_16816(acc1, a, wt[((g + 8) * kC + 2 * q) / 2], wt[((g + 8) * kC + 2 * q + 8) / 2]);
+  }
+  // C: c0,c1 -> (voxel g, out 2q, 2q+1); c2,c3 -> (voxel g+8, ...)
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    const Vox &p = half ? pb : pa;
+    if (!p.ok) continue;
+    const long long v = v0 + g + 8 * half;
+#pragma unroll
+    for (int tile = 0; tile < 2; ++tile) {
+      const float *acc = tile ? acc1 : acc0;
+      const int co = 2 * q + 8 * tile;
+      float r0 = acc[2 * half], r1 = acc[2 * half + 1];
+      if (bias) {
+        r0 += bias[co];
+        r1 += bias[co + 1];
+      }
+      if (relu) {
+        r0 = fmaxf(r0, 0.f);
+        r1 = fmaxf(r1, 0.f);
+      }
+      if (mask) {
+        const __nv_bfloat162 m = *reinterpret_cast<const __nv_bfloat162 *>(mask + v * kC + co);
+        if (!(__bfloat162float(m.x) > 0.f)) r0 = 0.f;
+        if (!(__bfloat162float(m.y) > 0.f)) r1 = 0.f;
+      }
+      *reinterpret_cast<__nv_bfloat162 *>(y + v * kC + co) = __floats2bfloat162_rn(r0, r1);
+      if (yf && co == 0) yf[v] = r0;
+    }
+  }
+}
+
+// Partial weight gradients: block (t, s) sums over the s-th share of the
+// 16-voxel chunks dW[t][in][out] = sum_v X[v + d_t][in] * dY[v][out] into
+// part[s][t][in][out]; blocks of the centre tap also sum dY into
+// bpart[s][out] (the bias gradient).
+__global__ void __launch_bounds__(32 * kConvWarps)
+wgrad_kernel(const __nv_bfloat16 *__restrict__ x, const __nv_bfloat16 *__restrict__ dy,
+             float *__restrict__ part, float *__restrict__ bpart, Dims d) {
+  __shared__ float red[kConvWarps][kC * kC];
+  __shared__ float bred[kConvWarps][kC];
+  const int t = blockIdx.x, s = blockIdx.y, S = gridDim.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, q = lane & 3;
+  float acc0[4] = {0.f, 0.f, 0.f, 0.f}, acc1[4] = {0.f, 0.f, 0.f, 0.f};
+  float bsum0 = 0.f, bsum1 = 0.f;
+  const long long nchunks = (d.nvox + 15) / 16;
+  for (long long c = (long long)s * kConvWarps + warp; c < nchunks; c += (long long)S * kConvWarps) {
+    const long long k0 = c * 16 + 2 * q;  // this lane's voxels: k0, k0+1, k0+8, k0+9
+    const long long vk[4] = {k0, k0 + 1, k0 + 8, k0 + 9};
+    long long nb[4], dv[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const Vox p = vox_of(vk[i], d);
+      nb[i] = nbr(p, t, d);
+      dv[i] = p.ok ? vk[i] : -1;
+    }
+    // A = X^T (rows in-channel, k voxel)
+    const uint32_t a[4] = {pack2(x, nb[0], nb[1], g), pack2(x, nb[0], nb[1], g + 8),
+                           pack2(x, nb[2], nb[3], g), pack2(x, nb[2], nb[3], g + 8)};
+    // B = dY (k voxel, n out-channel)
+    const uint32_t b00 = pack2(dy, dv[0], dv[1], g), b01 = pack2(dy, dv[2], dv[3], g);
+    const uint32_t b10 = pack2(dy, dv[0], dv[1], g + 8), b11 = pack2(dy, dv[2], dv[3], g + 8);
+    mma_16816(acc0, a, b00, b01);
+    mma_16816(acc1, a, b10, b11);
+    if (t == 13) {
+      const uint32_t bb[4] = {b00, b01, b10, b11};
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const float lo = __uint_as_float(bb[i] << 16), hi = __uint_as_float(bb[i] & 0xffff0000u);
+        if (i < 2) bsum0 += lo + hi;
+        else bsum1 += lo + hi;
+      }
+    }
+  }
+  // C tile layout: (row in g / g+8, col out 2q, 2q+1 [+8 for tile 1])
+#pragma unroll
+  for (int tile = 0; tile < 2; ++tile) {
+    const float *acc = tile ? acc1 : acc0;
+    const int co = 2 * q + 8 * tile;
+    red[warp][g * kC + co] = acc[0];
+    red[warp][g * kC + co + 1] = acc[1];
+    red[warp][(g + 8) * kC + co] = acc[2];
+    red[warp][(g + 8) * kC + co + 1] = acc[3];
+  }
+  bsum0 += __shfl_xor_sync(0xffffffffu, bsum0, 1);
+  bsum0 += __shfl_xor_sync(0xffffffffu, bsum0, 2);
+  bsum1 += __shfl_xor_sync(0xffffffffu, bsum1, 1);
+  bsum1 += __shfl_xor_sync(0xffffffffu, bsum1, 2);
+  if (q == 0) {
+    bred[warp][g] = bsum0;
+    bred[warp][g + 8] = bsum1;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kC * kC; i += blockDim.x) {
+    float v = 0.f;
+    for (int w = 0; w < kConvWarps; ++w) v += red[w][i];
+    part[((long long)s * kTaps + t) * kC * kC + i] = v;
+  }
+  if (t == 13 && threadIdx.x < kC) {
+    float v = 0.f;
+    for (int w = 0; w < kConvWarps; ++w) v += bred[w][threadIdx.x];
+    bpart[s * kC + threadIdx.x] = v;
+  }
+}
+
+__global__ void wgrad_reduce_kernel(const float *__restrict__ part,
+                                    const float *__restrict__ bpart, int S,
+                                    float *__restrict__ dw, float *__restrict__ db) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = kTaps * kC * kC;
+  if (i < n) {
+    float v = 0.f;
+    for (int s = 0; s < S; ++s) v += part[(long long)s * n + i];
+    dw[i] = v;
+  } else if (i < n + kC && db) {
+    float v = 0.f;
+    for (int s = 0; s < S; ++s) v += bpart[s * kC + (i - n)];
+    db[i - n] = v;
+  }
+}
+
+// FP32 master [27][in][out] -> BF16 forward [27][out][in] and backward-data
+// [27][in][out] with taps reversed (the adjoint convolution).
+__global__ void prep_weights_kernel(const float *__restrict__ w, __nv_bfloat16 *__restrict__ wf,
+                                    __nv_bfloat16 *__restrict__ wb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kTaps * kC * kC) return;
+  const int t = i / (kC * kC), ci = (i / kC) % kC, co = i % kC;
+  const __nv_bfloat16 v = __float2bfloat16_rn(w[i]);
+  wf[(t * kC + co) * kC + ci] = v;
+  wb[((kTaps - 1 - t) * kC + ci) * kC + co] = v;
+}
+
+// Adam (Kingma & Ba 2015) with bias corrections c1 = 1/(1 - b1^t),
+// c2 = 1/(1 - b2^t).
+__global__ void adam_kernel(float *__restrict__ w, const float *__restrict__ g,
+                            float *__restrict__ m, float *__restrict__ v, long long n, float lr,
+                            float b1, float b2, float eps, float c1, float c2) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  w[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+}
+
+// dY (channel 0) = 2 (pred - target) / n; per-block FP64 sums of the
+// squared error in part[blockIdx.x].
+__global__ void mse_kernel(const float *__restrict__ pred, const float *__restrict__ tgt,
+                           long long n, __nv_bfloat16 *__restrict__ dy,
+                           double *__restrict__ part) {
+  __shared__ double red[256];
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double e2 = 0.0;
+  if (i < n) {
+    const float e = pred[i] - tgt[i];
+    e2 = (double)e * (double)e;
+    uint4 z = make_uint4(0, 0, 0, 0);
+    uint4 *row = reinterpret_cast<uint4 *>(dy + i * kC);
+    row[0] = z;
+    row[1] = z;
+    dy[i * kC] = __float2bfloat16_rn(2.f * e / (float)n);
+  }
+  red[threadIdx.x] = e2;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// Fine stacked grids -> coarse network input.  Instance b sits at fine
+// origin ((b % nsx) * inx, 0, (b / nsx) * inz) of float grids with row pitch
+// `pitch` bytes and ny rows per plane; coarse cell (zc, yc, xc) averages the
+// fine cells [zc f, zc f + f) x ... inside the instance.  Channels: mean ln a0,
+// mean ln a1, mean ln a2, mean wrk1 * wscale, mean bnd, zeros.
+struct PoolArgs {
+  const float *a0, *a1, *a2, *wrk1, *bnd, *p;
+  long long pitch_e;  // row pitch in floats
+  int ny;             // rows per plane of the stacked grids
+  int inx, iny, inz;  // instance size
+  int nsx;            // instances along x
+  int f;              // pooling factor
+  int zc, yc, xc;     // coarse size
+  int batch;
+  float wscale, pscale;
+};
+
+__device__ __forceinline__ long long fine_index(const PoolArgs &a, int b, int z, int y, int x) {
+  const int ox = (b % a.nsx) * a.inx, oz = (b / a.nsx) * a.inz;
+  return ((long long)(oz + z) * a.ny + y) * a.pitch_e + ox + x;
+}
+
+__global__ void pool_inputs_kernel(PoolArgs a, __nv_bfloat16 *__restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = (long long)a.batch * a.zc * a.yc * a.xc;
+  if (i >= n) return;
+  const int xc = (int)(i % a.xc), yc = (int)((i / a.xc) % a.yc);
+  const int zc = (int)((i / ((long long)a.xc * a.yc)) % a.zc);
+  const int b = (int)(i / ((long long)a.xc * a.yc * a.zc));
+  float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  int cnt = 0;
+  for (int z = zc * a.f; z < min(zc * a.f + a.f, a.inz); ++z)
+    for (int y = yc * a.f; y < min(yc * a.f + a.f, a.iny); ++y)
+      for (int x = xc * a.f; x < min(xc * a.f + a.f, a.inx); ++x) {
+        const long long k = fine_index(a, b, z, y, x);
+        s[0] += logf(a.a0[k]);
+        s[1] += logf(a.a1[k]);
+        s[2] += logf(a.a2[k]);
+        s[3] += a.wrk1[k];
+        s[4] += a.bnd[k];
+        ++cnt;
+      }
+  const float inv = 1.f / (float)cnt;
+  __nv_bfloat16 *row = out + i * kC;
+  row[0] = __float2bfloat16_rn(s[0] * inv);
+  row[1] = __float2bfloat16_rn(s[1] * inv);
+  row[2] = __float2bfloat16_rn(s[2] * inv);
+  row[3] = __float2bfloat16_rn(s[3] * inv * a.wscale);
+  row[4] = __float2bfloat16_rn(s[4] * inv);
+  for (int c = 5; c < kC; ++c) row[c] = __float2bfloat16_rn(0.f);
+}
+
+__global__ void pool_target_kernel(PoolArgs a, float *__restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = (long long)a.batch * a.zc * a.yc * a.xc;
+  if (i >= n) return;
+  const int xc = (int)(i % a.xc), yc = (int)((i / a.xc) % a.yc);
+  const int zc = (int)((i / ((long long)a.xc * a.yc)) % a.zc);
+  const int b = (int)(i / ((long long)a.xc * a.yc * a.zc));
+  float s = 0.f;
+  int cnt = 0;
+  for (int z = zc * a.f; z < min(zc * a.f + a.f, a.inz); ++z)
+    for (int y = yc * a.f; y < min(yc * a.f + a.f, a.iny); ++y)
+      for (int x = xc * a.f; x < min(xc * a.f + a.f, a.inx); ++x) {
+        s += a.p[fine_index(a, b, z, y, x)];
+        ++cnt;
+      }
+  out[i] = s / (float)cnt * a.pscale;
+}
+
+// Coarse prediction (FP32, one value per coarse cell) -> fine p: trilinear
+// from coarse centres at (c + 0.5) f - 0.5, clamped, divided by pscale,
+// times bnd.  Writes every fine cell of every instance.
+__global__ void upsample_kernel(PoolArgs a, const float *__restrict__ coarse,
+                                float *__restrict__ p) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = (long long)a.batch * a.inz * a.iny * a.inx;
+  if (i >= n) return;
+  const int x = (int)(i % a.inx), y = (int)((i / a.inx) % a.iny);
+  const int z = (int)((i / ((long long)a.inx * a.iny)) % a.inz);
+  const int b = (int)(i / ((long long)a.inx * a.iny * a.inz));
+  auto axis = [&](int j, int nc, int &i0, int &i1, float &t) {
+    float pos = ((float)j + 0.5f) / (float)a.f - 0.5f;
+    pos = fminf(fmaxf(pos, 0.f), (float)(nc - 1));
+    i0 = (int)floorf(pos);
+    i1 = min(i0 + 1, nc - 1);
+    t = pos - (float)i0;
+  };
+  int z0, z1, y0, y1, x0, x1;
+  float tz, ty, tx;
+  axis(z, a.zc, z0, z1, tz);
+  axis(y, a.yc, y0, y1, ty);
+  axis(x, a.xc, x0, x1, tx);
+  const float *c = coarse + (long long)b * a.zc * a.yc * a.xc;
+  auto at = [&](int zz, int yy, int xx) { return c[((long long)zz * a.yc + yy) * a.xc + xx]; };
+  // interpolate x, then y, then z (the oracle's axis order is z, y, x;
+  // trilinear interpolation is the same up to rounding)
+  const float c00 = at(z0, y0, x0) * (1.f - tx) + at(z0, y0, x1) * tx;
+  const float c01 = at(z0, y1, x0) * (1.f - tx) + at(z0, y1, x1) * tx;
+  const float c10 = at(z1, y0, x0) * (1.f - tx) + at(z1, y0, x1) * tx;
+  const float c11 = at(z1, y1, x0) * (1.f - tx) + at(z1, y1, x1) * tx;
+  const float c0 = c00 * (1.f - ty) + c01 * ty, c1 = c10 * (1.f - ty) + c11 * ty;
+  const float v = (c0 * (1.f - tz) + c1 * tz) / a.pscale;
+  const long long k = fine_index(a, b, z, y, x);
+  p[k] = v * a.bnd[k];
+}
+
+}  // namespace
+
+int nn_conv(const void *x, const void *w, const float *bias, const void *mask, int relu,
+            void *y, float *yf, int B, int Z, int Y, int X, cudaStream_t s) {
+  Dims d{B, Z, Y, X, (long long)B * Z * Y * X};
+  if (d.nvox <= 0) return 0;
+  const long long blocks = (d.nvox + 16 * kConvWarps - 1) / (16 * kConvWarps);
+  conv_kernel<<<(unsigned)blocks, 32 * kConvWarps, 0, s>>>(
+      static_cast<const __nv_bfloat16 *>(x), static_cast<const __nv_bfloat16 *>(w), bias,
+      static_cast<const __nv_bfloat16 *>(mask), relu, static_cast<__nv_bfloat16 *>(y), yf, d);
+  return (int)cudaGetLastError();
+}
+
+int nn_wgrad(const void *x, const void *dy, float *part, int S, float *dw, float *db, int B,
+             int Z, int Y, int X, cudaStream_t s) {
+  Dims d{B, Z, Y, X, (long long)B * Z * Y * X};
+  if (S < 1) return -1;
+  float *bpart = part + (long long)S * kTaps * kC * kC;
+  wgrad_kernel<<<dim3(kTaps, S), 32 * kConvWarps, 0, s>>>(
+      static_cast<const __nv_bfloat16 *>(x), static_cast<const __nv_bfloat16 *>(dy), part, bpart,
+      d);
+  const int n = kTaps * kC * kC + kC;
+  wgrad_reduce_kernel<<<(n + 255) / 256, 256, 0, s>>>(part, bpart, S, dw, db);
+  return (int)cudaGetLastError();
+}
+
+int nn_prep_weights(const float *w, void *wf, void *wb, cudaStream_t s) {
+  prep_weights_kernel<<<(kTaps * kC * kC + 255) / 256, 256, 0, s>>>(
+      w, static_cast<__nv_bfloat16 *>(wf), static_cast<__nv_bfloat16 *>(wb));
+  return (int)cudaGetLastError();
+}
+
+int nn_adam(float *w, const float *g, float *m, float *v, long long n, float lr, float b1,
+            float b2, float eps, int step, cudaStream_t s) {
+  if (n <= 0 || step < 1) return -1;
+  const float c1 = (float)(1.0 / (1.0 - pow((double)b1, step)));
+  const float c2 = (float)(1.0 / (1.0 - pow((double)b2, step)));
+  adam_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(w, g, m, v, n, lr, b1, b2, eps, c1, c2);
+  return (int)cudaGetLastError();
+}
+
+int nn_mse(const float *pred, const float *tgt, long long n, void *dy, double *part,
+           cudaStream_t s) {
+  if (n <= 0) return -1;
+  mse_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(pred, tgt, n,
+                                                         static_cast<__nv_bfloat16 *>(dy), part);
+  return (int)cudaGetLastError();
+}
+
+static PoolArgs pool_args(const NNFields &f) {
+  PoolArgs a;
+  a.a0 = f.a0;
+  a.a1 = f.a1;
+  a.a2 = f.a2;
+  a.wrk1 = f.wrk1;
+  a.bnd = f.bnd;
+  a.p = f.p;
+  a.pitch_e = f.pitch / 4;
+  a.ny = f.ny;
+  a.inx = f.inx;
+  a.iny = f.iny;
+  a.inz = f.inz;
+  a.nsx = f.nsx;
+  a.f = f.factor;
+  a.zc = (f.inz + f.factor - 1) / f.factor;
+  a.yc = (f.iny + f.factor - 1) / f.factor;
+  a.xc = (f.inx + f.factor - 1) / f.factor;
+  a.batch = f.batch;
+  a.wscale = f.wscale;
+  a.pscale = f.pscale;
+  return a;
+}
+
+int nn_pool_inputs(const NNFields &f, void *out, cudaStream_t s) {
+  const PoolArgs a = pool_args(f);
+  const long long n = (long long)a.batch * a.zc * a.yc * a.xc;
+  if (n <= 0) return -1;
+  pool_inputs_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(
+      a, static_cast<__nv_bfloat16 *>(out));
+  return (int)cudaGetLastError();
+}
+
+int nn_pool_target(const NNFields &f, float *out, cudaStream_t s) {
+  const PoolArgs a = pool_args(f);
+  const long long n = (long long)a.batch * a.zc * a.yc * a.xc;
+  if (n <= 0 || !a.p) return -1;
+  pool_target_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a, out);
+  return (int)cudaGetLastError();
+}
+
+int nn_upsample(const NNFields &f, const float *coarse, float *p, cudaStream_t s) {
+  const PoolArgs a = pool_args(f);
+  const long long n = (long long)a.batch * a.inz * a.iny * a.inx;
+  if (n <= 0) return -1;
+  upsample_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, coarse, p);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace psg

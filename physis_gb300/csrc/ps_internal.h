@@ -188,6 +188,32 @@ bool jit_prepare(void *fn, int threads, size_t smem, int *occ);
 cudaError_t jit_launch_raw(void *fn, int grid, dim3 block, size_t smem, cudaStream_t s,
                            void **args);
 
+// ---- Learned warm start (nn.cu) -------------------------------------------
+// Fine stacked grids of a batch of Himeno instances (float, row pitch
+// `pitch` bytes, ny rows per plane): instance b at fine origin
+// ((b % nsx) * inx, 0, (b / nsx) * inz), size inx x iny x inz; coarse cells
+// are factor^3 blocks.
+struct NNFields {
+  const float *a0, *a1, *a2, *wrk1, *bnd, *p;
+  long long pitch;
+  int ny;
+  int inx, iny, inz, nsx, factor, batch;
+  float wscale, pscale;
+};
+// Each returns 0, -1 for invalid arguments, or the launch's cudaError_t.
+int nn_conv(const void *x, const void *w, const float *bias, const void *mask, int relu,
+            void *y, float *yf, int B, int Z, int Y, int X, cudaStream_t s);
+int nn_wgrad(const void *x, const void *dy, float *part, int S, float *dw, float *db, int B,
+             int Z, int Y, int X, cudaStream_t s);
+int nn_prep_weights(const float *w, void *wf, void *wb, cudaStream_t s);
+int nn_adam(float *w, const float *g, float *m, float *v, long long n, float lr, float b1,
+            float b2, float eps, int step, cudaStream_t s);
+int nn_mse(const float *pred, const float *tgt, long long n, void *dy, double *part,
+           cudaStream_t s);
+int nn_pool_inputs(const NNFields &f, void *out, cudaStream_t s);
+int nn_pool_target(const NNFields &f, float *out, cudaStream_t s);
+int nn_upsample(const NNFields &f, const float *coarse, float *p, cudaStream_t s);
+
 // ---- Reductions (reduce.cu) ----------------------------------------------
 // Reduces every element of g with op.  The 8-byte result is written to
 // *result: FP64 for float and double grids, int64 for int (wrapped to 32

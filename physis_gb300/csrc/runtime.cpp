@@ -2130,6 +2130,110 @@ void PSGetLaunchShape(int kernel, PSLaunchShape *shape) {
   shape->ctas_per_sm = c.ctas_per_sm;
 }
 
+static cudaStream_t ws_stream(void *stream) {
+  if (stream) return static_cast<cudaStream_t>(stream);
+  return rt ? rt->stream : nullptr;
+}
+
+// rc: 0, -1 (invalid arguments) or a cudaError_t from the launch.
+static int ws_status(int rc, const char *what) {
+  if (rc == 0) return PS_OK;
+  if (rc > 0) {
+    fail(PS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(static_cast<cudaError_t>(rc)));
+    return PS_ERR_CUDA;
+  }
+  fail(PS_ERR_INVALID_ARGUMENT, "%s: invalid arguments", what);
+  return PS_ERR_INVALID_ARGUMENT;
+}
+
+static psg::NNFields ws_fields(const PSWarmStartFields *f) {
+  psg::NNFields n;
+  n.a0 = f->a0;
+  n.a1 = f->a1;
+  n.a2 = f->a2;
+  n.wrk1 = f->wrk1;
+  n.bnd = f->bnd;
+  n.p = f->p;
+  n.pitch = f->pitch;
+  n.ny = f->ny;
+  n.inx = f->inx;
+  n.iny = f->iny;
+  n.inz = f->inz;
+  n.nsx = f->nsx;
+  n.factor = f->factor;
+  n.batch = f->batch;
+  n.wscale = f->wscale;
+  n.pscale = f->pscale;
+  return n;
+}
+
+static bool ws_fields_ok(const PSWarmStartFields *f, const char *what, bool need_p) {
+  if (!f || !f->a0 || !f->a1 || !f->a2 || !f->wrk1 || !f->bnd || (need_p && !f->p) ||
+      f->pitch <= 0 || f->pitch % 4 || f->inx < 1 || f->iny < 1 || f->inz < 1 || f->nsx < 1 ||
+      f->factor < 1 || f->batch < 1 || f->ny < f->iny || f->pitch / 4 < (long long)f->inx) {
+    fail(PS_ERR_INVALID_ARGUMENT, "%s: bad field description", what);
+    return false;
+  }
+  return true;
+}
+
+int PSWarmStartConv(const void *x, const void *w, const float *bias, const void *mask, int relu,
+                    void *y, float *y_ch0, int batch, int nz, int ny, int nx, void *stream) {
+  if (!x || !w || !y || batch < 1 || nz < 1 || ny < 1 || nx < 1)
+    return ws_status(-1, "PSWarmStartConv");
+  return ws_status(psg::nn_conv(x, w, bias, mask, relu, y, y_ch0, batch, nz, ny, nx,
+                                ws_stream(stream)),
+                   "PSWarmStartConv");
+}
+
+int PSWarmStartWeightGrad(const void *x, const void *dy, float *work, int nsplit, float *dw,
+                          float *db, int batch, int nz, int ny, int nx, void *stream) {
+  if (!x || !dy || !work || !dw || nsplit < 1 || nsplit > 65535 || batch < 1 || nz < 1 ||
+      ny < 1 || nx < 1)
+    return ws_status(-1, "PSWarmStartWeightGrad");
+  return ws_status(psg::nn_wgrad(x, dy, work, nsplit, dw, db, batch, nz, ny, nx,
+                                 ws_stream(stream)),
+                   "PSWarmStartWeightGrad");
+}
+
+int PSWarmStartPrepareWeights(const float *w, void *w_fwd, void *w_bwd, void *stream) {
+  if (!w || !w_fwd || !w_bwd) return ws_status(-1, "PSWarmStartPrepareWeights");
+  return ws_status(psg::nn_prep_weights(w, w_fwd, w_bwd, ws_stream(stream)),
+                   "PSWarmStartPrepareWeights");
+}
+
+int PSWarmStartAdam(float *w, const float *g, float *m, float *v, long long n, float lr, float b1,
+                    float b2, float eps, int step, void *stream) {
+  if (!w || !g || !m || !v) return ws_status(-1, "PSWarmStartAdam");
+  return ws_status(psg::nn_adam(w, g, m, v, n, lr, b1, b2, eps, step, ws_stream(stream)),
+                   "PSWarmStartAdam");
+}
+
+int PSWarmStartLoss(const float *pred, const float *target, long long n, void *dy,
+                    double *partials, void *stream) {
+  if (!pred || !target || !dy || !partials) return ws_status(-1, "PSWarmStartLoss");
+  return ws_status(psg::nn_mse(pred, target, n, dy, partials, ws_stream(stream)),
+                   "PSWarmStartLoss");
+}
+
+int PSWarmStartPool(const PSWarmStartFields *f, void *out, void *stream) {
+  if (!ws_fields_ok(f, "PSWarmStartPool", false) || !out) return PS_ERR_INVALID_ARGUMENT;
+  return ws_status(psg::nn_pool_inputs(ws_fields(f), out, ws_stream(stream)), "PSWarmStartPool");
+}
+
+int PSWarmStartPoolTarget(const PSWarmStartFields *f, float *out, void *stream) {
+  if (!ws_fields_ok(f, "PSWarmStartPoolTarget", true) || !out) return PS_ERR_INVALID_ARGUMENT;
+  return ws_status(psg::nn_pool_target(ws_fields(f), out, ws_stream(stream)),
+                   "PSWarmStartPoolTarget");
+}
+
+int PSWarmStartUpsample(const PSWarmStartFields *f, const float *coarse, float *p, void *stream) {
+  if (!ws_fields_ok(f, "PSWarmStartUpsample", false) || !coarse || !p)
+    return PS_ERR_INVALID_ARGUMENT;
+  return ws_status(psg::nn_upsample(ws_fields(f), coarse, p, ws_stream(stream)),
+                   "PSWarmStartUpsample");
+}
+
 int PSReduceNoAlloc(const void *data, size_t pitch, int nx, int ny, int nz, int type,
                     int op, void *result, void *stream) {
   const char *why = "";

@@ -1,0 +1,413 @@
+"""Learned warm start for the 19-point Jacobi (Himeno) pressure-Poisson solve.
+
+No counterpart in the reference.  A small 3D convolutional network predicts
+the solution of a variable-coefficient Jacobi solve from its coefficient and
+source fields; Jacobi then iterates from that prediction to the same
+residual tolerance, so the plain zero-start solve stays both the fallback
+and the judge (a bad prediction costs sweeps, it cannot change the answer).
+
+Pieces, all on the GPU through libphysis_gb300's C ABI:
+* instances (seeded, built on the host): coefficients a0, a1, a2 log-uniform
+  in [0.5, 2] smoothed by a Gaussian of sigma 4 cells (then stretched back to
+  [0.5, 2]); c_i = a_i; a3 = 1 / (2 (a0 + a1 + a2)); b = 0; source wrk1 = 8
+  Gaussian blobs (centres uniform, widths U[3, 12] cells, amplitudes N(0, 1));
+  bnd = 1 inside, 0 on the faces (Dirichlet zero); omega = 0.8;
+* targets: the library's own Himeno sweeps (PS_KERNEL_HIMENO19) run to a
+  relative residual of 1e-7, many instances at once in one stacked grid
+  (instances side by side in x and z; their bnd = 0 faces keep them apart),
+  the per-instance residual read with PSReduce's kernel form;
+* the network: pool the fine fields to factor^3 blocks, 6 conv layers 3x3x3 x
+  16 channels (ReLU between), BF16 weights and activations, FP32
+  accumulation (PSWarmStartConv on tensor cores), trained with MSE and Adam
+  (PSWarmStartWeightGrad, PSWarmStartLoss, PSWarmStartAdam); the coarse
+  prediction is upsampled trilinearly to the fine grid (PSWarmStartUpsample).
+
+Relative residual: ||ss|| / ||ss(p = 0)|| with ss = (s0 a3 - p) bnd, the
+Himeno residual (examples/himeno/himenobmtxpa_original.c:331-334).
+PyTorch provides device buffers and copies only; every computation is one of
+the library's kernels.
+"""
+import ctypes
+import math
+import time
+
+import numpy as np
+
+import physis_gb300 as ps
+
+OMEGA = 0.8
+C = 16
+LAYERS = 6
+
+
+# ---- instances ----------------------------------------------------------------
+
+def _gaussian_smooth(u, sigma):
+    """Separable Gaussian filter (truncated at 3 sigma, reflected edges)."""
+    r = int(math.ceil(3 * sigma))
+    k = np.exp(-0.5 * (np.arange(-r, r + 1) / sigma) ** 2)
+    k /= k.sum()
+    out = u
+    for axis in range(3):
+        pad = [(0, 0)] * 3
+        pad[axis] = (r, r)
+        p = np.pad(out, pad, mode="reflect")
+        acc = np.zeros_like(out)
+        for i, w in enumerate(k):
+            sl = [slice(None)] * 3
+            sl[axis] = slice(i, i + out.shape[axis])
+            acc += w * p[tuple(sl)]
+        out = acc
+    return out
+
+
+def make_instance(rng, shape):
+    """One seeded instance: dict of float32 fields shaped (nz, ny, nx)."""
+    lo, hi = math.log(0.5), math.log(2.0)
+    f = {}
+    for name in ("a0", "a1", "a2"):
+        s = _gaussian_smooth(rng.uniform(lo, hi, size=shape), 4.0)
+        s = (s - s.min()) / max(s.max() - s.min(), 1e-12) * (hi - lo) + lo
+        f[name] = np.exp(s).astype(np.float32)
+    nz, ny, nx = shape
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    w = np.zeros(shape)
+    for _ in range(8):
+        cz, cy, cx = rng.uniform(0, nz), rng.uniform(0, ny), rng.uniform(0, nx)
+        width = rng.uniform(3.0, 12.0)
+        amp = rng.normal()
+        w += amp * np.exp(-((z - cz) ** 2 + (y - cy) ** 2 + (x - cx) ** 2) / (2 * width ** 2))
+    f["wrk1"] = w.astype(np.float32)
+    bnd = np.zeros(shape, np.float32)
+    bnd[1:-1, 1:-1, 1:-1] = 1.0
+    f["bnd"] = bnd
+    return f
+
+
+def himeno_arrays(inst):
+    """The 12 coefficient/source arrays of PS_KERNEL_HIMENO19, in map order
+    (a0 a1 a2 a3 b0 b1 b2 c0 c1 c2 bnd wrk1)."""
+    a0, a1, a2 = inst["a0"], inst["a1"], inst["a2"]
+    a3 = (1.0 / (2.0 * (a0.astype(np.float64) + a1 + a2))).astype(np.float32)
+    z = np.zeros_like(a0)
+    return [a0, a1, a2, a3, z, z, z, a0, a1, a2, inst["bnd"], inst["wrk1"]]
+
+
+def residual0(inst):
+    """||ss(p = 0)||^2 = sum (wrk1 a3 bnd)^2 in FP64."""
+    arr = himeno_arrays(inst)
+    ss = arr[11].astype(np.float64) * arr[3] * arr[10]
+    return float((ss * ss).sum())
+
+
+# ---- stacked solves -------------------------------------------------------------
+
+class Stack:
+    """Up to nsx * nsz instances side by side in x and z of one set of
+    Himeno grids; unused slots have bnd = 0 (nothing moves there)."""
+
+    def __init__(self, instances, shape, nsx):
+        self.shape = shape
+        nz, ny, nx = shape
+        self.count = len(instances)
+        self.nsx = nsx
+        self.nsz = -(-self.count // nsx)
+        gshape = (self.nsz * nz, ny, nsx * nx)
+        host = [np.zeros(gshape, np.float32) for _ in range(12)]
+        ones = np.ones(shape, np.float32)
+        self.r0 = []
+        for b in range(self.nsx * self.nsz):
+            sl = self.slot(b)
+            if b < self.count:
+                arrs = himeno_arrays(instances[b])
+                self.r0.append(residual0(instances[b]))
+            else:
+                z = np.zeros(shape, np.float32)
+                arrs = [ones, ones, ones, ones * 0.1, z, z, z, ones, ones, ones, z, z]
+            for h, a in zip(host, arrs):
+                h[sl] = a
+        self.grids = [ps.Grid(gshape) for _ in range(14)]  # p0 p1 + 12
+        zero = np.zeros(gshape, np.float32)
+        self.grids[0].copyin(zero)
+        self.grids[1].copyin(zero)
+        for g, h in zip(self.grids[2:], host):
+            g.copyin(h)
+        self.scratch = ps.Grid(gshape)
+        self.gshape = gshape
+        self.inner = ps.domain(1, gshape[2] - 1, 1, gshape[1] - 1, 1, gshape[0] - 1)
+        order = [0, 1] + list(range(2, 14))
+        self.m1 = ps.stencil_map(ps.PS_KERNEL_HIMENO19, self.inner,
+                                 [self.grids[i] for i in order], [OMEGA])
+        order2 = [1, 0] + list(range(2, 14))
+        self.m2 = ps.stencil_map(ps.PS_KERNEL_HIMENO19, self.inner,
+                                 [self.grids[i] for i in order2], [OMEGA])
+
+    def slot(self, b):
+        nz, ny, nx = self.shape
+        ix, iz = b % self.nsx, b // self.nsx
+        return (slice(iz * nz, (iz + 1) * nz), slice(0, ny), slice(ix * nx, (ix + 1) * nx))
+
+    def set_p(self, p=None):
+        """p0 = p (a device grid's contents already written) or zeros."""
+        if p is None:
+            self.grids[0].copyin(np.zeros(self.gshape, np.float32))
+
+    def sweeps(self, n):
+        """n sweeps (n even: the result is back in p0)."""
+        assert n % 2 == 0
+        if n:
+            ps.stencil_run([self.m1, self.m2], n // 2)
+
+    def residuals(self):
+        """Relative residual of every instance (p in p0): one kernel-form
+        PSReduce over the instance's interior, into a scratch grid."""
+        nz, ny, nx = self.shape
+        out = []
+        grids = [self.grids[0], self.scratch] + self.grids[2:]
+        for b in range(self.count):
+            ix, iz = b % self.nsx, b // self.nsx
+            dom = ps.domain(ix * nx + 1, (ix + 1) * nx - 1, 1, ny - 1,
+                            iz * nz + 1, (iz + 1) * nz - 1)
+            g = ps.reduce_kernel(ps.PS_SUM, ps.PS_KERNEL_HIMENO19_GOSA, dom, grids, [OMEGA])
+            out.append(math.sqrt(max(float(g), 0.0) / self.r0[b]))
+        return np.array(out)
+
+    def solve(self, tol, chunk, max_sweeps):
+        """Sweeps (a multiple of `chunk`) after which each instance first
+        met `tol`; -1 if it did not within max_sweeps."""
+        done = np.full(self.count, -1)
+        n = 0
+        while n < max_sweeps and (done < 0).any():
+            self.sweeps(chunk)
+            n += chunk
+            r = self.residuals()
+            done[(done < 0) & (r <= tol)] = n
+        return done
+
+    def fields(self, factor, wscale=1.0, pscale=1.0, with_p=False):
+        """PSWarmStartFields describing this stack for the pooling kernels."""
+        f = ps.PSWarmStartFields()
+        g = self.grids
+        f.a0, f.a1, f.a2 = g[2].dev_ptr, g[3].dev_ptr, g[4].dev_ptr
+        f.wrk1, f.bnd = g[13].dev_ptr, g[12].dev_ptr
+        f.p = g[0].dev_ptr if with_p else None
+        f.pitch = g[0].pitch
+        f.ny = self.gshape[1]
+        f.inz, f.iny, f.inx = self.shape
+        f.nsx = self.nsx
+        f.factor = factor
+        f.batch = self.count
+        f.wscale, f.pscale = wscale, pscale
+        return f
+
+    def free(self):
+        for g in self.grids + [self.scratch]:
+            g.free()
+
+
+def coarse_shape(shape, factor):
+    return tuple(-(-n // factor) for n in shape)
+
+
+# ---- the network --------------------------------------------------------------
+
+class Net:
+    """6 conv layers 3x3x3 x 16 channels, ReLU between, on the coarse grid.
+    FP32 master weights and Adam moments; BF16 copies for the kernels."""
+
+    def __init__(self, seed=0):
+        import torch
+        self.torch = torch
+        dev = "cuda"
+        rng = np.random.default_rng(seed)
+        self.w, self.b = [], []
+        for l in range(LAYERS):
+            fan_in = 27 * (5 if l == 0 else C)
+            std = math.sqrt(2.0 / fan_in) if l < LAYERS - 1 else 0.1 * math.sqrt(1.0 / fan_in)
+            w = rng.normal(0, std, size=(27, C, C)).astype(np.float32)
+            if l == 0:
+                w[:, 5:, :] = 0.0
+            self.w.append(torch.tensor(w, device=dev))
+            self.b.append(torch.zeros(C, device=dev))
+        self.params = self.w + self.b
+        self.grads = [torch.zeros_like(p) for p in self.params]
+        self.m = [torch.zeros_like(p) for p in self.params]
+        self.v = [torch.zeros_like(p) for p in self.params]
+        self.wf = [torch.empty(27 * C * C, dtype=torch.bfloat16, device=dev) for _ in range(LAYERS)]
+        self.wb = [torch.empty(27 * C * C, dtype=torch.bfloat16, device=dev) for _ in range(LAYERS)]
+        self.step = 0
+        self._acts = None
+        self.prepare()
+
+    def stream(self):
+        return ctypes.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+
+    def prepare(self):
+        L = ps.lib()
+        for l in range(LAYERS):
+            _ok(L.PSWarmStartPrepareWeights(_p(self.w[l]), _p(self.wf[l]), _p(self.wb[l]),
+                                            self.stream()))
+
+    def forward(self, x, dims):
+        """x: BF16 tensor [B*Z*Y*X*16]; returns the FP32 channel-0 output."""
+        torch = self.torch
+        B, Z, Y, X = dims
+        n = B * Z * Y * X
+        L = ps.lib()
+        acts = [x]
+        out0 = torch.empty(n, dtype=torch.float32, device="cuda")
+        for l in range(LAYERS):
+            y = torch.empty(n * C, dtype=torch.bfloat16, device="cuda")
+            last = l == LAYERS - 1
+            _ok(L.PSWarmStartConv(_p(acts[-1]), _p(self.wf[l]), _p(self.b[l]), None,
+                                  0 if last else 1, _p(y), _p(out0) if last else None,
+                                  B, Z, Y, X, self.stream()))
+            acts.append(y)
+        self._acts = acts
+        return out0
+
+    def backward(self, dy, dims, work):
+        """Gradients of every parameter from dL/d(output) (BF16, [n*16])."""
+        torch = self.torch
+        B, Z, Y, X = dims
+        n = B * Z * Y * X
+        L = ps.lib()
+        nsplit = work.numel() // (27 * C * C + C)
+        g = dy
+        for l in range(LAYERS - 1, -1, -1):
+            _ok(L.PSWarmStartWeightGrad(_p(self._acts[l]), _p(g), _p(work), nsplit,
+                                        _p(self.grads[l]), _p(self.grads[LAYERS + l]),
+                                        B, Z, Y, X, self.stream()))
+            if l:
+                dx = torch.empty(n * C, dtype=torch.bfloat16, device="cuda")
+                _ok(L.PSWarmStartConv(_p(g), _p(self.wb[l]), None, _p(self._acts[l]), 0,
+                                      _p(dx), None, B, Z, Y, X, self.stream()))
+                g = dx
+
+    def adam(self, lr, b1=0.9, b2=0.999, eps=1e-8):
+        self.step += 1
+        L = ps.lib()
+        for p, g, m, v in zip(self.params, self.grads, self.m, self.v):
+            _ok(L.PSWarmStartAdam(_p(p), _p(g), _p(m), _p(v), p.numel(), ctypes.c_float(lr),
+                                  ctypes.c_float(b1), ctypes.c_float(b2), ctypes.c_float(eps),
+                                  self.step, self.stream()))
+        self.prepare()
+
+
+def _p(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _ok(code):
+    if code != 0:
+        ps.check()
+        raise ps.PSError(code, "warm-start call failed")
+
+
+def loss_grad(pred, target, work64):
+    """MSE of pred vs target (both FP32 [n]) and dL/dpred as BF16 [n*16]."""
+    import torch
+    n = pred.numel()
+    dy = torch.empty(n * C, dtype=torch.bfloat16, device="cuda")
+    _ok(ps.lib().PSWarmStartLoss(_p(pred), _p(target), n, _p(dy), _p(work64),
+                                 ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    nb = (n + 255) // 256
+    return float(work64[:nb].cpu().numpy().sum()) / n, dy
+
+
+# ---- data, training, evaluation -------------------------------------------------
+
+class Dataset:
+    """Pooled inputs and targets of many instances, resident on the GPU."""
+
+    def __init__(self, rng, count, shape, factor, nsx=15, per_stack=300, tol=1e-7,
+                 chunk=256, max_sweeps=40000, wscale=None, pscale=None, log=None):
+        import torch
+        self.shape, self.factor = shape, factor
+        zc, yc, xc = coarse_shape(shape, factor)
+        self.dims1 = (zc, yc, xc)
+        self.x = torch.empty((count, zc, yc, xc, C), dtype=torch.bfloat16, device="cuda")
+        self.t = torch.empty((count, zc, yc, xc), dtype=torch.float32, device="cuda")
+        self.sweeps = np.zeros(count, int)
+        self.wscale, self.pscale = wscale, pscale
+        self.solve_seconds = 0.0
+        L = ps.lib()
+        done = 0
+        while done < count:
+            k = min(per_stack, count - done)
+            insts = [make_instance(rng, shape) for _ in range(k)]
+            if self.wscale is None:
+                self.wscale = 1.0 / float(np.std(np.concatenate([i["wrk1"].ravel() for i in insts])))
+            st = Stack(insts, shape, nsx)
+            ps.synchronize()
+            t0 = time.perf_counter()
+            self.sweeps[done:done + k] = st.solve(tol, chunk, max_sweeps)
+            ps.synchronize()
+            self.solve_seconds += time.perf_counter() - t0
+            if self.pscale is None:
+                tmp = torch.empty((k, zc, yc, xc), dtype=torch.float32, device="cuda")
+                _ok(L.PSWarmStartPoolTarget(ctypes.byref(st.fields(factor, 1.0, 1.0, True)),
+                                            _p(tmp), None))
+                ps.synchronize()
+                self.pscale = 1.0 / float(np.std(tmp.cpu().numpy().astype(np.float64)))
+            f = st.fields(factor, self.wscale, self.pscale, True)
+            _ok(L.PSWarmStartPool(ctypes.byref(f), _p(self.x[done:done + k]), None))
+            _ok(L.PSWarmStartPoolTarget(ctypes.byref(f), _p(self.t[done:done + k]), None))
+            ps.synchronize()
+            st.free()
+            done += k
+            if log:
+                log(f"solved {done}/{count} instances")
+
+
+def train(net, data, epochs, batch, lr, log=None, seed=0):
+    import torch
+    count = data.x.shape[0]
+    zc, yc, xc = data.dims1
+    nvox = batch * zc * yc * xc
+    nsplit = 64
+    work = torch.empty(nsplit * (27 * C * C + C), dtype=torch.float32, device="cuda")
+    work64 = torch.empty((nvox + 255) // 256, dtype=torch.float64, device="cuda")
+    rng = np.random.default_rng(seed)
+    history = []
+    steps = epochs * (count // batch)
+    s = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for e in range(epochs):
+        order = rng.permutation(count)
+        tot = 0.0
+        for i in range(count // batch):
+            idx = torch.as_tensor(order[i * batch:(i + 1) * batch], device="cuda")
+            x = data.x.index_select(0, idx).reshape(-1)
+            t = data.t.index_select(0, idx).reshape(-1)
+            pred = net.forward(x, (batch, zc, yc, xc))
+            loss, dy = loss_grad(pred, t, work64)
+            net.backward(dy, (batch, zc, yc, xc), work)
+            rate = lr * 0.5 * (1 + math.cos(math.pi * s / max(steps, 1)))
+            net.adam(rate)
+            tot += loss
+            s += 1
+        history.append(tot / max(count // batch, 1))
+        if log:
+            log(f"epoch {e}: loss {history[-1]:.5f}")
+    torch.cuda.synchronize()
+    return history, time.perf_counter() - t0
+
+
+def predict_into(net, stack, data_scales, factor):
+    """Warm start: pool the stack's fields, run the network, upsample into
+    the stack's p0 (p1 too, so the first sweep starts from it)."""
+    import torch
+    wscale, pscale = data_scales
+    zc, yc, xc = coarse_shape(stack.shape, factor)
+    n = stack.count
+    L = ps.lib()
+    f = stack.fields(factor, wscale, pscale)
+    x = torch.empty(n * zc * yc * xc * C, dtype=torch.bfloat16, device="cuda")
+    _ok(L.PSWarmStartPool(ctypes.byref(f), _p(x), net.stream()))
+    pred = net.forward(x, (n, zc, yc, xc))
+    for g in (stack.grids[0], stack.grids[1]):
+        _ok(L.PSWarmStartUpsample(ctypes.byref(f), _p(pred), ctypes.c_void_p(g.dev_ptr),
+                                  net.stream()))
+    torch.cuda.synchronize()

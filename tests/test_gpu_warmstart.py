@@ -1,0 +1,266 @@
+"""The learned warm start on the GPU.
+
+* each kernel (convolution forward, backward-data with the ReLU mask, weight
+  and bias gradients, MSE gradient, Adam, pooling, upsampling) against the
+  FP64 oracle in oracle/nn_oracle.py: BF16 outputs within one BF16 rounding
+  step of the oracle's value, FP32 outputs within 1e-5 relative;
+* a network gradient check: one backward pass of the 6-layer network
+  against the oracle's backprop;
+* the gain: a network trained on the GPU on solved instances makes the
+  Jacobi solve of held-out instances reach 1e-6 in fewer sweeps than the
+  zero start, and both end at the same tolerance.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import physis_gb300 as ps
+from oracle import nn_oracle as nn
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def rt():
+    ps.build()
+    ps.init()
+    yield ps
+    ps.clear_error()
+
+
+def _bf(a):
+    """numpy float -> BF16 torch tensor on the GPU (flattened)."""
+    return torch.tensor(nn.to_bf16(a).view(np.int16).ravel(), device="cuda").view(torch.bfloat16)
+
+
+def _np_bf(t, shape):
+    return nn.from_bf16(t.view(torch.int16).cpu().numpy().view(np.uint16)).reshape(shape)
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _weights(rng, scale=0.2):
+    w = rng.normal(0, scale, size=(27, 16, 16)).astype(np.float32)
+    return nn.from_bf16(nn.to_bf16(w)).astype(np.float32)  # BF16-exact masters
+
+
+def _prep(w):
+    wt = torch.tensor(w.ravel(), device="cuda")
+    wf = torch.empty(27 * 256, dtype=torch.bfloat16, device="cuda")
+    wb = torch.empty(27 * 256, dtype=torch.bfloat16, device="cuda")
+    assert ps.lib().PSWarmStartPrepareWeights(_p(wt), _p(wf), _p(wb), _stream()) == 0
+    return wf, wb
+
+
+def _within_one_bf16_step(got, ref):
+    """|got - ref| <= one BF16 ulp of ref (FP32 accumulation order differs
+    from the FP64 oracle, so a value near a rounding tie may round the other
+    way)."""
+    ulp = np.maximum(np.abs(ref), 1e-30) * 2.0 ** -7
+    return np.all(np.abs(got - ref) <= ulp + 1e-30)
+
+
+DIMS = [(2, 5, 4, 7), (1, 3, 9, 2), (3, 17, 9, 9)]
+
+
+@pytest.mark.parametrize("dims", DIMS)
+def test_conv_forward(rt, dims):
+    rng = np.random.default_rng(1)
+    x = nn.from_bf16(nn.to_bf16(rng.normal(size=dims + (16,))))
+    w = _weights(rng)
+    bias = rng.normal(0, 0.1, 16).astype(np.float32)
+    wf, _ = _prep(w)
+    n = int(np.prod(dims))
+    y = torch.empty(n * 16, dtype=torch.bfloat16, device="cuda")
+    y0 = torch.empty(n, dtype=torch.float32, device="cuda")
+    bt = torch.tensor(bias, device="cuda")
+    for relu in (1, 0):
+        rc = ps.lib().PSWarmStartConv(_p(_bf(x)), _p(wf), _p(bt), None, relu, _p(y), _p(y0),
+                                      *dims, _stream())
+        assert rc == 0
+        ref = nn.conv_fwd(x, w, bias)
+        if relu:
+            ref = nn.relu(ref)
+        got = _np_bf(y, dims + (16,))
+        assert _within_one_bf16_step(got, ref)
+        assert np.allclose(y0.cpu().numpy().reshape(dims), ref[..., 0], rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("dims", DIMS)
+def test_conv_backward_data_with_mask(rt, dims):
+    rng = np.random.default_rng(2)
+    dy = nn.from_bf16(nn.to_bf16(rng.normal(size=dims + (16,))))
+    mask = nn.from_bf16(nn.to_bf16(rng.normal(size=dims + (16,))))
+    w = _weights(rng)
+    _, wb = _prep(w)
+    n = int(np.prod(dims))
+    dx = torch.empty(n * 16, dtype=torch.bfloat16, device="cuda")
+    rc = ps.lib().PSWarmStartConv(_p(_bf(dy)), _p(wb), None, _p(_bf(mask)), 0, _p(dx), None,
+                                  *dims, _stream())
+    assert rc == 0
+    ref = nn.conv_bwd_data(dy, w) * (mask > 0)
+    assert _within_one_bf16_step(_np_bf(dx, dims + (16,)), ref)
+
+
+@pytest.mark.parametrize("dims,nsplit", [((2, 5, 4, 7), 3), ((3, 17, 9, 9), 16),
+                                          ((1, 1, 1, 5), 1)])
+def test_weight_and_bias_gradients(rt, dims, nsplit):
+    rng = np.random.default_rng(3)
+    x = nn.from_bf16(nn.to_bf16(rng.normal(size=dims + (16,))))
+    dy = nn.from_bf16(nn.to_bf16(rng.normal(size=dims + (16,))))
+    work = torch.empty(nsplit * (27 * 256 + 16), dtype=torch.float32, device="cuda")
+    dw = torch.empty(27 * 256, dtype=torch.float32, device="cuda")
+    db = torch.empty(16, dtype=torch.float32, device="cuda")
+    rc = ps.lib().PSWarmStartWeightGrad(_p(_bf(x)), _p(_bf(dy)), _p(work), nsplit, _p(dw),
+                                        _p(db), *dims, _stream())
+    assert rc == 0
+    rdw, rdb = nn.conv_bwd_weight(x, dy)
+    scale = max(np.abs(rdw).max(), 1.0)
+    assert np.abs(dw.cpu().numpy().reshape(27, 16, 16) - rdw).max() <= 1e-5 * scale
+    assert np.abs(db.cpu().numpy() - rdb).max() <= 1e-5 * max(np.abs(rdb).max(), 1.0)
+    # deterministic: the same call gives the same bits
+    dw2 = dw.clone()
+    ps.lib().PSWarmStartWeightGrad(_p(_bf(x)), _p(_bf(dy)), _p(work), nsplit, _p(dw), _p(db),
+                                   *dims, _stream())
+    assert torch.equal(dw, dw2)
+
+
+def test_loss_and_adam(rt):
+    rng = np.random.default_rng(4)
+    n = 1000
+    pred = rng.normal(size=n).astype(np.float32)
+    tgt = rng.normal(size=n).astype(np.float32)
+    dy = torch.empty(n * 16, dtype=torch.bfloat16, device="cuda")
+    part = torch.empty((n + 255) // 256, dtype=torch.float64, device="cuda")
+    rc = ps.lib().PSWarmStartLoss(_p(torch.tensor(pred, device="cuda")),
+                                  _p(torch.tensor(tgt, device="cuda")), n, _p(dy), _p(part),
+                                  _stream())
+    assert rc == 0
+    loss, g = nn.mse_loss(pred.reshape(n, 1), tgt)
+    assert abs(part.cpu().numpy().sum() / n - loss) <= 1e-12 * max(loss, 1)
+    got = _np_bf(dy, (n, 16))
+    assert _within_one_bf16_step(got, g.reshape(n, 16))
+    w = rng.normal(size=500).astype(np.float32)
+    gr = rng.normal(size=500).astype(np.float32)
+    m = np.zeros(500)
+    v = np.zeros(500)
+    tw, tg = torch.tensor(w, device="cuda"), torch.tensor(gr, device="cuda")
+    tm, tv = torch.zeros(500, device="cuda"), torch.zeros(500, device="cuda")
+    ref = w.astype(np.float64)
+    for step in (1, 2, 3):
+        rc = ps.lib().PSWarmStartAdam(_p(tw), _p(tg), _p(tm), _p(tv), 500, 1e-2, 0.9, 0.999,
+                                      1e-8, step, _stream())
+        assert rc == 0
+        ref, m, v = nn.adam(ref, gr.astype(np.float64), m, v, step, 1e-2)
+    assert np.allclose(tw.cpu().numpy(), ref, rtol=1e-5, atol=1e-6)
+
+
+def test_pool_and_upsample(rt):
+    from physis_gb300 import warmstart as ws
+    rng = np.random.default_rng(5)
+    shape = (9, 6, 5)
+    insts = [ws.make_instance(rng, shape) for _ in range(3)]
+    st = ws.Stack(insts, shape, nsx=2)
+    p = np.zeros(st.gshape, np.float32)
+    for b in range(3):
+        p[st.slot(b)] = rng.normal(size=shape)
+    st.grids[0].copyin(p)
+    f = st.fields(4, wscale=0.5, pscale=2.0, with_p=True)
+    zc, yc, xc = ws.coarse_shape(shape, 4)
+    x = torch.empty(3 * zc * yc * xc * 16, dtype=torch.bfloat16, device="cuda")
+    t = torch.empty(3 * zc * yc * xc, dtype=torch.float32, device="cuda")
+    L = ps.lib()
+    assert L.PSWarmStartPool(ctypes.byref(f), _p(x), None) == 0
+    assert L.PSWarmStartPoolTarget(ctypes.byref(f), _p(t), None) == 0
+    ps.synchronize()
+    xin = _np_bf(x, (3, zc, yc, xc, 16))
+    tt = t.cpu().numpy().reshape(3, zc, yc, xc)
+    for b, inst in enumerate(insts):
+        feats = [nn.pool(np.log(inst["a0"].astype(np.float64)), 4),
+                 nn.pool(np.log(inst["a1"].astype(np.float64)), 4),
+                 nn.pool(np.log(inst["a2"].astype(np.float64)), 4),
+                 nn.pool(inst["wrk1"].astype(np.float64), 4) * 0.5,
+                 nn.pool(inst["bnd"].astype(np.float64), 4)]
+        for c, ref in enumerate(feats):
+            assert _within_one_bf16_step(xin[b, ..., c], ref), c
+        assert np.all(xin[b, ..., 5:] == 0)
+        assert np.allclose(tt[b], nn.pool(p[st.slot(b)].astype(np.float64), 4) * 2.0,
+                           rtol=1e-5, atol=1e-6)
+    coarse = rng.normal(size=(3, zc, yc, xc)).astype(np.float32)
+    ct = torch.tensor(coarse.ravel(), device="cuda")
+    assert L.PSWarmStartUpsample(ctypes.byref(f), _p(ct), ctypes.c_void_p(st.grids[1].dev_ptr),
+                                 None) == 0
+    ps.synchronize()
+    up = st.grids[1].copyout()
+    for b, inst in enumerate(insts):
+        ref = nn.upsample(coarse[b].astype(np.float64), shape, 4) / 2.0 * inst["bnd"]
+        assert np.allclose(up[st.slot(b)], ref, rtol=1e-5, atol=1e-6)
+    st.free()
+
+
+def test_network_gradients_match_oracle(rt):
+    # One forward + backward of the 6-layer network on the GPU against the
+    # oracle's FP64 backprop on the same BF16 weights and input.  The GPU
+    # rounds activations and gradients to BF16 between layers, so the
+    # gradients agree to BF16 precision (relative 2e-2 of each tensor's
+    # largest entry), not bit for bit.
+    from physis_gb300 import warmstart as ws
+    rng = np.random.default_rng(6)
+    net = ws.Net(seed=3)
+    dims = (2, 5, 4, 6)
+    x = nn.from_bf16(nn.to_bf16(rng.normal(size=dims + (16,))))
+    x[..., 5:] = 0.0
+    t = rng.normal(size=dims).astype(np.float32)
+    ws_ = [nn.from_bf16(nn.to_bf16(w.cpu().numpy())) for w in net.w]
+    for l in range(ws.LAYERS):  # make the masters BF16-exact
+        net.w[l].copy_(torch.tensor(ws_[l], device="cuda"))
+        net.b[l].copy_(torch.tensor(rng.normal(0, 0.05, 16).astype(np.float32), device="cuda"))
+    net.prepare()
+    bs_ = [b.cpu().numpy().astype(np.float64) for b in net.b]
+    pred = net.forward(_bf(x), dims)
+    n = int(np.prod(dims))
+    work64 = torch.empty((n + 255) // 256, dtype=torch.float64, device="cuda")
+    loss, dy = ws.loss_grad(pred, torch.tensor(t.ravel(), device="cuda"), work64)
+    work = torch.empty(8 * (27 * 256 + 16), dtype=torch.float32, device="cuda")
+    net.backward(dy, dims, work)
+    torch.cuda.synchronize()
+    ref_loss, dws, dbs = nn.network_grads(x, ws_, bs_, t)
+    assert abs(loss - ref_loss) <= 2e-2 * ref_loss
+    for l in range(ws.LAYERS):
+        g = net.grads[l].cpu().numpy()
+        assert np.abs(g - dws[l]).max() <= 2e-2 * np.abs(dws[l]).max() + 1e-9, l
+        gb = net.grads[ws.LAYERS + l].cpu().numpy()
+        assert np.abs(gb - dbs[l]).max() <= 2e-2 * np.abs(dbs[l]).max() + 1e-9, l
+
+
+def test_trained_network_saves_sweeps(rt):
+    # Small instances (33 x 17 x 17), 256 solved for training and 32 held
+    # out; a short GPU training run; the held-out solves from the warm start
+    # reach relative residual 1e-6 in fewer sweeps than from zero.
+    from physis_gb300 import warmstart as ws
+    rng = np.random.default_rng(7)
+    shape, factor = (33, 17, 17), 4
+    data = ws.Dataset(rng, 256, shape, factor, nsx=15, per_stack=300, tol=1e-7, chunk=64)
+    net = ws.Net(seed=1)
+    hist, _ = ws.train(net, data, epochs=60, batch=32, lr=2e-3)
+    assert hist[-1] < 0.5 * hist[0]
+    held = [ws.make_instance(rng, shape) for _ in range(32)]
+    st = ws.Stack(held, shape, nsx=15)
+    zero = st.solve(1e-6, 16, 20000)
+    st.grids[0].copyin(np.zeros(st.gshape, np.float32))
+    st.grids[1].copyin(np.zeros(st.gshape, np.float32))
+    ws.predict_into(net, st, (data.wscale, data.pscale), factor)
+    warm = st.solve(1e-6, 16, 20000)
+    r = st.residuals()
+    st.free()
+    assert (zero > 0).all() and (warm > 0).all()
+    assert (r <= 1e-6).all()
+    assert warm.mean() < 0.9 * zero.mean(), (warm.mean(), zero.mean())

@@ -1,0 +1,82 @@
+"""Pins the learned warm start's CPU oracle (oracle/nn_oracle.py) without a
+GPU: analytic backprop against central finite differences in float64, BF16
+rounding against known encodings, pooling and upsampling against their
+definitions."""
+import numpy as np
+import pytest
+
+from oracle import nn_oracle as nn
+
+
+def _net(rng, cin=3, c=4, layers=3):
+    ws, bs = [], []
+    for l in range(layers):
+        ci = cin if l == 0 else c
+        co = 1 if l == layers - 1 else c
+        ws.append(rng.normal(0, 0.3, size=(27, ci, co)))
+        bs.append(rng.normal(0, 0.1, size=co))
+    return ws, bs
+
+
+def test_backprop_matches_finite_differences():
+    rng = np.random.default_rng(0)
+    x = rng.normal(size=(2, 3, 4, 5, 3))
+    t = rng.normal(size=(2, 3, 4, 5))
+    ws, bs = _net(rng)
+    loss, dws, dbs = nn.network_grads(x, ws, bs, t)
+    h = 1e-6
+    for l in range(len(ws)):
+        for idx in [(0, 0, 0), (13, 1, 0), (26, 2, -1), (5, -1, 0)]:
+            w2 = [w.copy() for w in ws]
+            w2[l][idx] += h
+            lp = nn.network_grads(x, w2, bs, t)[0]
+            w2[l][idx] -= 2 * h
+            lm = nn.network_grads(x, w2, bs, t)[0]
+            fd = (lp - lm) / (2 * h)
+            assert abs(fd - dws[l][idx]) <= 1e-6 * max(1.0, abs(fd)), (l, idx)
+        b2 = [b.copy() for b in bs]
+        b2[l][0] += h
+        lp = nn.network_grads(x, ws, b2, t)[0]
+        b2[l][0] -= 2 * h
+        lm = nn.network_grads(x, ws, b2, t)[0]
+        assert abs((lp - lm) / (2 * h) - dbs[l][0]) <= 1e-6 * max(1.0, abs(dbs[l][0]))
+
+
+def test_bwd_data_is_the_adjoint_of_fwd():
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=(1, 4, 3, 5, 6))
+    dy = rng.normal(size=(1, 4, 3, 5, 7))
+    w = rng.normal(size=(27, 6, 7))
+    lhs = (nn.conv_fwd(x, w) * dy).sum()
+    rhs = (x * nn.conv_bwd_data(dy, w)).sum()
+    assert abs(lhs - rhs) <= 1e-9 * abs(lhs)
+
+
+def test_bf16_rounding():
+    vals = np.array([1.0, -2.5, 3.14159265, 1e-3, 65504.0, 1.00390625, 1.01171875],
+                    np.float32)
+    b = nn.to_bf16(vals)
+    assert list(b[:2]) == [0x3F80, 0xC020]
+    assert nn.from_bf16(nn.to_bf16(np.float32(1.00390625)))[()] == 1.0   # tie -> even
+    assert nn.from_bf16(nn.to_bf16(np.float32(1.01171875)))[()] == 1.015625
+    back = nn.from_bf16(b)
+    assert np.all(np.abs(back - vals) <= np.abs(vals) * 2 ** -8)
+
+
+def test_pool_and_upsample():
+    rng = np.random.default_rng(2)
+    f = rng.normal(size=(9, 6, 5))
+    p = nn.pool(f, 4)
+    assert p.shape == (3, 2, 2)
+    assert np.isclose(p[0, 0, 0], f[:4, :4, :4].mean())
+    assert np.isclose(p[2, 1, 1], f[8:, 4:, 4:].mean())
+    c = rng.normal(size=(3, 2, 2))
+    u = nn.upsample(np.ones_like(c) * 2.5, (9, 6, 5), 4)
+    assert np.allclose(u, 2.5)
+    # linear fields are reproduced between the first and last coarse centres
+    lin = np.fromfunction(lambda z, y, x: 0.5 * z - y + 2 * x, (3, 2, 2))
+    up = nn.upsample(lin, (12, 8, 8), 4)
+    zf, yf, xf = np.meshgrid((np.arange(12) + 0.5) / 4 - 0.5, (np.arange(8) + 0.5) / 4 - 0.5,
+                             (np.arange(8) + 0.5) / 4 - 0.5, indexing="ij")
+    inside = (zf >= 0) & (zf <= 2) & (yf >= 0) & (yf <= 1) & (xf >= 0) & (xf <= 1)
+    assert np.allclose(up[inside], (0.5 * zf - yf + 2 * xf)[inside])
