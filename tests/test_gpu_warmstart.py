@@ -82,8 +82,9 @@ def test_conv_forward(rt, dims):
     y = torch.empty(n * 16, dtype=torch.bfloat16, device="cuda")
     y0 = torch.empty(n, dtype=torch.float32, device="cuda")
     bt = torch.tensor(bias, device="cuda")
+    tx = _bf(x)  # kept alive: the kernel reads it asynchronously
     for relu in (1, 0):
-        rc = ps.lib().PSWarmStartConv(_p(_bf(x)), _p(wf), _p(bt), None, relu, _p(y), _p(y0),
+        rc = ps.lib().PSWarmStartConv(_p(tx), _p(wf), _p(bt), None, relu, _p(y), _p(y0),
                                       *dims, _stream())
         assert rc == 0
         ref = nn.conv_fwd(x, w, bias)
@@ -103,7 +104,8 @@ def test_conv_backward_data_with_mask(rt, dims):
     _, wb = _prep(w)
     n = int(np.prod(dims))
     dx = torch.empty(n * 16, dtype=torch.bfloat16, device="cuda")
-    rc = ps.lib().PSWarmStartConv(_p(_bf(dy)), _p(wb), None, _p(_bf(mask)), 0, _p(dx), None,
+    tdy, tmask = _bf(dy), _bf(mask)
+    rc = ps.lib().PSWarmStartConv(_p(tdy), _p(wb), None, _p(tmask), 0, _p(dx), None,
                                   *dims, _stream())
     assert rc == 0
     ref = nn.conv_bwd_data(dy, w) * (mask > 0)
@@ -119,7 +121,8 @@ def test_weight_and_bias_gradients(rt, dims, nsplit):
     work = torch.empty(nsplit * (27 * 256 + 16), dtype=torch.float32, device="cuda")
     dw = torch.empty(27 * 256, dtype=torch.float32, device="cuda")
     db = torch.empty(16, dtype=torch.float32, device="cuda")
-    rc = ps.lib().PSWarmStartWeightGrad(_p(_bf(x)), _p(_bf(dy)), _p(work), nsplit, _p(dw),
+    tx, tdy = _bf(x), _bf(dy)
+    rc = ps.lib().PSWarmStartWeightGrad(_p(tx), _p(tdy), _p(work), nsplit, _p(dw),
                                         _p(db), *dims, _stream())
     assert rc == 0
     rdw, rdb = nn.conv_bwd_weight(x, dy)
@@ -128,7 +131,7 @@ def test_weight_and_bias_gradients(rt, dims, nsplit):
     assert np.abs(db.cpu().numpy() - rdb).max() <= 1e-5 * max(np.abs(rdb).max(), 1.0)
     # deterministic: the same call gives the same bits
     dw2 = dw.clone()
-    ps.lib().PSWarmStartWeightGrad(_p(_bf(x)), _p(_bf(dy)), _p(work), nsplit, _p(dw), _p(db),
+    ps.lib().PSWarmStartWeightGrad(_p(tx), _p(tdy), _p(work), nsplit, _p(dw), _p(db),
                                    *dims, _stream())
     assert torch.equal(dw, dw2)
 
@@ -140,9 +143,8 @@ def test_loss_and_adam(rt):
     tgt = rng.normal(size=n).astype(np.float32)
     dy = torch.empty(n * 16, dtype=torch.bfloat16, device="cuda")
     part = torch.empty((n + 255) // 256, dtype=torch.float64, device="cuda")
-    rc = ps.lib().PSWarmStartLoss(_p(torch.tensor(pred, device="cuda")),
-                                  _p(torch.tensor(tgt, device="cuda")), n, _p(dy), _p(part),
-                                  _stream())
+    tp, tt = torch.tensor(pred, device="cuda"), torch.tensor(tgt, device="cuda")
+    rc = ps.lib().PSWarmStartLoss(_p(tp), _p(tt), n, _p(dy), _p(part), _stream())
     assert rc == 0
     loss, g = nn.mse_loss(pred.reshape(n, 1), tgt)
     assert abs(part.cpu().numpy().sum() / n - loss) <= 1e-12 * max(loss, 1)
@@ -225,10 +227,12 @@ def test_network_gradients_match_oracle(rt):
         net.b[l].copy_(torch.tensor(rng.normal(0, 0.05, 16).astype(np.float32), device="cuda"))
     net.prepare()
     bs_ = [b.cpu().numpy().astype(np.float64) for b in net.b]
-    pred = net.forward(_bf(x), dims)
+    tx = _bf(x)
+    pred = net.forward(tx, dims)
     n = int(np.prod(dims))
     work64 = torch.empty((n + 255) // 256, dtype=torch.float64, device="cuda")
-    loss, dy = ws.loss_grad(pred, torch.tensor(t.ravel(), device="cuda"), work64)
+    tt = torch.tensor(t.ravel(), device="cuda")
+    loss, dy = ws.loss_grad(pred, tt, work64)
     work = torch.empty(8 * (27 * 256 + 16), dtype=torch.float32, device="cuda")
     net.backward(dy, dims, work)
     torch.cuda.synchronize()
