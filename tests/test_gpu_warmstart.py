@@ -61,11 +61,12 @@ def _prep(w):
 
 
 def _within_one_bf16_step(got, ref):
-    """|got - ref| <= one BF16 ulp of ref (FP32 accumulation order differs
-    from the FP64 oracle, so a value near a rounding tie may round the other
-    way)."""
-    ulp = np.maximum(np.abs(ref), 1e-30) * 2.0 ** -7
-    return np.all(np.abs(got - ref) <= ulp + 1e-30)
+    """|got - ref| <= one BF16 step of ref, plus the FP32 accumulation error
+    of sums that cancel (1e-5 of the tensor's largest magnitude): the GPU
+    sums in FP32 in another order than the FP64 oracle, then rounds to
+    BF16."""
+    tol = np.abs(ref) * 2.0 ** -7 + 1e-5 * np.abs(ref).max() + 1e-30
+    return np.all(np.abs(got - ref) <= tol)
 
 
 DIMS = [(2, 5, 4, 7), (1, 3, 9, 2), (3, 17, 9, 9)]
