@@ -77,13 +77,22 @@ def relu(a):
     return np.maximum(a, 0.0)
 
 
-def network_fwd(x, ws, bs):
-    """The 6-layer net: conv+ReLU x5, conv; returns every layer's output
-    (float64, before any BF16 rounding)."""
+def _round_bf16(a):
+    return from_bf16(to_bf16(a)).astype(np.float64)
+
+
+def network_fwd(x, ws, bs, bf16=False):
+    """The 6-layer net: conv+ReLU x5, conv; returns every layer's output in
+    float64.  bf16=True rounds the hidden activations to BF16 where the GPU
+    stores them (the last layer's output stays unrounded)."""
     acts = [np.asarray(x, np.float64)]
     for l, (w, b) in enumerate(zip(ws, bs)):
         y = conv_fwd(acts[-1], w, b)
-        acts.append(relu(y) if l < len(ws) - 1 else y)
+        if l < len(ws) - 1:
+            y = relu(y)
+            if bf16:
+                y = _round_bf16(y)
+        acts.append(y)
     return acts
 
 
@@ -95,15 +104,21 @@ def mse_loss(pred, target):
     return float((diff ** 2).mean()), g
 
 
-def network_grads(x, ws, bs, target):
-    """Loss and gradients of every weight and bias (float64 backprop)."""
-    acts = network_fwd(x, ws, bs)
+def network_grads(x, ws, bs, target, bf16=False):
+    """Loss and gradients of every weight and bias (float64 backprop).
+    bf16=True also rounds the activations and the propagated gradients to
+    BF16 at the points where the GPU stores them in BF16."""
+    acts = network_fwd(x, ws, bs, bf16)
     loss, g = mse_loss(acts[-1], target)
+    if bf16:
+        g = _round_bf16(g)
     dws, dbs = [None] * len(ws), [None] * len(ws)
     for l in range(len(ws) - 1, -1, -1):
         dws[l], dbs[l] = conv_bwd_weight(acts[l], g)
         if l:
             g = conv_bwd_data(g, ws[l]) * (acts[l] > 0)
+            if bf16:
+                g = _round_bf16(g)
     return loss, dws, dbs
 
 
