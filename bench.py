@@ -846,6 +846,122 @@ def run_gpu_points(args, dist):
     g2.free()
 
 
+# ---------------------------------------------------------------------------
+# Learned warm start for the 19-point Jacobi solve (config 5, reduced scale)
+# ---------------------------------------------------------------------------
+
+def measured_bf16_tflops():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        for k in ("bf16_tflops", "bf16_tflops_burst"):
+            if k in d:
+                return float(d[k]), "measured"
+    return 1900.0, "fallback"
+
+
+def run_gpu_warmstart(args, dist):
+    """Train the warm-start network on solved instances, then time the
+    held-out Jacobi solves to relative residual 1e-6 from zero and from the
+    network's prediction (prediction time included)."""
+    import torch
+    import physis_gb300 as ps
+    from physis_gb300 import warmstart as ws
+    ps.init()
+    shape = (args.ws_nz, args.ws_ny, args.ws_nx)
+    factor = 4
+    rng = np.random.default_rng(5)
+    t0 = time.perf_counter()
+    data = ws.Dataset(rng, args.ws_train, shape, factor, tol=1e-7, chunk=256)
+    data_s = time.perf_counter() - t0
+    net = ws.Net(seed=1)
+    hist, train_s = ws.train(net, data, epochs=args.ws_epochs, batch=32, lr=2e-3)
+
+    held = [ws.make_instance(rng, shape) for _ in range(args.ws_held)]
+    st = ws.Stack(held, shape, nsx=15)
+    zeros = np.zeros(st.gshape, np.float32)
+
+    def reset():
+        st.grids[0].copyin(zeros)
+        st.grids[1].copyin(zeros)
+
+    scales = (data.wscale, data.pscale)
+    reset()
+    zero = st.solve(1e-6, 16, 200000)
+    reset()
+    ws.predict_into(net, st, scales, factor)
+    r_warm0 = st.residuals()
+    warm = st.solve(1e-6, 16, 200000)
+    nz_sw, nw_sw = int(zero.max()), int(warm.max())
+
+    def timed(warm_start, n):
+        reset()
+        ps.synchronize()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        if warm_start:
+            ws.predict_into(net, st, scales, factor)
+        st.sweeps(n)
+        ps.synchronize()
+        return time.perf_counter() - t
+
+    for _ in range(max(args.warmup, 3) // 3):  # warm-up of both paths
+        timed(False, 32)
+        timed(True, 32)
+    tz = min(timed(False, nz_sw) for _ in range(2))
+    tw = min(timed(True, nw_sw) for _ in range(2))
+    ok_zero = bool((zero > 0).all())
+    r_end = st.residuals()  # after the warm timed run
+    ok_warm = bool((warm > 0).all() and (r_end <= 1e-6).all())
+
+    # tensor roofline of the network's forward pass over the training set
+    zc, yc, xc = data.dims1
+    nvox = data.x.shape[0] * zc * yc * xc
+    x = data.x.reshape(-1)
+    net.forward(x, (data.x.shape[0], zc, yc, xc))
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(5):
+        net.forward(x, (data.x.shape[0], zc, yc, xc))
+    ev1.record()
+    torch.cuda.synchronize()
+    fwd_ms = ev0.elapsed_time(ev1) / 5
+    flops = 2.0 * 27 * 16 * 16 * nvox * ws.LAYERS
+    peak, peak_kind = measured_bf16_tflops()
+    tflops = flops / (fwd_ms / 1e3) / 1e12
+    st.free()
+    line = {
+        "metric": "Poisson time-to-1e-6 resid, learned vs plain (speed-up of the warm start)",
+        "value": tz / tw, "unit": "x", "n_gpus": 1, "steps": args.ws_held,
+        "warmup": max(args.warmup, 3), "ms_per_step": tw / args.ws_held * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16",
+        "data": f"synthetic seeded instances (seed 5), {args.ws_train} solved for training, "
+                f"{args.ws_held} held out",
+        "config": {"workload": f"learned warm start, 19-point Jacobi {shape[2]}x{shape[1]}x"
+                               f"{shape[0]} (x,y,z; reduced from 129x129x257)",
+                   "network": "pool 4^3 -> 6 conv 3x3x3 x16 (BF16, FP32 acc.) -> trilinear",
+                   "epochs": args.ws_epochs, "batch": 32,
+                   "l2": "held-out stack: 14 arrays x 1.0 GB total > L2"},
+        "zero_start": {"sweeps_mean": float(zero.mean()), "sweeps_max": nz_sw,
+                       "seconds": tz, "all_converged": ok_zero},
+        "warm_start": {"sweeps_mean": float(warm.mean()), "sweeps_max": nw_sw,
+                       "seconds": tw, "all_converged": ok_warm,
+                       "initial_residual_median": float(np.median(r_warm0))},
+        "sweeps_ratio_mean": float(zero.mean() / warm.mean()),
+        "training": {"seconds": train_s, "loss_first_epoch": hist[0],
+                     "loss_last_epoch": hist[-1]},
+        "dataset": {"seconds": data_s, "solve_seconds": data.solve_seconds,
+                    "target_sweeps_mean": float(data.sweeps.mean())},
+        "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s",
+                     "frac": tflops / peak, "traffic": None, "peak_source": peak_kind,
+                     "what": "network forward over the training set (mma.sync BF16)"},
+        "gpu_launches": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -864,9 +980,15 @@ def main():
                     help="batch workload with 48 small grids (launch-bound regime)")
     ap.add_argument("--workload", default="diffusion",
                     choices=["diffusion", "himeno", "batch", "points27", "points7",
-                             "function7", "function27"],
+                             "function7", "function27", "warmstart"],
                     help="diffusion: 7-point 512^3 (the headline); himeno: "
                          "19-point Jacobi 257x257x513 with fused residual")
+    ap.add_argument("--ws-train", type=int, default=4096)
+    ap.add_argument("--ws-held", type=int, default=256)
+    ap.add_argument("--ws-epochs", type=int, default=60)
+    ap.add_argument("--ws-nx", type=int, default=33)
+    ap.add_argument("--ws-ny", type=int, default=33)
+    ap.add_argument("--ws-nz", type=int, default=65)
     args = ap.parse_args()
     global N
     N = args.n
@@ -880,6 +1002,8 @@ def main():
             run_gpu_himeno(args, dist)
         elif args.workload == "batch":
             run_gpu_batch(args, dist)
+        elif args.workload == "warmstart":
+            run_gpu_warmstart(args, dist)
         elif args.workload in ("points27", "points7", "function7", "function27"):
             run_gpu_points(args, dist)
         else:

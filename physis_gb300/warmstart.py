@@ -43,7 +43,13 @@ LAYERS = 6
 # ---- instances ----------------------------------------------------------------
 
 def _gaussian_smooth(u, sigma):
-    """Separable Gaussian filter (truncated at 3 sigma, reflected edges)."""
+    """Separable Gaussian filter (truncated at 3 sigma, edges mirrored about
+    the boundary half-sample, scipy.ndimage's "reflect")."""
+    try:  # scipy's C implementation of the same filter, when present
+        from scipy.ndimage import gaussian_filter
+        return gaussian_filter(u, sigma, mode="reflect", truncate=3.0)
+    except ImportError:
+        pass
     r = int(math.ceil(3 * sigma))
     k = np.exp(-0.5 * (np.arange(-r, r + 1) / sigma) ** 2)
     k /= k.sum()
@@ -51,7 +57,7 @@ def _gaussian_smooth(u, sigma):
     for axis in range(3):
         pad = [(0, 0)] * 3
         pad[axis] = (r, r)
-        p = np.pad(out, pad, mode="reflect")
+        p = np.pad(out, pad, mode="symmetric")
         acc = np.zeros_like(out)
         for i, w in enumerate(k):
             sl = [slice(None)] * 3
