@@ -380,13 +380,17 @@ def train(net, data, epochs, batch, lr, log=None, seed=0):
     s = 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    nb = count // batch
     for e in range(epochs):
-        order = rng.permutation(count)
+        # The instances are generated independently, so minibatches are
+        # fixed contiguous slices (views: no copy) visited in a new random
+        # order each epoch.
+        order = rng.permutation(nb)
         tot = 0.0
-        for i in range(count // batch):
-            idx = torch.as_tensor(order[i * batch:(i + 1) * batch], device="cuda")
-            x = data.x.index_select(0, idx).reshape(-1)
-            t = data.t.index_select(0, idx).reshape(-1)
+        for i in range(nb):
+            j = int(order[i])
+            x = data.x[j * batch:(j + 1) * batch].reshape(-1)
+            t = data.t[j * batch:(j + 1) * batch].reshape(-1)
             pred = net.forward(x, (batch, zc, yc, xc))
             loss, dy = loss_grad(pred, t, work64)
             net.backward(dy, (batch, zc, yc, xc), work)
@@ -394,7 +398,7 @@ def train(net, data, epochs, batch, lr, log=None, seed=0):
             net.adam(rate)
             tot += loss
             s += 1
-        history.append(tot / max(count // batch, 1))
+        history.append(tot / max(nb, 1))
         if log:
             log(f"epoch {e}: loss {history[-1]:.5f}")
     torch.cuda.synchronize()
