@@ -873,7 +873,8 @@ def run_gpu_warmstart(args, dist):
     factor = 4
     rng = np.random.default_rng(5)
     t0 = time.perf_counter()
-    data = ws.Dataset(rng, args.ws_train, shape, factor, tol=1e-7, chunk=256)
+    data = ws.Dataset(rng, args.ws_train, shape, factor, tol=1e-7, chunk=256,
+                      max_sweeps=args.ws_max_sweeps)
     data_s = time.perf_counter() - t0
     net = ws.Net(seed=1)
     hist, train_s = ws.train(net, data, epochs=args.ws_epochs, batch=32, lr=2e-3)
@@ -887,13 +888,18 @@ def run_gpu_warmstart(args, dist):
         st.grids[1].copyin(zeros)
 
     scales = (data.wscale, data.pscale)
+    # Sweep counts, checked every 32 sweeps.  Float32 Jacobi has a residual
+    # floor near 1e-7 * ||p|| / ||ss(0)||; instances whose floor lies above
+    # 1e-6 never get there from either start and are left out of the
+    # comparison (counted in the output).
     reset()
-    zero = st.solve(1e-6, 16, 200000)
+    zero = st.solve(1e-6, 32, args.ws_max_sweeps)
     reset()
     ws.predict_into(net, st, scales, factor)
     r_warm0 = st.residuals()
-    warm = st.solve(1e-6, 16, 200000)
-    nz_sw, nw_sw = int(zero.max()), int(warm.max())
+    warm = st.solve(1e-6, 32, args.ws_max_sweeps)
+    both = (zero > 0) & (warm > 0)
+    nz_sw, nw_sw = int(zero[both].max()), int(warm[both].max())
 
     def timed(warm_start, n):
         reset()
@@ -910,10 +916,11 @@ def run_gpu_warmstart(args, dist):
         timed(False, 32)
         timed(True, 32)
     tz = min(timed(False, nz_sw) for _ in range(2))
+    r_zero_end = st.residuals()
     tw = min(timed(True, nw_sw) for _ in range(2))
-    ok_zero = bool((zero > 0).all())
     r_end = st.residuals()  # after the warm timed run
-    ok_warm = bool((warm > 0).all() and (r_end <= 1e-6).all())
+    ok_zero = bool((r_zero_end[both] <= 1e-6).all())
+    ok_warm = bool((r_end[both] <= 1e-6).all())
 
     # tensor roofline of the network's forward pass over the training set
     zc, yc, xc = data.dims1
@@ -921,13 +928,11 @@ def run_gpu_warmstart(args, dist):
     x = data.x.reshape(-1)
     net.forward(x, (data.x.shape[0], zc, yc, xc))
     torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record()
+    t0 = time.perf_counter()
     for _ in range(5):
         net.forward(x, (data.x.shape[0], zc, yc, xc))
-    ev1.record()
     torch.cuda.synchronize()
-    fwd_ms = ev0.elapsed_time(ev1) / 5
+    fwd_ms = (time.perf_counter() - t0) / 5 * 1e3
     flops = 2.0 * 27 * 16 * 16 * nvox * ws.LAYERS
     peak, peak_kind = measured_bf16_tflops()
     tflops = flops / (fwd_ms / 1e3) / 1e12
@@ -944,14 +949,18 @@ def run_gpu_warmstart(args, dist):
                    "network": "pool 4^3 -> 6 conv 3x3x3 x16 (BF16, FP32 acc.) -> trilinear",
                    "epochs": args.ws_epochs, "batch": 32,
                    "l2": "held-out stack: 14 arrays x 1.0 GB total > L2"},
-        "zero_start": {"sweeps_mean": float(zero.mean()), "sweeps_max": nz_sw,
-                       "seconds": tz, "all_converged": ok_zero},
-        "warm_start": {"sweeps_mean": float(warm.mean()), "sweeps_max": nw_sw,
-                       "seconds": tw, "all_converged": ok_warm,
+        "compared_instances": int(both.sum()),
+        "below_1e-6_unreachable": {"zero_start": int((zero <= 0).sum()),
+                                   "warm_start": int((warm <= 0).sum())},
+        "zero_start": {"sweeps_mean": float(zero[both].mean()), "sweeps_max": nz_sw,
+                       "seconds": tz, "all_compared_converged": ok_zero},
+        "warm_start": {"sweeps_mean": float(warm[both].mean()), "sweeps_max": nw_sw,
+                       "seconds": tw, "all_compared_converged": ok_warm,
                        "initial_residual_median": float(np.median(r_warm0))},
-        "sweeps_ratio_mean": float(zero.mean() / warm.mean()),
+        "sweeps_ratio_mean": float(zero[both].mean() / warm[both].mean()),
         "training": {"seconds": train_s, "loss_first_epoch": hist[0],
                      "loss_last_epoch": hist[-1]},
+        "network_forward_ms": fwd_ms,
         "dataset": {"seconds": data_s, "solve_seconds": data.solve_seconds,
                     "target_sweeps_mean": float(data.sweeps.mean())},
         "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s",
@@ -989,6 +998,7 @@ def main():
     ap.add_argument("--ws-nx", type=int, default=33)
     ap.add_argument("--ws-ny", type=int, default=33)
     ap.add_argument("--ws-nz", type=int, default=65)
+    ap.add_argument("--ws-max-sweeps", type=int, default=12000)
     args = ap.parse_args()
     global N
     N = args.n
