@@ -919,8 +919,10 @@ def run_gpu_warmstart(args, dist):
     r_zero_end = st.residuals()
     tw = min(timed(True, nw_sw) for _ in range(2))
     r_end = st.residuals()  # after the warm timed run
-    ok_zero = bool((r_zero_end[both] <= 1e-6).all())
-    ok_warm = bool((r_end[both] <= 1e-6).all())
+    # instances at or below 1e-6 after the timed runs (a few whose float32
+    # floor lies just under 1e-6 can drift back above it between checks)
+    ok_zero = int((r_zero_end[both] <= 1e-6).sum())
+    ok_warm = int((r_end[both] <= 1e-6).sum())
 
     # tensor roofline of the network's forward pass over the training set
     zc, yc, xc = data.dims1
@@ -953,9 +955,9 @@ def run_gpu_warmstart(args, dist):
         "below_1e-6_unreachable": {"zero_start": int((zero <= 0).sum()),
                                    "warm_start": int((warm <= 0).sum())},
         "zero_start": {"sweeps_mean": float(zero[both].mean()), "sweeps_max": nz_sw,
-                       "seconds": tz, "all_compared_converged": ok_zero},
+                       "seconds": tz, "at_1e-6_after_timed_run": ok_zero},
         "warm_start": {"sweeps_mean": float(warm[both].mean()), "sweeps_max": nw_sw,
-                       "seconds": tw, "all_compared_converged": ok_warm,
+                       "seconds": tw, "at_1e-6_after_timed_run": ok_warm,
                        "initial_residual_median": float(np.median(r_warm0))},
         "sweeps_ratio_mean": float(zero[both].mean() / warm[both].mean()),
         "training": {"seconds": train_s, "loss_first_epoch": hist[0],
