@@ -337,10 +337,12 @@ typedef struct PSWarmStartFields {
 /* Network input: per factor^3 block of each instance, channels mean ln a0,
  * mean ln a1, mean ln a2, mean wrk1 * wscale, mean bnd, then zeros. */
 int PSWarmStartPool(const PSWarmStartFields *f, void *out, void *stream);
-/* Training target: per block, mean p * pscale (FP32). */
+/* Training target: p at each block's centre (c + 0.5) * factor - 0.5, the
+ * mean of the fine cells nearest to it, times pscale (FP32). */
 int PSWarmStartPoolTarget(const PSWarmStartFields *f, float *out, void *stream);
-/* Warm start: p = bnd * trilinear(coarse) / pscale at every fine cell, from
- * coarse cell centres at (c + 0.5) * factor - 0.5 (clamped). */
+/* Warm start: p = bnd * cubic(coarse) / pscale at every fine cell:
+ * Catmull-Rom interpolation per axis from coarse cell centres at
+ * (c + 0.5) * factor - 0.5 (clamped). */
 int PSWarmStartUpsample(const PSWarmStartFields *f, const float *coarse, float *p, void *stream);
 
 #if defined(__GNUC__)

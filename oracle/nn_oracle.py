@@ -145,20 +145,45 @@ def pool(fine, f):
     return s / n
 
 
+def centre_sample(fine, f):
+    """Value at each f^3 block's centre (z_c + 0.5) f - 0.5: the mean of the
+    fine cells nearest to it (2 per axis for even f, 1 for odd f), clamped to
+    the grid."""
+    out = np.asarray(fine, np.float64)
+    for axis, n in enumerate(fine.shape):
+        nc = -(-n // f)
+        pos = (np.arange(nc) + 0.5) * f - 0.5
+        i0 = np.minimum(np.floor(pos).astype(int), n - 1)
+        i1 = np.minimum(np.ceil(pos).astype(int), n - 1)
+        out = 0.5 * (np.take(out, i0, axis=axis) + np.take(out, i1, axis=axis))
+    return out
+
+
+def catmull_rom(t):
+    """Weights of points -1, 0, 1, 2 for a position t in [0, 1] past point 0
+    (Catmull & Rom 1974: the cubic through the four points with central-
+    difference end slopes)."""
+    t2, t3 = t * t, t * t * t
+    return ((-t3 + 2 * t2 - t) / 2, (3 * t3 - 5 * t2 + 2) / 2,
+            (-3 * t3 + 4 * t2 + t) / 2, (t3 - t2) / 2)
+
+
 def upsample(coarse, shape, f):
-    """Trilinear interpolation from coarse cell centres (z_c + 0.5) * f - 0.5
-    to every fine point, clamped at the ends."""
-    out = coarse
+    """Catmull-Rom cubic interpolation, axis by axis, from coarse cell
+    centres (c + 0.5) f - 0.5 to every fine point; positions are clamped to
+    [0, nc - 1] and neighbour indices to the coarse grid."""
+    out = np.asarray(coarse, np.float64)
     for axis, n in enumerate(shape):
         nc = coarse.shape[axis]
-        pos = (np.arange(n) + 0.5) / f - 0.5
-        pos = np.clip(pos, 0, nc - 1)
-        i0 = np.floor(pos).astype(int)
-        i1 = np.minimum(i0 + 1, nc - 1)
+        pos = np.clip((np.arange(n) + 0.5) / f - 0.5, 0, nc - 1)
+        i0 = np.minimum(np.floor(pos).astype(int), nc - 1)
         t = pos - i0
-        a = np.take(out, i0, axis=axis)
-        b = np.take(out, i1, axis=axis)
+        ws = catmull_rom(t)
         sh = [1] * out.ndim
         sh[axis] = n
-        out = a * (1 - t.reshape(sh)) + b * t.reshape(sh)
+        acc = 0.0
+        for k, w in zip((-1, 0, 1, 2), ws):
+            idx = np.clip(i0 + k, 0, nc - 1)
+            acc = acc + np.take(out, idx, axis=axis) * w.reshape(sh)
+        out = acc
     return out

@@ -328,6 +328,8 @@ __global__ void pool_inputs_kernel(PoolArgs a, __nv_bfloat16 *__restrict__ out) 
   for (int c = 5; c < kC; ++c) row[c] = __float2bfloat16_rn(0.f);
 }
 
+// Training target: p at each block's centre (c + 0.5) f - 0.5, the mean of
+// the fine cells nearest to it (two per axis for even f), times pscale.
 __global__ void pool_target_kernel(PoolArgs a, float *__restrict__ out) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long n = (long long)a.batch * a.zc * a.yc * a.xc;
@@ -335,20 +337,38 @@ __global__ void pool_target_kernel(PoolArgs a, float *__restrict__ out) {
   const int xc = (int)(i % a.xc), yc = (int)((i / a.xc) % a.yc);
   const int zc = (int)((i / ((long long)a.xc * a.yc)) % a.zc);
   const int b = (int)(i / ((long long)a.xc * a.yc * a.zc));
+  // nearest fine cells to the centre: lo = floor, hi = ceil of (c + 0.5) f - 0.5
+  auto near = [&](int c, int nf, int &lo, int &hi) {
+    lo = min((2 * c * a.f + a.f - 1) / 2, nf - 1);
+    hi = min((2 * c * a.f + a.f) / 2, nf - 1);
+  };
+  int z0, z1, y0, y1, x0, x1;
+  near(zc, a.inz, z0, z1);
+  near(yc, a.iny, y0, y1);
+  near(xc, a.inx, x0, x1);
+  const int zs[2] = {z0, z1}, ys[2] = {y0, y1}, xs[2] = {x0, x1};
   float s = 0.f;
-  int cnt = 0;
-  for (int z = zc * a.f; z < min(zc * a.f + a.f, a.inz); ++z)
-    for (int y = yc * a.f; y < min(yc * a.f + a.f, a.iny); ++y)
-      for (int x = xc * a.f; x < min(xc * a.f + a.f, a.inx); ++x) {
-        s += a.p[fine_index(a, b, z, y, x)];
-        ++cnt;
-      }
-  out[i] = s / (float)cnt * a.pscale;
+  for (int k = 0; k < 2; ++k)
+    for (int j = 0; j < 2; ++j)
+      for (int m = 0; m < 2; ++m) s += a.p[fine_index(a, b, zs[k], ys[j], xs[m])];
+  out[i] = s * 0.125f * a.pscale;
 }
 
-// Coarse prediction (FP32, one value per coarse cell) -> fine p: trilinear
-// from coarse centres at (c + 0.5) f - 0.5, clamped, divided by pscale,
-// times bnd.  Writes every fine cell of every instance.
+// Catmull-Rom weights of points -1, 0, 1, 2 at t in [0, 1] past point 0
+// (Catmull & Rom 1974).
+__device__ __forceinline__ void catmull_rom(float t, float (&w)[4]) {
+  const float t2 = t * t, t3 = t2 * t;
+  w[0] = 0.5f * (-t3 + 2.f * t2 - t);
+  w[1] = 0.5f * (3.f * t3 - 5.f * t2 + 2.f);
+  w[2] = 0.5f * (-3.f * t3 + 4.f * t2 + t);
+  w[3] = 0.5f * (t3 - t2);
+}
+
+// Coarse prediction (FP32, one value per coarse cell) -> fine p:
+// Catmull-Rom cubic interpolation per axis from coarse centres at
+// (c + 0.5) f - 0.5 (positions clamped to [0, nc - 1], neighbour indices to
+// the coarse grid), divided by pscale, times bnd.  Writes every fine cell of
+// every instance.
 __global__ void upsample_kernel(PoolArgs a, const float *__restrict__ coarse,
                                 float *__restrict__ p) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -357,30 +377,32 @@ __global__ void upsample_kernel(PoolArgs a, const float *__restrict__ coarse,
   const int x = (int)(i % a.inx), y = (int)((i / a.inx) % a.iny);
   const int z = (int)((i / ((long long)a.inx * a.iny)) % a.inz);
   const int b = (int)(i / ((long long)a.inx * a.iny * a.inz));
-  auto axis = [&](int j, int nc, int &i0, int &i1, float &t) {
+  auto axis = [&](int j, int nc, int (&idx)[4], float (&w)[4]) {
     float pos = ((float)j + 0.5f) / (float)a.f - 0.5f;
     pos = fminf(fmaxf(pos, 0.f), (float)(nc - 1));
-    i0 = (int)floorf(pos);
-    i1 = min(i0 + 1, nc - 1);
-    t = pos - (float)i0;
+    const int i0 = min((int)floorf(pos), nc - 1);
+    catmull_rom(pos - (float)i0, w);
+    for (int k = 0; k < 4; ++k) idx[k] = min(max(i0 - 1 + k, 0), nc - 1);
   };
-  int z0, z1, y0, y1, x0, x1;
-  float tz, ty, tx;
-  axis(z, a.zc, z0, z1, tz);
-  axis(y, a.yc, y0, y1, ty);
-  axis(x, a.xc, x0, x1, tx);
+  int iz[4], iy[4], ix[4];
+  float wz[4], wy[4], wx[4];
+  axis(z, a.zc, iz, wz);
+  axis(y, a.yc, iy, wy);
+  axis(x, a.xc, ix, wx);
   const float *c = coarse + (long long)b * a.zc * a.yc * a.xc;
-  auto at = [&](int zz, int yy, int xx) { return c[((long long)zz * a.yc + yy) * a.xc + xx]; };
-  // interpolate x, then y, then z (the oracle's axis order is z, y, x;
-  // trilinear interpolation is the same up to rounding)
-  const float c00 = at(z0, y0, x0) * (1.f - tx) + at(z0, y0, x1) * tx;
-  const float c01 = at(z0, y1, x0) * (1.f - tx) + at(z0, y1, x1) * tx;
-  const float c10 = at(z1, y0, x0) * (1.f - tx) + at(z1, y0, x1) * tx;
-  const float c11 = at(z1, y1, x0) * (1.f - tx) + at(z1, y1, x1) * tx;
-  const float c0 = c00 * (1.f - ty) + c01 * ty, c1 = c10 * (1.f - ty) + c11 * ty;
-  const float v = (c0 * (1.f - tz) + c1 * tz) / a.pscale;
+  float v = 0.f;
+  for (int kz = 0; kz < 4; ++kz) {
+    float vy = 0.f;
+    for (int ky = 0; ky < 4; ++ky) {
+      const float *row = c + ((long long)iz[kz] * a.yc + iy[ky]) * a.xc;
+      float vx = 0.f;
+      for (int kx = 0; kx < 4; ++kx) vx += wx[kx] * row[ix[kx]];
+      vy += wy[ky] * vx;
+    }
+    v += wz[kz] * vy;
+  }
   const long long k = fine_index(a, b, z, y, x);
-  p[k] = v * a.bnd[k];
+  p[k] = v / a.pscale * a.bnd[k];
 }
 
 }  // namespace

@@ -199,7 +199,7 @@ def test_pool_and_upsample(rt):
         for c, ref in enumerate(feats):
             assert _within_one_bf16_step(xin[b, ..., c], ref), c
         assert np.all(xin[b, ..., 5:] == 0)
-        assert np.allclose(tt[b], nn.pool(p[st.slot(b)].astype(np.float64), 4) * 2.0,
+        assert np.allclose(tt[b], nn.centre_sample(p[st.slot(b)].astype(np.float64), 4) * 2.0,
                            rtol=1e-5, atol=1e-6)
     coarse = rng.normal(size=(3, zc, yc, xc)).astype(np.float32)
     ct = torch.tensor(coarse.ravel(), device="cuda")

@@ -73,10 +73,17 @@ def test_pool_and_upsample():
     c = rng.normal(size=(3, 2, 2))
     u = nn.upsample(np.ones_like(c) * 2.5, (9, 6, 5), 4)
     assert np.allclose(u, 2.5)
-    # linear fields are reproduced between the first and last coarse centres
-    lin = np.fromfunction(lambda z, y, x: 0.5 * z - y + 2 * x, (3, 2, 2))
-    up = nn.upsample(lin, (12, 8, 8), 4)
-    zf, yf, xf = np.meshgrid((np.arange(12) + 0.5) / 4 - 0.5, (np.arange(8) + 0.5) / 4 - 0.5,
-                             (np.arange(8) + 0.5) / 4 - 0.5, indexing="ij")
-    inside = (zf >= 0) & (zf <= 2) & (yf >= 0) & (yf <= 1) & (xf >= 0) & (xf <= 1)
+    # the coarse values are reproduced at the coarse centres, and linear
+    # fields between the second and the second-to-last centre (where all
+    # four Catmull-Rom points lie inside)
+    lin = np.fromfunction(lambda z, y, x: 0.5 * z - y + 2 * x, (5, 5, 5))
+    up = nn.upsample(lin, (20, 20, 20), 4)
+    zf, yf, xf = np.meshgrid(*([(np.arange(20) + 0.5) / 4 - 0.5] * 3), indexing="ij")
+    inside = (zf >= 1) & (zf <= 3) & (yf >= 1) & (yf <= 3) & (xf >= 1) & (xf <= 3)
     assert np.allclose(up[inside], (0.5 * zf - yf + 2 * xf)[inside])
+    w = nn.catmull_rom(np.linspace(0, 1, 7))
+    assert np.allclose(sum(w), 1.0)
+    f2 = np.arange(8 * 8 * 8, dtype=float).reshape(8, 8, 8)
+    cs = nn.centre_sample(f2, 4)
+    assert cs.shape == (2, 2, 2)
+    assert np.isclose(cs[0, 0, 0], f2[1:3, 1:3, 1:3].mean())
