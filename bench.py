@@ -948,7 +948,7 @@ def run_gpu_warmstart(args, dist):
                 f"{args.ws_held} held out",
         "config": {"workload": f"learned warm start, 19-point Jacobi {shape[2]}x{shape[1]}x"
                                f"{shape[0]} (x,y,z; reduced from 129x129x257)",
-                   "network": "pool 4^3 -> 6 conv 3x3x3 x16 (BF16, FP32 acc.) -> trilinear",
+                   "network": "pool 4^3 -> 6 conv 3x3x3 x16 (BF16, FP32 acc.) -> Catmull-Rom",
                    "epochs": args.ws_epochs, "batch": 32,
                    "l2": "held-out stack: 14 arrays x 1.0 GB total > L2"},
         "compared_instances": int(both.sum()),

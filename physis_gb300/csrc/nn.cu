@@ -13,7 +13,7 @@
 // and transposed in channels; the weight gradient is a K = voxels GEMM per
 // tap, split over CTAs and reduced in a fixed order (deterministic).
 // Pooling (fine grids -> coarse network input), the MSE gradient, Adam and
-// trilinear upsampling (coarse prediction -> fine warm start) complete the
+// cubic upsampling (coarse prediction -> fine warm start) complete the
 // set.  Every kernel is checked against oracle/nn_oracle.py.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>

@@ -20,7 +20,9 @@ Pieces, all on the GPU through libphysis_gb300's C ABI:
   16 channels (ReLU between), BF16 weights and activations, FP32
   accumulation (PSWarmStartConv on tensor cores), trained with MSE and Adam
   (PSWarmStartWeightGrad, PSWarmStartLoss, PSWarmStartAdam); the coarse
-  prediction is upsampled trilinearly to the fine grid (PSWarmStartUpsample).
+  prediction is upsampled to the fine grid by Catmull-Rom cubic
+  interpolation (PSWarmStartUpsample); targets are sampled at the block
+  centres, so the upsampled target reproduces the solution to O(h^3).
 
 Relative residual: ||ss|| / ||ss(p = 0)|| with ss = (s0 a3 - p) bnd, the
 Himeno residual (examples/himeno/himenobmtxpa_original.c:331-334).
@@ -421,3 +423,31 @@ def predict_into(net, stack, data_scales, factor):
         _ok(L.PSWarmStartUpsample(ctypes.byref(f), _p(pred), ctypes.c_void_p(g.dev_ptr),
                                   net.stream()))
     torch.cuda.synchronize()
+
+
+def _time_forward(instances=1024, shape=(65, 33, 33), factor=4, reps=5):
+    """Times the forward pass of a randomly initialised network over the
+    coarse grids of `instances` instances (zeros: the arithmetic does not
+    depend on the values); returns milliseconds per pass and TFLOP/s."""
+    import torch
+    ps.init()
+    zc, yc, xc = coarse_shape(shape, factor)
+    net = Net(seed=0)
+    x = torch.zeros(instances * zc * yc * xc * C, dtype=torch.bfloat16, device="cuda")
+    dims = (instances, zc, yc, xc)
+    net.forward(x, dims)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        net.forward(x, dims)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) / reps * 1e3
+    flops = 2.0 * 27 * C * C * instances * zc * yc * xc * LAYERS
+    return ms, flops / (ms / 1e3) / 1e12
+
+
+if __name__ == "__main__":
+    import sys
+    n = int(sys.argv[1]) if len(sys.argv) > 1 else 1024
+    ms, tf = _time_forward(n)
+    print(f"network forward, {n} instances: {ms:.3f} ms, {tf:.1f} TFLOP/s")
