@@ -996,7 +996,7 @@ def main():
                          "19-point Jacobi 257x257x513 with fused residual")
     ap.add_argument("--ws-train", type=int, default=4096)
     ap.add_argument("--ws-held", type=int, default=256)
-    ap.add_argument("--ws-epochs", type=int, default=60)
+    ap.add_argument("--ws-epochs", type=int, default=200)
     ap.add_argument("--ws-nx", type=int, default=33)
     ap.add_argument("--ws-ny", type=int, default=33)
     ap.add_argument("--ws-nz", type=int, default=65)
