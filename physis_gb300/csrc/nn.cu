@@ -16,13 +16,17 @@
 // cubic upsampling (coarse prediction -> fine warm start) complete the
 // set.  Every kernel is checked against oracle/nn_oracle.py.
 #include <cuda_bf16.h>
+#include <stdlib.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "ps_arith.cuh"
 #include "ps_internal.h"
 
 namespace psg {
 namespace {
+
+int *g_err = nullptr;  // the runtime's device error word (bounded waits)
 
 constexpr int kC = 16;       // channels
 constexpr int kTaps = 27;
@@ -130,6 +134,149 @@ conv_kernel(const __nv_bfloat16 *__restrict__ x, const __nv_bfloat16 *__restrict
       *reinterpret_cast<__nv_bfloat162 *>(y + v * kC + co) = __floats2bfloat162_rn(r0, r1);
       if (yf && co == 0) yf[v] = r0;
     }
+  }
+}
+
+// ---- tcgen05 implicit GEMM -------------------------------------------------
+//
+// One CTA: M = 128 consecutive voxels, N = 16 output channels, K = 27 taps x
+// 16 input channels.  All 256 threads gather the 27 A tiles (each voxel's
+// neighbour row of 16 BF16 channels, zero outside) and the 27 B tiles (the
+// layer's [tap][out][in] weights) into shared memory in the canonical
+// no-swizzle K-major layout of 8-row x 16-byte core matrices (K-adjacent core
+// matrices 128 B apart, M/N-adjacent ones 256 B apart); one thread issues the
+// 27 tcgen05.mma (kind::f16, BF16 x BF16 -> FP32 in tensor memory) and
+// commits them to an mbarrier; after a bounded wait, warps 0-3 and 4-7 read
+// columns 0-7 and 8-15 of the 128 x 16 accumulator with tcgen05.ld and apply
+// the epilogue.  Tensor memory (32 columns) is allocated and freed by warp 0
+// on every path.
+constexpr int kTcM = 128;
+constexpr int kTcThreads = 256;
+constexpr int kTcATile = kTcM * kC * 2;   // 4096 B per tap
+constexpr int kTcBTile = kC * kC * 2;     // 512 B per tap
+constexpr size_t kTcSmem = 1024 + (size_t)kTaps * (kTcATile + kTcBTile) + 64;
+
+// Shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
+// offsets >> 4, descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor: FP32 accumulate, BF16 A and B, both K-major,
+// N = 16, M = 128.
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kC >> 3) << 17) |
+                              ((uint32_t)(kTcM >> 4) << 24);
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+conv_tc_kernel(const __nv_bfloat16 *__restrict__ x, const __nv_bfloat16 *__restrict__ w,
+               const float *__restrict__ bias, const __nv_bfloat16 *__restrict__ mask, int relu,
+               __nv_bfloat16 *__restrict__ y, float *__restrict__ yf, Dims d, int *err) {
+  extern __shared__ __align__(1024) unsigned char tc_raw[];
+  unsigned char *smem = tc_raw + ((1024u - (smem_u32(tc_raw) & 1023u)) & 1023u);
+  unsigned char *sa = smem;
+  unsigned char *sb = sa + kTaps * kTcATile;
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(sb + kTaps * kTcBTile);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long v0 = (long long)blockIdx.x * kTcM;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(
+                     smem_u32(tslot))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    fence_barrier_init();
+  }
+  // B tiles: row n (out channel) of 16 in-channels = two 16-byte halves
+  for (int i = tid; i < kTaps * kC * 2; i += kTcThreads) {
+    const int t = i / (kC * 2), n = (i / 2) % kC, c = i & 1;
+    const uint4 v = *reinterpret_cast<const uint4 *>(w + (t * kC + n) * kC + c * 8);
+    *reinterpret_cast<uint4 *>(sb + t * kTcBTile + (n >> 3) * 256 + c * 128 + (n & 7) * 16) = v;
+  }
+  // A tiles: thread = (row m, half c); 27 neighbour rows each
+  {
+    const int m = tid & (kTcM - 1), c = tid >> 7;
+    const Vox p = vox_of(v0 + m, d);
+    unsigned char *dst = sa + (m >> 3) * 256 + c * 128 + (m & 7) * 16;
+#pragma unroll 3
+    for (int t = 0; t < kTaps; ++t) {
+      const long long nb = nbr(p, t, d);
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (nb >= 0) v = *reinterpret_cast<const uint4 *>(x + nb * kC + c * 8);
+      *reinterpret_cast<uint4 *>(dst + t * kTcATile) = v;
+    }
+  }
+  // make the generic-proxy writes visible to the tensor core (async proxy)
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  if (tid == 0) {
+    const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+    for (int t = 0; t < kTaps; ++t) {
+      const uint64_t ad = umma_desc(a0 + t * kTcATile, 128, 256);
+      const uint64_t bd = umma_desc(b0 + t * kTcBTile, 128, 256);
+      asm volatile(
+          "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
+          "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+          "l"(ad), "l"(bd), "r"(kTcIdesc), "r"((uint32_t)(t > 0))
+          : "memory");
+    }
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(bar))
+        : "memory");
+  }
+  const bool ok = mbar_wait(bar, 0, err);
+  tc_fence_after();
+  // epilogue: warp quadrant q = rows 32q..32q+31, column half h
+  {
+    const int q = warp & 3, h = warp >> 2;
+    uint32_t r[8];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7])
+        : "r"(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(8 * h)));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    const long long v = v0 + 32 * q + lane;
+    if (ok && v < d.nvox) {
+      float f[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int co = 8 * h + i;
+        float a = __uint_as_float(r[i]);
+        if (bias) a += bias[co];
+        if (relu) a = fmaxf(a, 0.f);
+        if (mask && !(__bfloat162float(mask[v * kC + co]) > 0.f)) a = 0.f;
+        f[i] = a;
+      }
+      uint4 o;
+      __nv_bfloat162 *ob = reinterpret_cast<__nv_bfloat162 *>(&o);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) ob[i] = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+      *reinterpret_cast<uint4 *>(y + v * kC + 8 * h) = o;
+      if (yf && h == 0) yf[v] = f[0];
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem)
+                 : "memory");
   }
 }
 
@@ -407,10 +554,32 @@ __global__ void upsample_kernel(PoolArgs a, const float *__restrict__ coarse,
 
 }  // namespace
 
+void nn_set_error_word(int *err) { g_err = err; }
+
+static bool use_tcgen05() {
+  const char *e = getenv("PS_WARMSTART_TC");
+  return !(e && e[0] == '0');
+}
+
 int nn_conv(const void *x, const void *w, const float *bias, const void *mask, int relu,
             void *y, float *yf, int B, int Z, int Y, int X, cudaStream_t s) {
   Dims d{B, Z, Y, X, (long long)B * Z * Y * X};
   if (d.nvox <= 0) return 0;
+  if (use_tcgen05()) {
+    static bool attr = false;
+    if (!attr) {
+      const cudaError_t e = cudaFuncSetAttribute(
+          conv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+      if (e != cudaSuccess) return (int)e;
+      attr = true;
+    }
+    const long long blocks = (d.nvox + kTcM - 1) / kTcM;
+    conv_tc_kernel<<<(unsigned)blocks, kTcThreads, kTcSmem, s>>>(
+        static_cast<const __nv_bfloat16 *>(x), static_cast<const __nv_bfloat16 *>(w), bias,
+        static_cast<const __nv_bfloat16 *>(mask), relu, static_cast<__nv_bfloat16 *>(y), yf, d,
+        g_err);
+    return (int)cudaGetLastError();
+  }
   const long long blocks = (d.nvox + 16 * kConvWarps - 1) / (16 * kConvWarps);
   conv_kernel<<<(unsigned)blocks, 32 * kConvWarps, 0, s>>>(
       static_cast<const __nv_bfloat16 *>(x), static_cast<const __nv_bfloat16 *>(w), bias,

@@ -201,6 +201,10 @@ struct NNFields {
   float wscale, pscale;
 };
 // Each returns 0, -1 for invalid arguments, or the launch's cudaError_t.
+// Device error word for the kernels' bounded waits (set at PSInit).
+void nn_set_error_word(int *err);
+// The convolution runs as a tcgen05 implicit GEMM unless PS_WARMSTART_TC=0
+// selects the mma.sync kernel.
 int nn_conv(const void *x, const void *w, const float *bias, const void *mask, int relu,
             void *y, float *yf, int B, int Z, int Y, int X, cudaStream_t s);
 int nn_wgrad(const void *x, const void *dy, float *part, int S, float *dw, float *db, int B,

@@ -1543,6 +1543,7 @@ void PSInitV(int trace) {
   r->shapes[PS_KERNEL_HIMENO19] = MarchConfig{4, 1, 5, 2, 0};
   r->shapes[PS_KERNEL_HIMENO19_GOSA] = MarchConfig{4, 1, 5, 2, 0};
   cudaDeviceSynchronize();
+  psg::nn_set_error_word(r->dev_err);
   rt = r;
   if (!rt->tune_path.empty()) load_tuned(rt->tune_path.c_str());
 }

@@ -30,6 +30,23 @@ def rt():
     ps.clear_error()
 
 
+@pytest.fixture(params=["tcgen05", "mma.sync"])
+def conv_form(request):
+    """The convolution as a tcgen05 implicit GEMM (the default) and as the
+    mma.sync kernel (PS_WARMSTART_TC=0)."""
+    import os
+    old = os.environ.get("PS_WARMSTART_TC")
+    if request.param == "mma.sync":
+        os.environ["PS_WARMSTART_TC"] = "0"
+    else:
+        os.environ.pop("PS_WARMSTART_TC", None)
+    yield request.param
+    if old is None:
+        os.environ.pop("PS_WARMSTART_TC", None)
+    else:
+        os.environ["PS_WARMSTART_TC"] = old
+
+
 def _bf(a):
     """numpy float -> BF16 torch tensor on the GPU (flattened)."""
     return torch.tensor(nn.to_bf16(a).view(np.int16).ravel(), device="cuda").view(torch.bfloat16)
@@ -69,11 +86,11 @@ def _within_one_bf16_step(got, ref):
     return np.all(np.abs(got - ref) <= tol)
 
 
-DIMS = [(2, 5, 4, 7), (1, 3, 9, 2), (3, 17, 9, 9)]
+DIMS = [(2, 5, 4, 7), (1, 3, 9, 2), (3, 17, 9, 9), (7, 17, 9, 9)]
 
 
 @pytest.mark.parametrize("dims", DIMS)
-def test_conv_forward(rt, dims):
+def test_conv_forward(rt, conv_form, dims):
     rng = np.random.default_rng(1)
     x = nn.from_bf16(nn.to_bf16(rng.normal(size=dims + (16,))))
     w = _weights(rng)
@@ -97,7 +114,7 @@ def test_conv_forward(rt, dims):
 
 
 @pytest.mark.parametrize("dims", DIMS)
-def test_conv_backward_data_with_mask(rt, dims):
+def test_conv_backward_data_with_mask(rt, conv_form, dims):
     rng = np.random.default_rng(2)
     dy = nn.from_bf16(nn.to_bf16(rng.normal(size=dims + (16,))))
     mask = nn.from_bf16(nn.to_bf16(rng.normal(size=dims + (16,))))
@@ -213,7 +230,7 @@ def test_pool_and_upsample(rt):
     st.free()
 
 
-def test_network_gradients_match_oracle(rt):
+def test_network_gradients_match_oracle(rt, conv_form):
     # One forward + backward of the 6-layer network on the GPU against the
     # oracle's FP64 backprop on the same BF16 weights and input, with the
     # activations and propagated gradients rounded to BF16 where the GPU
