@@ -140,21 +140,24 @@ conv_kernel(const __nv_bfloat16 *__restrict__ x, const __nv_bfloat16 *__restrict
 // ---- tcgen05 implicit GEMM -------------------------------------------------
 //
 // One CTA: M = 128 consecutive voxels, N = 16 output channels, K = 27 taps x
-// 16 input channels.  All 256 threads gather the 27 A tiles (each voxel's
-// neighbour row of 16 BF16 channels, zero outside) and the 27 B tiles (the
-// layer's [tap][out][in] weights) into shared memory in the canonical
+// 16 input channels, in three phases of 9 taps (one z offset each).  Per
+// phase all 256 threads gather the 9 A tiles (each voxel's neighbour row of
+// 16 BF16 channels, zero outside) into shared memory in the canonical
 // no-swizzle K-major layout of 8-row x 16-byte core matrices (K-adjacent core
-// matrices 128 B apart, M/N-adjacent ones 256 B apart); one thread issues the
-// 27 tcgen05.mma (kind::f16, BF16 x BF16 -> FP32 in tensor memory) and
-// commits them to an mbarrier; after a bounded wait, warps 0-3 and 4-7 read
-// columns 0-7 and 8-15 of the 128 x 16 accumulator with tcgen05.ld and apply
-// the epilogue.  Tensor memory (32 columns) is allocated and freed by warp 0
-// on every path.
+// matrices 128 B apart, M-adjacent ones 256 B apart); one thread issues the 9
+// tcgen05.mma (kind::f16, BF16 x BF16 -> FP32 in tensor memory) and commits
+// them to an mbarrier; everyone waits (bounded) before the buffer is reused.
+// The 27 B tiles (the layer's [tap][out][in] weights) are staged once.  After
+// the last phase warps 0-3 and 4-7 read columns 0-7 and 8-15 of the 128 x 16
+// accumulator with tcgen05.ld and apply the epilogue.  52 KB of shared
+// memory: 4 CTAs per SM.  Tensor memory (32 columns) is allocated and freed
+// by warp 0 on every path.
 constexpr int kTcM = 128;
 constexpr int kTcThreads = 256;
+constexpr int kTcPhaseTaps = 9;
 constexpr int kTcATile = kTcM * kC * 2;   // 4096 B per tap
 constexpr int kTcBTile = kC * kC * 2;     // 512 B per tap
-constexpr size_t kTcSmem = 1024 + (size_t)kTaps * (kTcATile + kTcBTile) + 64;
+constexpr size_t kTcSmem = 1024 + (size_t)kTcPhaseTaps * kTcATile + (size_t)kTaps * kTcBTile + 64;
 
 // Shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
 // offsets >> 4, descriptor version 1, no swizzle.
@@ -175,14 +178,14 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(kTcThreads, 4)
 conv_tc_kernel(const __nv_bfloat16 *__restrict__ x, const __nv_bfloat16 *__restrict__ w,
                const float *__restrict__ bias, const __nv_bfloat16 *__restrict__ mask, int relu,
                __nv_bfloat16 *__restrict__ y, float *__restrict__ yf, Dims d, int *err) {
   extern __shared__ __align__(1024) unsigned char tc_raw[];
   unsigned char *smem = tc_raw + ((1024u - (smem_u32(tc_raw) & 1023u)) & 1023u);
   unsigned char *sa = smem;
-  unsigned char *sb = sa + kTaps * kTcATile;
+  unsigned char *sb = sa + kTcPhaseTaps * kTcATile;
   unsigned long long *bar = reinterpret_cast<unsigned long long *>(sb + kTaps * kTcBTile);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -204,43 +207,56 @@ conv_tc_kernel(const __nv_bfloat16 *__restrict__ x, const __nv_bfloat16 *__restr
     const uint4 v = *reinterpret_cast<const uint4 *>(w + (t * kC + n) * kC + c * 8);
     *reinterpret_cast<uint4 *>(sb + t * kTcBTile + (n >> 3) * 256 + c * 128 + (n & 7) * 16) = v;
   }
-  // A tiles: thread = (row m, half c); 27 neighbour rows each
-  {
-    const int m = tid & (kTcM - 1), c = tid >> 7;
-    const Vox p = vox_of(v0 + m, d);
-    unsigned char *dst = sa + (m >> 3) * 256 + c * 128 + (m & 7) * 16;
-#pragma unroll 3
-    for (int t = 0; t < kTaps; ++t) {
-      const long long nb = nbr(p, t, d);
+  // this thread's A row (voxel m, 16-byte half c) and its neighbour bounds
+  const int m = tid & (kTcM - 1), c = tid >> 7;
+  const Vox p = vox_of(v0 + m, d);
+  const long long vm = v0 + m;
+  const long long YX = (long long)d.Y * d.X;
+  const bool ylo = p.y > 0, yhi = p.y < d.Y - 1, xlo = p.x > 0, xhi = p.x < d.X - 1;
+  unsigned char *dst = sa + (m >> 3) * 256 + c * 128 + (m & 7) * 16;
+  const __nv_bfloat16 *src = x + vm * kC + c * 8;
+
+  bool ok = true;
+  uint32_t tmem = 0;
+  for (int g = 0; g < 3; ++g) {
+    const int dz = g - 1;
+    const bool zok = p.ok && (dz < 0 ? p.z > 0 : (dz > 0 ? p.z < d.Z - 1 : true));
+#pragma unroll
+    for (int k = 0; k < kTcPhaseTaps; ++k) {
+      const int dy = k / 3 - 1, dx = k % 3 - 1;
+      const bool in = zok && (dy < 0 ? ylo : (dy > 0 ? yhi : true)) &&
+                      (dx < 0 ? xlo : (dx > 0 ? xhi : true));
       uint4 v = make_uint4(0, 0, 0, 0);
-      if (nb >= 0) v = *reinterpret_cast<const uint4 *>(x + nb * kC + c * 8);
-      *reinterpret_cast<uint4 *>(dst + t * kTcATile) = v;
+      if (in) v = *reinterpret_cast<const uint4 *>(src + (dz * YX + dy * d.X + dx) * kC);
+      *reinterpret_cast<uint4 *>(dst + k * kTcATile) = v;
     }
-  }
-  // make the generic-proxy writes visible to the tensor core (async proxy)
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = *tslot;
-  if (tid == 0) {
-    const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
-    for (int t = 0; t < kTaps; ++t) {
-      const uint64_t ad = umma_desc(a0 + t * kTcATile, 128, 256);
-      const uint64_t bd = umma_desc(b0 + t * kTcBTile, 128, 256);
+    // make the generic-proxy writes visible to the tensor core (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    tmem = *tslot;
+    if (tid == 0) {
+      const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+      for (int k = 0; k < kTcPhaseTaps; ++k) {
+        const int t = g * kTcPhaseTaps + k;
+        const uint64_t ad = umma_desc(a0 + k * kTcATile, 128, 256);
+        const uint64_t bd = umma_desc(b0 + t * kTcBTile, 128, 256);
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(kTcIdesc), "r"((uint32_t)(t > 0))
+            : "memory");
+      }
       asm volatile(
-          "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
-          "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-          "l"(ad), "l"(bd), "r"(kTcIdesc), "r"((uint32_t)(t > 0))
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_u32(bar))
           : "memory");
     }
-    asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-            smem_u32(bar))
-        : "memory");
+    // the A buffer is reused by the next phase only after these MMAs are done
+    if (!mbar_wait(bar, (uint32_t)(g & 1), err)) ok = false;
+    tc_fence_after();
   }
-  const bool ok = mbar_wait(bar, 0, err);
-  tc_fence_after();
   // epilogue: warp quadrant q = rows 32q..32q+31, column half h
   {
     const int q = warp & 3, h = warp >> 2;
