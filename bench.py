@@ -967,7 +967,7 @@ def run_gpu_warmstart(args, dist):
                     "target_sweeps_mean": float(data.sweeps.mean())},
         "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s",
                      "frac": tflops / peak, "traffic": None, "peak_source": peak_kind,
-                     "what": "network forward over the training set (mma.sync BF16)"},
+                     "what": "network forward over the training set (tcgen05 BF16 implicit GEMM)"},
         "gpu_launches": None,
     }
     print(json.dumps(line), flush=True)
