@@ -329,6 +329,9 @@ def run_gpu(args, dist):
     if args.warps or args.rows or args.ns or args.ctas:
         ps.set_launch_shape(ps.PS_KERNEL_DIFFUSION7, warps=args.warps,
                             rows=args.rows, ns=args.ns, ctas_per_sm=args.ctas)
+    if args.temporal > 1:
+        tw, tr, tn = (int(v) for v in args.tshape.split(","))
+        ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, args.temporal, warps=tw, rows=tr, ns=tn)
     m1 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g1, g2], COEF)
     m2 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g2, g1], COEF)
     K, W = args.steps, args.warmup
@@ -417,6 +420,7 @@ def run_gpu(args, dist):
                                  "ns": shape_used[2],
                                  "ctas_per_sm": shape_used[4] or "auto"},
                 "e2e_job": "PSGridCopyin(pinned) + K steps + PSGridCopyout(pinned)",
+                "temporal_k": args.temporal,
             },
             "e2e": {"value": e2e, "unit": "GLUPS",
                     "h2d_bytes_per_step": nbytes / K,
@@ -994,6 +998,10 @@ def main():
                              "function7", "function27", "warmstart"],
                     help="diffusion: 7-point 512^3 (the headline); himeno: "
                          "19-point Jacobi 257x257x513 with fused residual")
+    ap.add_argument("--temporal", type=int, default=1,
+                    help="diffusion: temporal blocking depth k (1 = plain sweeps)")
+    ap.add_argument("--tshape", default="8,4,3",
+                    help="warps,rows,ring stages of the temporal passes")
     ap.add_argument("--ws-train", type=int, default=4096)
     ap.add_argument("--ws-held", type=int, default=256)
     ap.add_argument("--ws-epochs", type=int, default=200)
