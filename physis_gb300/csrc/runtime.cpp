@@ -893,8 +893,9 @@ std::vector<Plan> candidates(const std::vector<Map *> &ms) {
   for (auto &c : sh) out.push_back(Plan{MarchConfig{c[0], c[1], c[2], 0, 0}, 1, tdef});
   if (ms.size() == 2 && pair_eligible(*ms[0], *ms[1])) {
     const int maxk = psg::temporal7_max_k(m0.grids[0]->esz);
-    const int tc[][4] = {{2, 8, 2, 3}, {2, 8, 4, 3}, {2, 4, 4, 4}, {3, 8, 2, 4},
-                         {3, 8, 4, 3}, {4, 8, 4, 3}};
+    // {k, warps, rows, stages}; 4 rows at k >= 3 spill registers
+    const int tc[][4] = {{2, 8, 4, 3}, {2, 8, 2, 3}, {2, 4, 4, 3}, {3, 8, 2, 4},
+                         {3, 4, 2, 4}, {4, 8, 2, 4}};
     for (auto &c : tc) {
       if (c[0] > maxk) continue;
       out.push_back(Plan{MarchConfig{8, 2, 4, 0, 0}, c[0], MarchConfig{c[1], c[2], c[3], 0, 0}});

@@ -256,9 +256,6 @@ t7_kernel(const __grid_constant__ CUtensorMap tin, const TParams<T> p) {
     it.west_face = (it.x == 0);
     it.east_elem = p.nx - 1 - it.x;
     it.vec_in = it.out_lane && (it.x + VEC <= p.nx);
-    // Does E contain a cell on a grid face in x or y?  (z faces are uniform
-    // per plane and handled in every item.)
-    const bool edge = xe0 <= 0 || xe0 + 32 * VEC >= p.nx || ye0 <= 0 || ye0 + TYE >= p.ny;
 
     T Q[K][3][RY][VEC];
     {
@@ -284,13 +281,13 @@ t7_kernel(const __grid_constant__ CUtensorMap tin, const TParams<T> p) {
     const T *prev_in = ring + ((cstage + ns - 1) % ns) * plane_elems;  // plane 1
 
     // One pipeline step for input plane q, with rotation R of the slots.
+// One step body per slot rotation (three in all).  Every tile runs the
+// clamp-aware body: a second, clamp-free copy for interior tiles doubled the
+// code and cost more in instruction-cache misses than its selects saved.
 #define PS_T7_STEP(R)                                                         \
   {                                                                           \
     const T *in_t = wait_next();                                              \
-    if (edge)                                                                 \
-      t7_step<T, RY, K, R, true>(Q, in_t, prev_in, zin0 + q, p, it, ok);      \
-    else                                                                      \
-      t7_step<T, RY, K, R, false>(Q, in_t, prev_in, zin0 + q, p, it, ok);     \
+    t7_step<T, RY, K, R, true>(Q, in_t, prev_in, zin0 + q, p, it, ok);        \
     prev_in = in_t;                                                           \
     ok = __syncthreads_and(ok);                                               \
     if (!ok) break;                                                           \
