@@ -873,18 +873,26 @@ def run_gpu_warmstart(args, dist):
     import physis_gb300 as ps
     from physis_gb300 import warmstart as ws
     ps.init()
-    shape = (args.ws_nz, args.ws_ny, args.ws_nx)
-    factor = 4
+    if args.ws_full:
+        # the specified 129 x 129 x 257 (x, y, z); 16^3 blocks give the network
+        # the same 17 x 9 x 9 coarse grid as the reduced instances; 16
+        # instances side by side in x keep the sweep's 128-wide tiles full
+        shape, factor, nsx, per_stack, chunk = (257, 129, 129), 16, 16, 64, 2000
+    else:
+        shape, factor, nsx, per_stack, chunk = (args.ws_nz, args.ws_ny, args.ws_nx), 4, 15, 300, 256
     rng = np.random.default_rng(5)
+    workers = min(16, os.cpu_count() or 1)
     t0 = time.perf_counter()
-    data = ws.Dataset(rng, args.ws_train, shape, factor, tol=1e-7, chunk=256,
-                      max_sweeps=args.ws_max_sweeps)
+    data = ws.Dataset(rng, args.ws_train, shape, factor, nsx=nsx, per_stack=per_stack, tol=1e-7,
+                      chunk=chunk, max_sweeps=args.ws_max_sweeps, workers=workers)
     data_s = time.perf_counter() - t0
     net = ws.Net(seed=1)
     hist, train_s = ws.train(net, data, epochs=args.ws_epochs, batch=32, lr=2e-3)
 
-    held = [ws.make_instance(rng, shape) for _ in range(args.ws_held)]
-    st = ws.Stack(held, shape, nsx=15)
+    held = ws.make_instances(rng, args.ws_held, shape, workers)
+    st = ws.Stack(held, shape, nsx=min(nsx, args.ws_held))
+    echunk = 500 if args.ws_full else 32
+    stack_gb = 14 * 4 * float(np.prod(st.gshape)) / 1e9
     zeros = np.zeros(st.gshape, np.float32)
 
     def reset():
@@ -897,11 +905,11 @@ def run_gpu_warmstart(args, dist):
     # 1e-6 never get there from either start and are left out of the
     # comparison (counted in the output).
     reset()
-    zero = st.solve(1e-6, 32, args.ws_max_sweeps)
+    zero = st.solve(1e-6, echunk, args.ws_max_sweeps)
     reset()
     ws.predict_into(net, st, scales, factor)
     r_warm0 = st.residuals()
-    warm = st.solve(1e-6, 32, args.ws_max_sweeps)
+    warm = st.solve(1e-6, echunk, args.ws_max_sweeps)
     both = (zero > 0) & (warm > 0)
     nz_sw, nw_sw = int(zero[both].max()), int(warm[both].max())
 
@@ -919,9 +927,10 @@ def run_gpu_warmstart(args, dist):
     for _ in range(max(args.warmup, 3) // 3):  # warm-up of both paths
         timed(False, 32)
         timed(True, 32)
-    tz = min(timed(False, nz_sw) for _ in range(2))
+    reps = 1 if args.ws_full else 2
+    tz = min(timed(False, nz_sw) for _ in range(reps))
     r_zero_end = st.residuals()
-    tw = min(timed(True, nw_sw) for _ in range(2))
+    tw = min(timed(True, nw_sw) for _ in range(reps))
     r_end = st.residuals()  # after the warm timed run
     # instances at or below 1e-6 after the timed runs (a few whose float32
     # floor lies just under 1e-6 can drift back above it between checks)
@@ -951,10 +960,13 @@ def run_gpu_warmstart(args, dist):
         "data": f"synthetic seeded instances (seed 5), {args.ws_train} solved for training, "
                 f"{args.ws_held} held out",
         "config": {"workload": f"learned warm start, 19-point Jacobi {shape[2]}x{shape[1]}x"
-                               f"{shape[0]} (x,y,z; reduced from 129x129x257)",
+                               f"{shape[0]} (x,y,z" +
+                               ("; the specified size)" if args.ws_full
+                                else "; reduced from 129x129x257)"),
+                   "pool_factor": factor, "sweep_count_resolution": echunk,
                    "network": "pool 4^3 -> 6 conv 3x3x3 x16 (BF16, FP32 acc.) -> Catmull-Rom",
                    "epochs": args.ws_epochs, "batch": 32,
-                   "l2": "held-out stack: 14 arrays x 1.0 GB total > L2"},
+                   "l2": f"held-out stack: 14 arrays, {stack_gb:.1f} GB in all, > L2"},
         "compared_instances": int(both.sum()),
         "below_1e-6_unreachable": {"zero_start": int((zero <= 0).sum()),
                                    "warm_start": int((warm <= 0).sum())},
@@ -1009,6 +1021,9 @@ def main():
     ap.add_argument("--ws-ny", type=int, default=33)
     ap.add_argument("--ws-nz", type=int, default=65)
     ap.add_argument("--ws-max-sweeps", type=int, default=12000)
+    ap.add_argument("--ws-full", action="store_true",
+                    help="config 5 at the specified 129x129x257 (use --ws-train/--ws-held "
+                         "to size it, e.g. 128/32, and --ws-max-sweeps 100000)")
     args = ap.parse_args()
     global N
     N = args.n

@@ -325,11 +325,28 @@ def loss_grad(pred, target, work64):
 
 # ---- data, training, evaluation -------------------------------------------------
 
+def _instance_job(args):
+    seed, shape = args
+    return make_instance(np.random.default_rng(seed), shape)
+
+
+def make_instances(rng, count, shape, workers=0):
+    """count instances; with workers > 1 they are built in a spawned process
+    pool (each from its own seed drawn from rng, so the result does not
+    depend on the number of workers)."""
+    seeds = [int(v) for v in rng.integers(0, 2 ** 63 - 1, size=count)]
+    if workers <= 1 or count < 2:
+        return [_instance_job((sd, shape)) for sd in seeds]
+    import multiprocessing as mp
+    with mp.get_context("spawn").Pool(workers) as pool:
+        return pool.map(_instance_job, [(sd, shape) for sd in seeds])
+
+
 class Dataset:
     """Pooled inputs and targets of many instances, resident on the GPU."""
 
     def __init__(self, rng, count, shape, factor, nsx=15, per_stack=300, tol=1e-7,
-                 chunk=256, max_sweeps=40000, wscale=None, pscale=None, log=None):
+                 chunk=256, max_sweeps=40000, wscale=None, pscale=None, log=None, workers=0):
         import torch
         self.shape, self.factor = shape, factor
         zc, yc, xc = coarse_shape(shape, factor)
@@ -343,7 +360,7 @@ class Dataset:
         done = 0
         while done < count:
             k = min(per_stack, count - done)
-            insts = [make_instance(rng, shape) for _ in range(k)]
+            insts = make_instances(rng, k, shape, workers)
             if self.wscale is None:
                 self.wscale = 1.0 / float(np.std(np.concatenate([i["wrk1"].ravel() for i in insts])))
             st = Stack(insts, shape, nsx)
