@@ -964,7 +964,8 @@ def run_gpu_warmstart(args, dist):
                                ("; the specified size)" if args.ws_full
                                 else "; reduced from 129x129x257)"),
                    "pool_factor": factor, "sweep_count_resolution": echunk,
-                   "network": "pool 4^3 -> 6 conv 3x3x3 x16 (BF16, FP32 acc.) -> Catmull-Rom",
+                   "network": f"pool {factor}^3 -> 6 conv 3x3x3 x16 (BF16, FP32 acc.) "
+                              "-> Catmull-Rom",
                    "epochs": args.ws_epochs, "batch": 32,
                    "l2": f"held-out stack: 14 arrays, {stack_gb:.1f} GB in all, > L2"},
         "compared_instances": int(both.sum()),
