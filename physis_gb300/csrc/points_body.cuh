@@ -16,7 +16,7 @@ namespace psg {
 
 constexpr int kPtsTX = 128;       // tile width in cells
 constexpr int kPtsVX = 4;         // columns per lane (lane + 32*j)
-constexpr int kPtsPrefetch = 2;   // planes in flight ahead of the newest needed plane
+constexpr int kPtsPrefetch = 2;   // cp.async ring: planes in flight ahead of the newest needed one
 constexpr int kPtsMaxPoints = 64;
 // Shared memory: point table (run-time spec only: offsets, lags, weights),
 // then the ring's mbarriers, then the ring (128-byte aligned stages).
