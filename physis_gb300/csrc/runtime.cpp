@@ -495,7 +495,8 @@ int shape_slot(int kernel) {
 
 // One point-stencil map: one launch per colour it runs.
 bool launch_points_map(const Map &m, const PointStencil &ps) {
-  psg::PointsArgs a;
+  psg::PointsArgs a{};
+  a.has_tmap = true;  // planes arrive by TMA (sizes the ring below)
   a.in = view(m.grids[0]);
   a.out = view(m.grids[1]);
   for (int d = 0; d < 3; ++d) {
@@ -534,7 +535,7 @@ bool launch_points_map(const Map &m, const PointStencil &ps) {
 
 // One plain sweep of a 7-point-family map with explicit input/output views.
 bool launch_s7(const Map &m, const GridView &in, const GridView &out) {
-  psg::Stencil7Args a;
+  psg::Stencil7Args a{};
   a.kernel = m.kernel;
   a.in = in;
   a.out = out;
@@ -591,7 +592,7 @@ bool launch_map(const Map &m, bool want_gosa) {
     return true;  // empty domain: nothing to do, as in the REF loops
   cudaError_t e;
   if (m.kernel == PS_KERNEL_HIMENO19 || m.kernel == PS_KERNEL_HIMENO19_GOSA) {
-    psg::Himeno19Args a;
+    psg::Himeno19Args a{};
     for (int i = 0; i < 14; ++i) a.g[i] = view(m.grids[i]);
     a.dom = box;
     a.omega = (float)m.scalars[0];
@@ -617,7 +618,7 @@ bool launch_map(const Map &m, bool want_gosa) {
 
 // One temporal pass: out = k steps of map m's stencil applied to in.
 bool launch_t7(const Map &m, const GridView &in, const GridView &out, int k) {
-  psg::Temporal7Args a;
+  psg::Temporal7Args a{};
   a.in = in;
   a.out = out;
   a.k = k;
