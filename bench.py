@@ -884,10 +884,13 @@ def run_gpu_warmstart(args, dist):
     workers = min(16, os.cpu_count() or 1)
     t0 = time.perf_counter()
     data = ws.Dataset(rng, args.ws_train, shape, factor, nsx=nsx, per_stack=per_stack, tol=1e-7,
-                      chunk=chunk, max_sweeps=args.ws_max_sweeps, workers=workers)
+                      chunk=chunk, max_sweeps=args.ws_max_sweeps, workers=workers,
+                      mirrors=args.ws_mirrors)
     data_s = time.perf_counter() - t0
     net = ws.Net(seed=1)
-    hist, train_s = ws.train(net, data, epochs=args.ws_epochs, batch=32, lr=2e-3)
+    per_epoch = max(1, data.x.shape[0] // 32)
+    epochs = max(1, round(args.ws_steps / per_epoch))
+    hist, train_s = ws.train(net, data, epochs=epochs, batch=32, lr=2e-3)
 
     held = ws.make_instances(rng, args.ws_held, shape, workers)
     st = ws.Stack(held, shape, nsx=min(nsx, args.ws_held))
@@ -957,16 +960,17 @@ def run_gpu_warmstart(args, dist):
         "value": tz / tw, "unit": "x", "n_gpus": 1, "steps": args.ws_held,
         "warmup": max(args.warmup, 3), "ms_per_step": tw / args.ws_held * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16",
-        "data": f"synthetic seeded instances (seed 5), {args.ws_train} solved for training, "
-                f"{args.ws_held} held out",
+        "data": f"synthetic seeded instances (seed 5), {args.ws_train} solved for training "
+                f"(x {len(data.flips)} mirror images), {args.ws_held} held out",
         "config": {"workload": f"learned warm start, 19-point Jacobi {shape[2]}x{shape[1]}x"
                                f"{shape[0]} (x,y,z" +
                                ("; the specified size)" if args.ws_full
                                 else "; reduced from 129x129x257)"),
                    "pool_factor": factor, "sweep_count_resolution": echunk,
-                   "network": f"pool {factor}^3 -> 6 conv 3x3x3 x16 (BF16, FP32 acc.) "
+                   "network": f"pool {factor}^3 (9 channels) -> 6 conv 3x3x3 x16 (BF16, FP32 acc.) "
                               "-> Catmull-Rom",
-                   "epochs": args.ws_epochs, "batch": 32,
+                   "epochs": epochs, "adam_steps": epochs * per_epoch, "batch": 32,
+                   "mirror_images": len(data.flips),
                    "l2": f"held-out stack: 14 arrays, {stack_gb:.1f} GB in all, > L2"},
         "compared_instances": int(both.sum()),
         "below_1e-6_unreachable": {"zero_start": int((zero <= 0).sum()),
@@ -1017,7 +1021,10 @@ def main():
                     help="warps,rows,ring stages of the temporal passes")
     ap.add_argument("--ws-train", type=int, default=4096)
     ap.add_argument("--ws-held", type=int, default=256)
-    ap.add_argument("--ws-epochs", type=int, default=200)
+    ap.add_argument("--ws-steps", type=int, default=25600,
+                    help="warm start: Adam steps (minibatches of 32) of training")
+    ap.add_argument("--ws-mirrors", type=int, default=16,
+                    help="warm start: training pairs per solved instance (its mirror images)")
     ap.add_argument("--ws-nx", type=int, default=33)
     ap.add_argument("--ws-ny", type=int, default=33)
     ap.add_argument("--ws-nz", type=int, default=65)

@@ -269,7 +269,9 @@ int PSStencilFunctionNew(const char *source, const char *name);
 /* Parses and compiles a stencil function like PSStencilFunctionNew without
  * loading it (no device or PSInit needed).  Returns PS_OK, else
  * PS_ERR_INVALID_ARGUMENT (the reason and compiler log, truncated, in
- * log[0..logsize)) or PS_ERR_UNSUPPORTED without NVRTC. */
+ * log[0..logsize)) or PS_ERR_UNSUPPORTED without NVRTC.  On success log
+ * names the grids the tiled entry stages in shared memory, one
+ * "staged <grid> <rx> <ry> <rz> <clamp|periodic>;" each ("" if none). */
 int PSStencilFunctionCheck(const char *source, const char *name, char *log, size_t logsize);
 
 /* Map colours: every cell, red (x + y + z even), black (odd), red then black. */
@@ -332,10 +334,17 @@ typedef struct PSWarmStartFields {
   int ny;
   int inx, iny, inz, nsx, factor, batch;
   float wscale, pscale;
+  /* Mirror image the pooling calls read (0: the instance itself): bits 0, 1,
+   * 2 mirror x, y, z; bit 3 swaps x and y together with a2 and a1, the x
+   * and y coefficients (needs inx == iny).  With c_i = a_i and b = 0 the mirrored fields' solution is
+   * the mirrored solution.  PSWarmStartUpsample needs 0. */
+  int flip;
 } PSWarmStartFields;
 
-/* Network input: per factor^3 block of each instance, channels mean ln a0,
- * mean ln a1, mean ln a2, mean wrk1 * wscale, mean bnd, then zeros. */
+/* Network input: per factor^3 block of each instance (of its mirror image),
+ * channels: mean ln a0, mean ln a1, mean ln a2, mean wrk1 * wscale, mean bnd,
+ * mean wrk1 * 3 / (a0 + a1 + a2) * wscale, -ln mean(1 / a0), -ln mean(1 / a1),
+ * -ln mean(1 / a2), then zeros. */
 int PSWarmStartPool(const PSWarmStartFields *f, void *out, void *stream);
 /* Training target: p at each block's centre (c + 0.5) * factor - 0.5, the
  * mean of the fine cells nearest to it, times pscale (FP32). */

@@ -187,3 +187,46 @@ def upsample(coarse, shape, f):
             acc = acc + np.take(out, idx, axis=axis) * w.reshape(sh)
         out = acc
     return out
+
+
+def mirror(field, flip):
+    """Mirror image of a [z, y, x] field: flip bits 0/1/2 mirror x/y/z and bit
+    3 swaps x and y (the swap is applied to the stored field first, then the
+    mirrors, so image(z', y', x') = field(z, y, x) with x1 = mirrored x',
+    y1 = mirrored y' and (x, y) = (y1, x1) under the swap)."""
+    a = np.asarray(field)
+    if flip & 8:
+        a = a.transpose(0, 2, 1)
+    if flip & 1:
+        a = a[:, :, ::-1]
+    if flip & 2:
+        a = a[:, ::-1, :]
+    if flip & 4:
+        a = a[::-1, :, :]
+    return np.ascontiguousarray(a)
+
+
+def mirror_instance(inst, flip):
+    """The mirrored instance: every field mirrored, a2 and a1 exchanged under
+    the x/y swap (the 19-point sweep weighs the z neighbours with a0, the y
+    neighbours with a1 and the x neighbours with a2)."""
+    out = {k: mirror(v, flip) for k, v in inst.items()}
+    if flip & 8:
+        out["a1"], out["a2"] = out["a2"], out["a1"]
+    return out
+
+
+POOL_CHANNELS = 9
+
+
+def pool_features(inst, f, wscale):
+    """The network input of one instance, [zc, yc, xc, 9] float64: block means
+    of ln a0, ln a1, ln a2, wrk1 * wscale, bnd, wrk1 * 3 / (a0 + a1 + a2) *
+    wscale, and -ln of the block means of 1 / a0, 1 / a1, 1 / a2."""
+    a0, a1, a2 = (np.asarray(inst[k], np.float64) for k in ("a0", "a1", "a2"))
+    w = np.asarray(inst["wrk1"], np.float64)
+    feats = [pool(np.log(a0), f), pool(np.log(a1), f), pool(np.log(a2), f),
+             pool(w, f) * wscale, pool(np.asarray(inst["bnd"], np.float64), f),
+             pool(w * 3.0 / (a0 + a1 + a2), f) * wscale,
+             -np.log(pool(1.0 / a0, f)), -np.log(pool(1.0 / a1, f)), -np.log(pool(1.0 / a2, f))]
+    return np.stack(feats, axis=-1)

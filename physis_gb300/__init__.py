@@ -82,7 +82,7 @@ class PSWarmStartFields(ctypes.Structure):
                 ("pitch", ctypes.c_longlong), ("ny", ctypes.c_int), ("inx", ctypes.c_int),
                 ("iny", ctypes.c_int), ("inz", ctypes.c_int), ("nsx", ctypes.c_int),
                 ("factor", ctypes.c_int), ("batch", ctypes.c_int), ("wscale", ctypes.c_float),
-                ("pscale", ctypes.c_float)]
+                ("pscale", ctypes.c_float), ("flip", ctypes.c_int)]
 
 
 class PSError(RuntimeError):

@@ -25,7 +25,9 @@
 #include <cuda_runtime.h>
 #include <dlfcn.h>
 
+#include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <regex>
 #include <string>
@@ -138,10 +140,27 @@ bool load_driver(std::string *err) {
 // arithmetic as the reference's (physis_cuda.h:237-269): x fastest, periodic
 // reads wrap with (i + n) % n.
 const char *kPrelude = R"PSJIT(
+#include "ps_arith.cuh"
 typedef int PSIndex;
-template <typename T> struct __PSGridDev {
+// Kernel parameter (host layout: GridArg in jit.cpp).
+template <typename T> struct __PSGridArg {
   T *p; long long row; long long plane; int nx; int ny; int nz; int rank; long long cur;
 };
+// What the stencil function sees.  A grid the tiled entry staged in shared
+// memory (staged == 1) answers reads inside its window -- x in [sx0, sx0 + sw),
+// y in [sy0, sy0 + sh), z within rz of the current plane sz -- from plane
+// pointer pl[z - sz + 4]; every other read goes to global memory.
+template <typename T> struct __PSGridDev {
+  T *p; long long row; long long plane; int nx; int ny; int nz; int rank; long long cur;
+  int staged, sx0, sy0, sz, sw, sh, rz;
+  const T *pl[9];
+};
+template <typename T> __device__ __forceinline__ __PSGridDev<T> __ps_dev(const __PSGridArg<T> &a) {
+  __PSGridDev<T> g;
+  g.p = a.p; g.row = a.row; g.plane = a.plane; g.nx = a.nx; g.ny = a.ny; g.nz = a.nz;
+  g.rank = a.rank; g.cur = 0; g.staged = 0;
+  return g;
+}
 #define __PS_GRID_TYPES(N, T) \
   typedef __PSGridDev<T> PSGrid1D##N; typedef __PSGridDev<T> PSGrid2D##N; \
   typedef __PSGridDev<T> PSGrid3D##N;
@@ -149,6 +168,16 @@ __PS_GRID_TYPES(Float, float)
 __PS_GRID_TYPES(Double, double)
 __PS_GRID_TYPES(Int, int)
 __PS_GRID_TYPES(Long, long long)
+template <typename T>
+__device__ __forceinline__ bool __ps_in_stage(const __PSGridDev<T> &g, int x, int y, int z) {
+  const int dz = z - g.sz;
+  return g.staged && dz >= -g.rz && dz <= g.rz && (unsigned)(x - g.sx0) < (unsigned)g.sw &&
+         (unsigned)(y - g.sy0) < (unsigned)g.sh;
+}
+template <typename T>
+__device__ __forceinline__ T __ps_staged(const __PSGridDev<T> &g, int x, int y, int z) {
+  return g.pl[z - g.sz + 4][(y - g.sy0) * g.sw + (x - g.sx0)];
+}
 template <typename T> __device__ __forceinline__ T __ps_get(const __PSGridDev<T> &g, int x) {
   return g.p[x];
 }
@@ -157,6 +186,7 @@ template <typename T> __device__ __forceinline__ T __ps_get(const __PSGridDev<T>
 }
 template <typename T>
 __device__ __forceinline__ T __ps_get(const __PSGridDev<T> &g, int x, int y, int z) {
+  if (__ps_in_stage(g, x, y, z)) return __ps_staged(g, x, y, z);
   return g.p[(long long)z * g.plane + (long long)y * g.row + x];
 }
 template <typename T> __device__ __forceinline__ T __ps_getp(const __PSGridDev<T> &g, int x) {
@@ -166,8 +196,11 @@ template <typename T>
 __device__ __forceinline__ T __ps_getp(const __PSGridDev<T> &g, int x, int y) {
   return g.p[(long long)((y + g.ny) % g.ny) * g.row + (x + g.nx) % g.nx];
 }
+// Staged windows of periodic grids hold the wrapped values at the unwrapped
+// coordinates, so the window is looked up before wrapping.
 template <typename T>
 __device__ __forceinline__ T __ps_getp(const __PSGridDev<T> &g, int x, int y, int z) {
+  if (__ps_in_stage(g, x, y, z)) return __ps_staged(g, x, y, z);
   return g.p[(long long)((z + g.nz) % g.nz) * g.plane + (long long)((y + g.ny) % g.ny) * g.row +
              (x + g.nx) % g.nx];
 }
@@ -178,6 +211,33 @@ template <typename T> __device__ __forceinline__ int __ps_dim(const __PSGridDev<
 #define PSGridGetPeriodic(g, ...) __ps_getp((g), __VA_ARGS__)
 #define PSGridEmit(g, v) ((void)((g).p[(g).cur] = (v)))
 #define PSGridDim(g, d) __ps_dim((g), (d))
+
+// ---- staging for the tiled entry ----
+template <int S> __device__ __forceinline__ int __ps_slot(int z) { return ((z % S) + S) % S; }
+template <bool PER> __device__ __forceinline__ int __ps_fit(int v, int n) {
+  if (PER) {
+    if ((unsigned)v >= (unsigned)n) {
+      v %= n;
+      if (v < 0) v += n;
+    }
+    return v;
+  }
+  return min(max(v, 0), n - 1);
+}
+// Plane zp (unwrapped) of the W x H window at (x0 - RX, y0 - RY) into its
+// ring slot, one cp.async per cell; cells outside the grid wrap (PER) or
+// clamp.
+template <typename T, int W, int H, int S, int RX, int RY, bool PER>
+__device__ __forceinline__ void __ps_stage(T *ring, const __PSGridArg<T> &a, int x0, int y0,
+                                           int zp) {
+  T *dst = ring + __ps_slot<S>(zp) * (W * H);
+  const T *src = a.p + (long long)__ps_fit<PER>(zp, a.nz) * a.plane;
+  for (int e = threadIdx.x; e < W * H; e += 256) {
+    const int r = e / W, c = e - r * W;
+    const int gy = __ps_fit<PER>(y0 - RY + r, a.ny), gx = __ps_fit<PER>(x0 - RX + c, a.nx);
+    psg::cp_async_small<(int)sizeof(T)>(dst + e, src + (long long)gy * a.row + gx);
+  }
+}
 )PSJIT";
 
 // Host mirror of __PSGridDev<T> (same layout for every T: one pointer).
@@ -214,6 +274,7 @@ bool parse_param(const std::string &decl, JitParam *p, std::string *err) {
     if (!(c == ' ' && (t.empty() || t.back() == ' '))) t += (c == '\t' ? ' ' : c);
   type = trim(t);
   p->decl_type = type;
+  p->name = trim(d.substr(cut + 1));
   std::smatch m;
   if (std::regex_match(type, m, grid_re)) {
     p->grid = true;
@@ -274,7 +335,7 @@ bool parse_signature(const std::string &src, const std::string &name, JitKernel 
     JitParam p;
     if (!parse_param(d, &p, err)) return false;
     if (!p.grid && !seen_grid && p.type == kInt && k->params.empty() && k->nd < 3) {
-      ++k->nd;  // a leading index parameter
+      k->idx[k->nd++] = p.name;  // a leading index parameter
       continue;
     }
     if (p.grid) seen_grid = true;
@@ -306,6 +367,33 @@ std::string scalar_ctype(int type) {
   }
 }
 
+// Source expression of the grid argument arg in an entry: the device view
+// g<i> the entry built from kernel parameter a<i>.
+std::string cur_expr(const JitParam &p, const std::string &g) {
+  return p.rank == 1 ? std::string("x")
+         : p.rank == 2 ? "(long long)y * " + g + ".row + x"
+                       : "(long long)z * " + g + ".plane + (long long)y * " + g + ".row + x";
+}
+
+std::string entry_params(const JitKernel &k) {
+  std::string s;
+  for (size_t i = 0; i < k.params.size(); ++i) {
+    const JitParam &p = k.params[i];
+    s += ", " + (p.grid ? "__PSGridArg<" + scalar_ctype(p.type) + ">" : scalar_ctype(p.type)) +
+         " a" + std::to_string(i);
+  }
+  return s;
+}
+
+std::string call_source(const JitKernel &k) {
+  std::string s = k.name + "(x";
+  if (k.nd >= 2) s += ", y";
+  if (k.nd >= 3) s += ", z";
+  for (size_t i = 0; i < k.params.size(); ++i)
+    s += (k.params[i].grid ? ", g" : ", a") + std::to_string(i);
+  return s + ");\n";
+}
+
 // The generated entry: one thread per (x, y), a z-chunk per block row in z;
 // red/black maps visit every other x from the REF start
 // min + ((min & 1) ^ ((y + z + color) % 2))
@@ -313,13 +401,12 @@ std::string scalar_ctype(int type) {
 std::string entry_source(const JitKernel &k) {
   std::string s =
       "\nextern \"C\" __global__ void __launch_bounds__(256) __ps_entry(int dmin0, int dmax0, "
-      "int dmin1, int dmax1, int dmin2, int dmax2, int color, int zlen";
-  for (size_t i = 0; i < k.params.size(); ++i) {
-    const JitParam &p = k.params[i];
-    s += ", " + (p.grid ? p.decl_type : scalar_ctype(p.type)) + " a" + std::to_string(i);
-  }
-  s += ") {\n"
-       "  const int tx = blockIdx.x * blockDim.x + threadIdx.x;\n"
+      "int dmin1, int dmax1, int dmin2, int dmax2, int color, int zlen" +
+      entry_params(k) + ") {\n";
+  for (size_t i = 0; i < k.params.size(); ++i)
+    if (k.params[i].grid)
+      s += "  auto g" + std::to_string(i) + " = __ps_dev(a" + std::to_string(i) + ");\n";
+  s += "  const int tx = blockIdx.x * blockDim.x + threadIdx.x;\n"
        "  const int y = dmin1 + blockIdx.y * blockDim.y + threadIdx.y;\n"
        "  if (y >= dmax1) return;\n"
        "  const int zs = dmin2 + blockIdx.z * zlen;\n"
@@ -330,36 +417,203 @@ std::string entry_source(const JitKernel &k) {
        "    if (x >= dmax0) continue;\n";
   for (size_t i = 0; i < k.params.size(); ++i) {
     if (!k.params[i].grid) continue;
-    const std::string a = "a" + std::to_string(i);
-    const int r = k.params[i].rank;
-    s += "    " + a + ".cur = " +
-         (r == 1 ? std::string("x")
-                 : r == 2 ? "(long long)y * " + a + ".row + x"
-                          : "(long long)z * " + a + ".plane + (long long)y * " + a +
-                                ".row + x") +
-         ";\n";
+    const std::string g = "g" + std::to_string(i);
+    s += "    " + g + ".cur = " + cur_expr(k.params[i], g) + ";\n";
   }
-  s += "    " + k.name + "(x";
-  if (k.nd >= 2) s += ", y";
-  if (k.nd >= 3) s += ", z";
-  for (size_t i = 0; i < k.params.size(); ++i) s += ", a" + std::to_string(i);
-  s += ");\n  }\n}\n";
+  s += "    " + call_source(k) + "  }\n}\n";
+  return s;
+}
+
+// ---- the tiled entry ---------------------------------------------------------
+// A CTA of 256 threads owns a 64 x 16 (x, y) tile and a chunk of z.  Grids
+// the stencil reads at neighbour offsets (and never emits to) are staged:
+// each z step copies one plane of the tile plus halo into a ring of 2 rz + 3
+// shared-memory planes with cp.async, one plane ahead of the compute, and the
+// function's reads inside the window come from there.  The reads themselves
+// are unchanged, so every result is bit-identical to the plain entry's.
+constexpr int kTileX = 64, kTileY = 16;
+constexpr size_t kStageBudget = 96 * 1024;  // two or more CTAs per SM
+
+// Splits the argument list of the call whose '(' is at src[open] into its
+// top-level arguments; npos-safe (returns false if unbalanced).
+bool call_args(const std::string &src, size_t open, std::vector<std::string> *args,
+               size_t *close) {
+  int depth = 0;
+  std::string cur;
+  for (size_t i = open; i < src.size(); ++i) {
+    const char c = src[i];
+    if (c == '(' || c == '[' || c == '{') {
+      if (depth++ > 0) cur += c;
+      continue;
+    }
+    if (c == ')' || c == ']' || c == '}') {
+      if (--depth == 0) {
+        args->push_back(cur);
+        *close = i;
+        return true;
+      }
+      cur += c;
+      continue;
+    }
+    if (c == ',' && depth == 1) {
+      args->push_back(cur);
+      cur.clear();
+      continue;
+    }
+    cur += c;
+  }
+  return false;
+}
+
+// Chooses the staged grids of a 3D stencil from its source text.  A grid is
+// staged when some PSGridGet / PSGridGetPeriodic of it reads off the centre
+// and no PSGridEmit anywhere in the source names it.  A coordinate written
+// as `x`, `x + c` or `x - c` (x the index parameter of that axis, c a
+// literal) widens the halo to c; any other coordinate expression widens it to
+// at least 1.  Halos are capped at 4: the window test in the accessors sends
+// any read outside the staged window to global memory, so the choice affects
+// speed only, never results.
+void choose_stages(JitKernel *k) {
+  k->stages.clear();
+  k->stage_smem = 0;
+  if (k->nd != 3) return;
+  const std::string &src = k->source;
+  std::vector<std::string> emitted;
+  {
+    const std::regex emit_re("\\bPSGridEmit\\s*\\(\\s*(\\w+)");
+    for (auto it = std::sregex_iterator(src.begin(), src.end(), emit_re);
+         it != std::sregex_iterator(); ++it)
+      emitted.push_back((*it)[1].str());
+  }
+  const std::regex get_re("\\bPSGridGet(Periodic)?\\s*\\(");
+  for (size_t pi = 0; pi < k->params.size(); ++pi) {
+    const JitParam &p = k->params[pi];
+    if (!p.grid || p.rank != 3) continue;
+    bool is_emitted = false;
+    for (const std::string &e : emitted) is_emitted |= (e == p.name);
+    if (is_emitted) continue;
+    int r[3] = {0, 0, 0};
+    bool off_centre = false, periodic = false;
+    for (auto it = std::sregex_iterator(src.begin(), src.end(), get_re);
+         it != std::sregex_iterator(); ++it) {
+      const size_t open = it->position(0) + it->length(0) - 1;
+      std::vector<std::string> args;
+      size_t close = 0;
+      if (!call_args(src, open, &args, &close) || args.size() != 4 || trim(args[0]) != p.name)
+        continue;
+      if ((*it)[1].matched) periodic = true;
+      for (int d = 0; d < 3; ++d) {
+        std::smatch m;
+        const std::string a = trim(args[d + 1]);
+        static const std::regex lit_re("^(\\w+)\\s*(?:([+-])\\s*([0-9]+))?$");
+        if (std::regex_match(a, m, lit_re) && m[1].str() == k->idx[d]) {
+          const int c = m[3].matched ? std::atoi(m[3].str().c_str()) : 0;
+          if (c) off_centre = true;
+          r[d] = std::max(r[d], std::min(c, 4));
+        } else {
+          off_centre = true;
+          r[d] = std::max(r[d], 1);
+        }
+      }
+    }
+    if (!off_centre) continue;
+    JitStage st;
+    st.param = (int)pi;
+    st.rx = r[0];
+    st.ry = r[1];
+    st.rz = r[2];
+    st.periodic = periodic;
+    st.esz = (p.type == kFloat || p.type == kInt) ? 4 : 8;
+    st.bytes = (size_t)(2 * st.rz + 3) * (kTileX + 2 * st.rx) * (kTileY + 2 * st.ry) * st.esz;
+    st.bytes = (st.bytes + 15) / 16 * 16;
+    if (k->stage_smem + st.bytes > kStageBudget) continue;
+    st.off = k->stage_smem;
+    k->stage_smem += st.bytes;
+    k->stages.push_back(st);
+  }
+}
+
+std::string tiled_entry_source(const JitKernel &k) {
+  std::string s =
+      "\nextern \"C\" __global__ void __launch_bounds__(256) __ps_entry_t(int dmin0, int dmax0, "
+      "int dmin1, int dmax1, int dmin2, int dmax2, int ntx, int zlen" +
+      entry_params(k) + ") {\n"
+      "  extern __shared__ __align__(16) unsigned char __ps_sm[];\n"
+      "  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;\n"
+      "  const int x0 = dmin0 + (int)(blockIdx.x % (unsigned)ntx) * " + std::to_string(kTileX) +
+      ";\n"
+      "  const int y0 = dmin1 + (int)(blockIdx.x / (unsigned)ntx) * " + std::to_string(kTileY) +
+      ";\n"
+      "  const int zs = dmin2 + (int)blockIdx.y * zlen;\n"
+      "  const int ze = min(zs + zlen, dmax2);\n"
+      "  if (zs >= ze) return;\n";
+  for (size_t i = 0; i < k.params.size(); ++i)
+    if (k.params[i].grid)
+      s += "  auto g" + std::to_string(i) + " = __ps_dev(a" + std::to_string(i) + ");\n";
+  std::string stage_next;
+  for (size_t j = 0; j < k.stages.size(); ++j) {
+    const JitStage &st = k.stages[j];
+    const std::string i = std::to_string(st.param), sj = std::to_string(j);
+    const std::string T = scalar_ctype(k.params[st.param].type);
+    const int W = kTileX + 2 * st.rx, H = kTileY + 2 * st.ry, S = 2 * st.rz + 3;
+    const std::string tpl = "<" + T + ", " + std::to_string(W) + ", " + std::to_string(H) +
+                            ", " + std::to_string(S) + ", " + std::to_string(st.rx) + ", " +
+                            std::to_string(st.ry) + ", " + (st.periodic ? "true" : "false") +
+                            ">";
+    s += "  " + T + " *s" + sj + " = reinterpret_cast<" + T + " *>(__ps_sm + " +
+         std::to_string(st.off) + ");\n";
+    s += "  for (int d = -" + std::to_string(st.rz) + "; d <= " + std::to_string(st.rz) +
+         "; ++d) __ps_stage" + tpl + "(s" + sj + ", a" + i + ", x0, y0, zs + d);\n";
+    s += "  g" + i + ".staged = 1; g" + i + ".sx0 = x0 - " + std::to_string(st.rx) + "; g" + i +
+         ".sy0 = y0 - " + std::to_string(st.ry) + "; g" + i + ".sw = " + std::to_string(W) +
+         "; g" + i + ".sh = " + std::to_string(H) + "; g" + i + ".rz = " +
+         std::to_string(st.rz) + ";\n";
+    stage_next += "      __ps_stage" + tpl + "(s" + sj + ", a" + i + ", x0, y0, z + 1 + " +
+                  std::to_string(st.rz) + ");\n";
+  }
+  s += "  psg::cp_async_commit();\n"
+       "  for (int z = zs; z < ze; ++z) {\n"
+       "    if (z + 1 < ze) {\n" + stage_next + "    }\n"
+       "    psg::cp_async_commit();\n"
+       "    psg::cp_async_wait<1>();\n"
+       "    __syncthreads();\n";
+  for (size_t j = 0; j < k.stages.size(); ++j) {
+    const JitStage &st = k.stages[j];
+    const std::string g = "g" + std::to_string(st.param), sj = std::to_string(j);
+    const int W = kTileX + 2 * st.rx, H = kTileY + 2 * st.ry, S = 2 * st.rz + 3;
+    s += "    " + g + ".sz = z;\n";
+    s += "    for (int d = -" + std::to_string(st.rz) + "; d <= " + std::to_string(st.rz) +
+         "; ++d) " + g + ".pl[d + 4] = s" + sj + " + __ps_slot<" + std::to_string(S) +
+         ">(z + d) * " + std::to_string(W * H) + ";\n";
+  }
+  s += "#pragma unroll\n"
+       "    for (int jy = 0; jy < " + std::to_string(kTileY / 8) + "; ++jy) {\n"
+       "      const int y = y0 + warp + 8 * jy;\n"
+       "#pragma unroll\n"
+       "      for (int jx = 0; jx < " + std::to_string(kTileX / 32) + "; ++jx) {\n"
+       "        const int x = x0 + lane + 32 * jx;\n"
+       "        if (x < dmax0 && y < dmax1) {\n";
+  for (size_t i = 0; i < k.params.size(); ++i) {
+    if (!k.params[i].grid) continue;
+    const std::string g = "g" + std::to_string(i);
+    s += "          " + g + ".cur = " + cur_expr(k.params[i], g) + ";\n";
+  }
+  s += "          " + call_source(k) + "        }\n      }\n    }\n  }\n"
+       "  psg::cp_async_wait<0>();\n}\n";
   return s;
 }
 
 }  // namespace
 
-bool jit_build(const char *source, const char *name, JitKernel *k, std::vector<char> *image,
-               std::string *err) {
-  if (!load_nvrtc(err)) return false;
-  k->name = name;
-  k->source = source;
-  if (!parse_signature(k->source, k->name, k, err)) return false;
-  const std::string program =
-      std::string(kPrelude) + "#line 1 \"stencil\"\n" + k->source + "\n" + entry_source(*k);
+namespace {
+
+// Compiles one program text for sm_103a (headers: ps_arith.cuh).
+bool nvrtc_compile(const std::string &program, std::vector<char> *image, std::string *log) {
   nvrtcProgram_t prog = nullptr;
-  if (g_nvrtc.create(&prog, program.c_str(), "stencil.cu", 0, nullptr, nullptr) != 0) {
-    *err = "nvrtcCreateProgram failed";
+  const char *hdr_src[] = {kEmbedArith};
+  const char *hdr_name[] = {"ps_arith.cuh"};
+  if (g_nvrtc.create(&prog, program.c_str(), "stencil.cu", 1, hdr_src, hdr_name) != 0) {
+    *log = "nvrtcCreateProgram failed";
     return false;
   }
   const char *opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "--fmad=false",
@@ -369,10 +623,9 @@ bool jit_build(const char *source, const char *name, JitKernel *k, std::vector<c
   if (rc != 0) {
     size_t n = 0;
     g_nvrtc.log_size(prog, &n);
-    std::string log(n, '\0');
-    if (n) g_nvrtc.log(prog, &log[0]);
+    log->assign(n, '\0');
+    if (n) g_nvrtc.log(prog, &(*log)[0]);
     g_nvrtc.destroy(&prog);
-    *err = "stencil " + k->name + " does not compile: " + log.substr(0, 600);
     return false;
   }
   size_t n = 0;
@@ -383,11 +636,34 @@ bool jit_build(const char *source, const char *name, JitKernel *k, std::vector<c
   return true;
 }
 
+}  // namespace
+
+bool jit_build(const char *source, const char *name, JitKernel *k, std::vector<char> *image,
+               std::string *err) {
+  if (!load_nvrtc(err)) return false;
+  k->name = name;
+  k->source = source;
+  if (!parse_signature(k->source, k->name, k, err)) return false;
+  choose_stages(k);
+  const std::string base =
+      std::string(kPrelude) + "#line 1 \"stencil\"\n" + k->source + "\n" + entry_source(*k);
+  std::string log;
+  // Both entries in one program; should the tiled one not compile, the plain
+  // entry alone (the stencil then runs untiled).
+  if (!k->stages.empty() && nvrtc_compile(base + tiled_entry_source(*k), image, &log))
+    return true;
+  k->stages.clear();
+  k->stage_smem = 0;
+  if (nvrtc_compile(base, image, &log)) return true;
+  *err = "stencil " + k->name + " does not compile: " + log.substr(0, 600);
+  return false;
+}
+
 bool jit_compile(const char *source, const char *name, JitKernel *k, std::string *err) {
   std::vector<char> image;
   if (!jit_build(source, name, k, &image, err) || !load_driver(err)) return false;
   CUmodule mod = nullptr;
-  CUfunction fn = nullptr;
+  CUfunction fn = nullptr, fn_t = nullptr;
   if (g_drv.load(&mod, image.data()) != CUDA_SUCCESS) {
     *err = "loading the compiled stencil failed";
     return false;
@@ -397,31 +673,99 @@ bool jit_compile(const char *source, const char *name, JitKernel *k, std::string
     *err = "compiled stencil has no entry";
     return false;
   }
+  if (!k->stages.empty()) {
+    if (g_drv.get(&fn_t, mod, "__ps_entry_t") != CUDA_SUCCESS ||
+        g_drv.set_attr(fn_t, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES,
+                       (int)k->stage_smem) != CUDA_SUCCESS) {
+      fn_t = nullptr;
+      k->stages.clear();
+      k->stage_smem = 0;
+    }
+  }
+  k->tiled_occ = 0;
+  if (fn_t && (g_drv.occupancy(&k->tiled_occ, fn_t, 256, k->stage_smem) != CUDA_SUCCESS ||
+               k->tiled_occ < 1)) {
+    k->tiled_occ = 0;
+    fn_t = nullptr;
+  }
   k->module = mod;
   k->func = fn;
+  k->func_tiled = fn_t;
   return true;
 }
 
 void jit_unload(JitKernel *k) {
   if (k->module && g_drv.unload) g_drv.unload(static_cast<CUmodule>(k->module));
-  k->module = k->func = nullptr;
+  k->module = k->func = k->func_tiled = nullptr;
 }
 
+namespace {
+
+// PS_FUNCTION_TILED=0 runs every map on the plain entry (read per launch).
+bool tiled_enabled() {
+  const char *e = getenv("PS_FUNCTION_TILED");
+  return !(e && e[0] == '0');
+}
+
+}  // namespace
+
+// The tiled entry runs every-point maps of stencils with staged grids when
+// no staged grid shares its memory with another grid argument (a staged copy
+// of a grid that the same launch writes would be stale); red/black maps and
+// everything else run the plain entry.
 cudaError_t jit_launch(const JitKernel &k, const Box &dom, int color, const GridView *grids,
                        const double *scalars, int sm_count, cudaStream_t s) {
   const int nxd = dom.max[0] - dom.min[0], nyd = dom.max[1] - dom.min[1],
             nzd = dom.max[2] - dom.min[2];
   if (nxd <= 0 || nyd <= 0 || nzd <= 0) return cudaSuccess;
-  const unsigned bx = 64, by = 4;
-  const int xs = color < 0 ? nxd : (nxd + 1) / 2;
-  const unsigned gx = (unsigned)((xs + bx - 1) / bx), gy = (unsigned)((nyd + by - 1) / by);
-  long long want = 8LL * sm_count;  // blocks in flight: a few per SM
-  long long gz = (want + (long long)gx * gy - 1) / ((long long)gx * gy);
-  if (gz < 1) gz = 1;
-  if (gz > nzd) gz = nzd;
-  const int zlen = (int)((nzd + gz - 1) / gz);
-  gz = (nzd + zlen - 1) / zlen;
-  if (gy > 65535 || gz > 65535) return cudaErrorInvalidConfiguration;
+  bool tiled = k.func_tiled && color < 0 && tiled_enabled() && k.tiled_occ > 0;
+  for (const JitStage &st : k.stages) {
+    int gi = 0, sgi = -1;
+    for (size_t i = 0; i < k.params.size(); ++i)
+      if (k.params[i].grid) {
+        if ((int)i == st.param) sgi = gi;
+        ++gi;
+      }
+    for (int j = 0; j < gi && tiled; ++j)
+      if (j != sgi && grids[j].ptr == grids[sgi].ptr) tiled = false;
+  }
+  unsigned gx, gy, gz, bx, by;
+  int head[8];
+  if (tiled) {
+    const long long ntx = (nxd + kTileX - 1) / kTileX, nty = (nyd + kTileY - 1) / kTileY;
+    const long long tiles = ntx * nty;
+    const long long want = (long long)k.tiled_occ * sm_count;
+    long long chunks = (want + tiles - 1) / tiles;
+    chunks = std::max(1LL, std::min(chunks, (long long)(nzd + 7) / 8));  // z chunks >= 8 planes
+    const int zlen = (int)((nzd + chunks - 1) / chunks);
+    chunks = (nzd + zlen - 1) / zlen;
+    if (tiles > 0x7fffffffLL || chunks > 65535) return cudaErrorInvalidConfiguration;
+    gx = (unsigned)tiles;
+    gy = (unsigned)chunks;
+    gz = 1;
+    bx = 256;
+    by = 1;
+    const int h[8] = {dom.min[0], dom.max[0], dom.min[1], dom.max[1],
+                      dom.min[2], dom.max[2], (int)ntx, zlen};
+    memcpy(head, h, sizeof(h));
+  } else {
+    bx = 64;
+    by = 4;
+    const int xs = color < 0 ? nxd : (nxd + 1) / 2;
+    gx = (unsigned)((xs + bx - 1) / bx);
+    gy = (unsigned)((nyd + by - 1) / by);
+    long long want = 8LL * sm_count;  // blocks in flight: a few per SM
+    long long nz = (want + (long long)gx * gy - 1) / ((long long)gx * gy);
+    if (nz < 1) nz = 1;
+    if (nz > nzd) nz = nzd;
+    const int zlen = (int)((nzd + nz - 1) / nz);
+    nz = (nzd + zlen - 1) / zlen;
+    if (gy > 65535 || nz > 65535) return cudaErrorInvalidConfiguration;
+    gz = (unsigned)nz;
+    const int h[8] = {dom.min[0], dom.max[0], dom.min[1], dom.max[1],
+                      dom.min[2], dom.max[2], color, zlen};
+    memcpy(head, h, sizeof(h));
+  }
 
   // argument storage: 8 ints, then each parameter at its alignment
   std::vector<unsigned char> buf(64 + 64 * k.params.size());
@@ -433,8 +777,6 @@ cudaError_t jit_launch(const JitKernel &k, const Box &dom, int color, const Grid
     args.push_back(buf.data() + off);
     off += n;
   };
-  const int head[8] = {dom.min[0], dom.max[0], dom.min[1], dom.max[1],
-                       dom.min[2], dom.max[2], color, zlen};
   for (int v : head) put(&v, 4, 4);
   int gi = 0, si = 0;
   for (const JitParam &p : k.params) {
@@ -460,8 +802,9 @@ cudaError_t jit_launch(const JitKernel &k, const Box &dom, int color, const Grid
       }
     }
   }
-  const CUresult r = g_drv.launch(static_cast<CUfunction>(k.func), gx, gy, (unsigned)gz, bx,
-                                  by, 1, 0, static_cast<CUstream>(s), args.data(), nullptr);
+  const CUresult r = g_drv.launch(static_cast<CUfunction>(tiled ? k.func_tiled : k.func), gx,
+                                  gy, gz, bx, by, 1, tiled ? (unsigned)k.stage_smem : 0,
+                                  static_cast<CUstream>(s), args.data(), nullptr);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorLaunchFailure;
 }
 

@@ -30,6 +30,7 @@ int *g_err = nullptr;  // the runtime's device error word (bounded waits)
 
 constexpr int kC = 16;       // channels
 constexpr int kTaps = 27;
+constexpr int kPoolChannels = 9;  // network input channels in use
 constexpr int kConvWarps = 8;
 
 __device__ __forceinline__ void mma_16816(float (&d)[4], const uint32_t (&a)[4],
@@ -442,8 +443,16 @@ __global__ void mse_kernel(const float *__restrict__ pred, const float *__restri
 // Fine stacked grids -> coarse network input.  Instance b sits at fine
 // origin ((b % nsx) * inx, 0, (b / nsx) * inz) of float grids with row pitch
 // `pitch` bytes and ny rows per plane; coarse cell (zc, yc, xc) averages the
-// fine cells [zc f, zc f + f) x ... inside the instance.  Channels: mean ln a0,
-// mean ln a1, mean ln a2, mean wrk1 * wscale, mean bnd, zeros.
+// fine cells [zc f, zc f + f) x ... inside the instance.
+//
+// `flip` selects one of the 16 mirror images of an instance that are
+// instances of the same problem family: bit 0/1/2 mirror x/y/z, bit 3 swaps
+// x and y (with a2 and a1, the x and y coefficients; needs inx == iny).  The 19-point operator with
+// c_i = a_i and b = 0 weighs both neighbours of a cell along an axis with
+// that cell's own a_i, and the Dirichlet faces are symmetric, so the mirrored
+// fields' solution is the mirrored solution: one solve gives 16 training
+// pairs.  Coordinates below are those of the mirror image; vmap takes them
+// back to the stored instance.
 struct PoolArgs {
   const float *a0, *a1, *a2, *wrk1, *bnd, *p;
   long long pitch_e;  // row pitch in floats
@@ -453,6 +462,7 @@ struct PoolArgs {
   int f;              // pooling factor
   int zc, yc, xc;     // coarse size
   int batch;
+  int flip;
   float wscale, pscale;
 };
 
@@ -461,6 +471,24 @@ __device__ __forceinline__ long long fine_index(const PoolArgs &a, int b, int z,
   return ((long long)(oz + z) * a.ny + y) * a.pitch_e + ox + x;
 }
 
+// Index of mirror-image cell (z, y, x) of instance b in the stored grids.
+__device__ __forceinline__ long long vmap(const PoolArgs &a, int b, int z, int y, int x) {
+  if (a.flip & 1) x = a.inx - 1 - x;
+  if (a.flip & 2) y = a.iny - 1 - y;
+  if (a.flip & 4) z = a.inz - 1 - z;
+  if (a.flip & 8) {
+    const int t = x;
+    x = y;
+    y = t;
+  }
+  return fine_index(a, b, z, y, x);
+}
+
+// Channels (means over the block): 0-2 ln a0, ln a1, ln a2; 3 wrk1 * wscale;
+// 4 bnd; 5 wrk1 * 3 / (a0 + a1 + a2) * wscale (the source over the local
+// coefficient, whose block mean the means of wrk1 and a do not give);
+// 6-8 -ln mean(1 / a_i) (log harmonic means: a block's series
+// conductance); 9-15 zeros.  a1/a2 are those of the mirror image.
 __global__ void pool_inputs_kernel(PoolArgs a, __nv_bfloat16 *__restrict__ out) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long n = (long long)a.batch * a.zc * a.yc * a.xc;
@@ -468,17 +496,25 @@ __global__ void pool_inputs_kernel(PoolArgs a, __nv_bfloat16 *__restrict__ out) 
   const int xc = (int)(i % a.xc), yc = (int)((i / a.xc) % a.yc);
   const int zc = (int)((i / ((long long)a.xc * a.yc)) % a.zc);
   const int b = (int)(i / ((long long)a.xc * a.yc * a.zc));
-  float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  // a0 weighs the z neighbours, a1 the y and a2 the x neighbours
+  const float *ay = (a.flip & 8) ? a.a2 : a.a1;
+  const float *ax = (a.flip & 8) ? a.a1 : a.a2;
+  float s[kPoolChannels] = {};
   int cnt = 0;
   for (int z = zc * a.f; z < min(zc * a.f + a.f, a.inz); ++z)
     for (int y = yc * a.f; y < min(yc * a.f + a.f, a.iny); ++y)
       for (int x = xc * a.f; x < min(xc * a.f + a.f, a.inx); ++x) {
-        const long long k = fine_index(a, b, z, y, x);
-        s[0] += logf(a.a0[k]);
-        s[1] += logf(a.a1[k]);
-        s[2] += logf(a.a2[k]);
-        s[3] += a.wrk1[k];
+        const long long k = vmap(a, b, z, y, x);
+        const float c0 = a.a0[k], c1 = ay[k], c2 = ax[k], w = a.wrk1[k];
+        s[0] += logf(c0);
+        s[1] += logf(c1);
+        s[2] += logf(c2);
+        s[3] += w;
         s[4] += a.bnd[k];
+        s[5] += w * 3.f / (c0 + c1 + c2);
+        s[6] += 1.f / c0;
+        s[7] += 1.f / c1;
+        s[8] += 1.f / c2;
         ++cnt;
       }
   const float inv = 1.f / (float)cnt;
@@ -488,11 +524,14 @@ __global__ void pool_inputs_kernel(PoolArgs a, __nv_bfloat16 *__restrict__ out) 
   row[2] = __float2bfloat16_rn(s[2] * inv);
   row[3] = __float2bfloat16_rn(s[3] * inv * a.wscale);
   row[4] = __float2bfloat16_rn(s[4] * inv);
-  for (int c = 5; c < kC; ++c) row[c] = __float2bfloat16_rn(0.f);
+  row[5] = __float2bfloat16_rn(s[5] * inv * a.wscale);
+  for (int c = 6; c < 9; ++c) row[c] = __float2bfloat16_rn(-logf(s[c] * inv));
+  for (int c = kPoolChannels; c < kC; ++c) row[c] = __float2bfloat16_rn(0.f);
 }
 
 // Training target: p at each block's centre (c + 0.5) f - 0.5, the mean of
-// the fine cells nearest to it (two per axis for even f), times pscale.
+// the fine cells nearest to it (two per axis for even f), times pscale; in
+// the mirror image's coordinates.
 __global__ void pool_target_kernel(PoolArgs a, float *__restrict__ out) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long n = (long long)a.batch * a.zc * a.yc * a.xc;
@@ -513,7 +552,7 @@ __global__ void pool_target_kernel(PoolArgs a, float *__restrict__ out) {
   float s = 0.f;
   for (int k = 0; k < 2; ++k)
     for (int j = 0; j < 2; ++j)
-      for (int m = 0; m < 2; ++m) s += a.p[fine_index(a, b, zs[k], ys[j], xs[m])];
+      for (int m = 0; m < 2; ++m) s += a.p[vmap(a, b, zs[k], ys[j], xs[m])];
   out[i] = s * 0.125f * a.pscale;
 }
 
@@ -640,7 +679,7 @@ int nn_mse(const float *pred, const float *tgt, long long n, void *dy, double *p
 }
 
 static PoolArgs pool_args(const NNFields &f) {
-  PoolArgs a;
+  PoolArgs a{};
   a.a0 = f.a0;
   a.a1 = f.a1;
   a.a2 = f.a2;
@@ -658,6 +697,7 @@ static PoolArgs pool_args(const NNFields &f) {
   a.yc = (f.iny + f.factor - 1) / f.factor;
   a.xc = (f.inx + f.factor - 1) / f.factor;
   a.batch = f.batch;
+  a.flip = f.flip;
   a.wscale = f.wscale;
   a.pscale = f.pscale;
   return a;
@@ -683,7 +723,7 @@ int nn_pool_target(const NNFields &f, float *out, cudaStream_t s) {
 int nn_upsample(const NNFields &f, const float *coarse, float *p, cudaStream_t s) {
   const PoolArgs a = pool_args(f);
   const long long n = (long long)a.batch * a.inz * a.iny * a.inx;
-  if (n <= 0) return -1;
+  if (n <= 0 || a.flip) return -1;
   upsample_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, coarse, p);
   return (int)cudaGetLastError();
 }

@@ -148,13 +148,28 @@ struct JitParam {
   int type;               // ElemType
   int rank;               // grids: 1..3
   std::string decl_type;  // the type as declared ("PSGrid3DFloat", "float")
+  std::string name;       // the parameter's name
+};
+// A grid the tiled entry stages in shared memory: planes of (64 + 2 rx) x
+// (16 + 2 ry) cells around the CTA's tile, a ring of 2 rz + 3 of them.
+struct JitStage {
+  int param;            // index into params
+  int rx, ry, rz;       // halo widths
+  bool periodic;        // halo cells wrap (else clamp to the grid)
+  int esz;              // element size
+  size_t off, bytes;    // byte range in dynamic shared memory
 };
 struct JitKernel {
   std::string name, source;
   int nd = 0;                     // index parameters (x[, y[, z]])
+  std::string idx[3];             // their names
   std::vector<JitParam> params;   // after the indices, in order
   int ngrids = 0, nscalars = 0;
+  std::vector<JitStage> stages;   // grids the tiled entry stages (3D only)
+  size_t stage_smem = 0;
   void *module = nullptr, *func = nullptr;
+  void *func_tiled = nullptr;     // __ps_entry_t, when stages is not empty
+  int tiled_occ = 0;              // its resident CTAs per SM
 };
 // Parses `void name(...)` in source and compiles source + entry for sm_103a
 // into *image (no device needed).  false with *err on failure.
@@ -199,6 +214,7 @@ struct NNFields {
   int ny;
   int inx, iny, inz, nsx, factor, batch;
   float wscale, pscale;
+  int flip;  // mirror image: bits 0-2 mirror x/y/z, bit 3 swaps x and y
 };
 // Each returns 0, -1 for invalid arguments, or the launch's cudaError_t.
 // Device error word for the kernels' bounded waits (set at PSInit).

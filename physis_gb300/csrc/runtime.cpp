@@ -1810,7 +1810,15 @@ int PSStencilFunctionCheck(const char *source, const char *name, char *log, size
   psg::JitKernel k;
   std::vector<char> image;
   std::string why;
-  if (psg::jit_build(source, name, &k, &image, &why)) return PS_OK;
+  if (psg::jit_build(source, name, &k, &image, &why)) {
+    std::string rep;
+    for (const psg::JitStage &st : k.stages)
+      rep += "staged " + k.params[st.param].name + " " + std::to_string(st.rx) + " " +
+             std::to_string(st.ry) + " " + std::to_string(st.rz) +
+             (st.periodic ? " periodic;" : " clamp;");
+    if (log && logsize) snprintf(log, logsize, "%s", rep.c_str());
+    return PS_OK;
+  }
   if (log && logsize) snprintf(log, logsize, "%s", why.c_str());
   const bool missing = why.find("not available") != std::string::npos ||
                        why.find("lacks") != std::string::npos;
@@ -2150,7 +2158,7 @@ static int ws_status(int rc, const char *what) {
 }
 
 static psg::NNFields ws_fields(const PSWarmStartFields *f) {
-  psg::NNFields n;
+  psg::NNFields n{};
   n.a0 = f->a0;
   n.a1 = f->a1;
   n.a2 = f->a2;
@@ -2167,13 +2175,15 @@ static psg::NNFields ws_fields(const PSWarmStartFields *f) {
   n.batch = f->batch;
   n.wscale = f->wscale;
   n.pscale = f->pscale;
+  n.flip = f->flip;
   return n;
 }
 
 static bool ws_fields_ok(const PSWarmStartFields *f, const char *what, bool need_p) {
   if (!f || !f->a0 || !f->a1 || !f->a2 || !f->wrk1 || !f->bnd || (need_p && !f->p) ||
       f->pitch <= 0 || f->pitch % 4 || f->inx < 1 || f->iny < 1 || f->inz < 1 || f->nsx < 1 ||
-      f->factor < 1 || f->batch < 1 || f->ny < f->iny || f->pitch / 4 < (long long)f->inx) {
+      f->factor < 1 || f->batch < 1 || f->ny < f->iny || f->pitch / 4 < (long long)f->inx ||
+      f->flip < 0 || f->flip > 15 || ((f->flip & 8) && f->inx != f->iny)) {
     fail(PS_ERR_INVALID_ARGUMENT, "%s: bad field description", what);
     return false;
   }

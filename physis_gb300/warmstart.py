@@ -22,7 +22,9 @@ Pieces, all on the GPU through libphysis_gb300's C ABI:
   (PSWarmStartWeightGrad, PSWarmStartLoss, PSWarmStartAdam); the coarse
   prediction is upsampled to the fine grid by Catmull-Rom cubic
   interpolation (PSWarmStartUpsample); targets are sampled at the block
-  centres, so the upsampled target reproduces the solution to O(h^3).
+  centres, so the upsampled target reproduces the solution to O(h^3);
+* training pairs: each solved instance and its mirror images (axis mirrors
+  and the x/y swap), which solve the mirrored problem exactly.
 
 Relative residual: ||ss|| / ||ss(p = 0)|| with ss = (s0 a3 - p) bnd, the
 Himeno residual (examples/himeno/himenobmtxpa_original.c:331-334).
@@ -40,6 +42,7 @@ import physis_gb300 as ps
 OMEGA = 0.8
 C = 16
 LAYERS = 6
+CIN = 9  # input channels the pooling kernel fills (the rest are zeros)
 
 
 # ---- instances ----------------------------------------------------------------
@@ -192,8 +195,9 @@ class Stack:
             done[(done < 0) & (r <= tol)] = n
         return done
 
-    def fields(self, factor, wscale=1.0, pscale=1.0, with_p=False):
-        """PSWarmStartFields describing this stack for the pooling kernels."""
+    def fields(self, factor, wscale=1.0, pscale=1.0, with_p=False, flip=0):
+        """PSWarmStartFields describing this stack for the pooling kernels
+        (of mirror image `flip` of every instance)."""
         f = ps.PSWarmStartFields()
         g = self.grids
         f.a0, f.a1, f.a2 = g[2].dev_ptr, g[3].dev_ptr, g[4].dev_ptr
@@ -206,6 +210,7 @@ class Stack:
         f.factor = factor
         f.batch = self.count
         f.wscale, f.pscale = wscale, pscale
+        f.flip = flip
         return f
 
     def free(self):
@@ -230,11 +235,11 @@ class Net:
         rng = np.random.default_rng(seed)
         self.w, self.b = [], []
         for l in range(LAYERS):
-            fan_in = 27 * (5 if l == 0 else C)
+            fan_in = 27 * (CIN if l == 0 else C)
             std = math.sqrt(2.0 / fan_in) if l < LAYERS - 1 else 0.1 * math.sqrt(1.0 / fan_in)
             w = rng.normal(0, std, size=(27, C, C)).astype(np.float32)
             if l == 0:
-                w[:, 5:, :] = 0.0
+                w[:, CIN:, :] = 0.0
             self.w.append(torch.tensor(w, device=dev))
             self.b.append(torch.zeros(C, device=dev))
         self.params = self.w + self.b
@@ -342,17 +347,35 @@ def make_instances(rng, count, shape, workers=0):
         return pool.map(_instance_job, [(sd, shape) for sd in seeds])
 
 
+def mirror_images(shape, count):
+    """The first `count` of the 16 mirror images (flip codes) an instance of
+    this shape has: the 8 axis mirrors, then with x and y swapped when
+    nx == ny."""
+    nz, ny, nx = shape
+    codes = list(range(16)) if nx == ny else list(range(8))
+    return codes[:max(1, min(count, len(codes)))]
+
+
 class Dataset:
-    """Pooled inputs and targets of many instances, resident on the GPU."""
+    """Pooled inputs and targets of many instances, resident on the GPU.
+
+    Each solved instance gives `mirrors` training pairs (its mirror images,
+    which solve the mirrored problem).  Samples are stored mirror-major:
+    sample m * count + i is mirror image m of instance i, so contiguous
+    minibatches hold different instances."""
 
     def __init__(self, rng, count, shape, factor, nsx=15, per_stack=300, tol=1e-7,
-                 chunk=256, max_sweeps=40000, wscale=None, pscale=None, log=None, workers=0):
+                 chunk=256, max_sweeps=40000, wscale=None, pscale=None, log=None, workers=0,
+                 mirrors=1):
         import torch
         self.shape, self.factor = shape, factor
         zc, yc, xc = coarse_shape(shape, factor)
         self.dims1 = (zc, yc, xc)
-        self.x = torch.empty((count, zc, yc, xc, C), dtype=torch.bfloat16, device="cuda")
-        self.t = torch.empty((count, zc, yc, xc), dtype=torch.float32, device="cuda")
+        self.flips = mirror_images(shape, mirrors)
+        nm = len(self.flips)
+        self.count = count
+        self.x = torch.empty((nm * count, zc, yc, xc, C), dtype=torch.bfloat16, device="cuda")
+        self.t = torch.empty((nm * count, zc, yc, xc), dtype=torch.float32, device="cuda")
         self.sweeps = np.zeros(count, int)
         self.wscale, self.pscale = wscale, pscale
         self.solve_seconds = 0.0
@@ -375,9 +398,11 @@ class Dataset:
                                             _p(tmp), None))
                 ps.synchronize()
                 self.pscale = 1.0 / float(np.std(tmp.cpu().numpy().astype(np.float64)))
-            f = st.fields(factor, self.wscale, self.pscale, True)
-            _ok(L.PSWarmStartPool(ctypes.byref(f), _p(self.x[done:done + k]), None))
-            _ok(L.PSWarmStartPoolTarget(ctypes.byref(f), _p(self.t[done:done + k]), None))
+            for m, flip in enumerate(self.flips):
+                f = st.fields(factor, self.wscale, self.pscale, True, flip)
+                lo = m * count + done
+                _ok(L.PSWarmStartPool(ctypes.byref(f), _p(self.x[lo:lo + k]), None))
+                _ok(L.PSWarmStartPoolTarget(ctypes.byref(f), _p(self.t[lo:lo + k]), None))
             ps.synchronize()
             st.free()
             done += k

@@ -28,6 +28,43 @@ def test_stencil_functions_compile(built, src, name):
     assert code == ps.PS_OK, log
 
 
+# The grids the tiled entry stages: read off the centre and never emitted;
+# literal offsets set the halo, other coordinate expressions widen it to 1.
+STAGES = {"branchy": "staged in 1 0 0 clamp;", "clamped": "",
+          "mix7": "staged src 1 1 1 clamp;", "line3": "staged a 1 0 0 clamp;",
+          "axes": "staged a 1 1 1 clamp;", "planes": "staged a 1 1 1 clamp;",
+          "wrap27": "staged a 1 1 1 periodic;", "rb7": "", "three": "", "nine": "",
+          "weighted": "staged a 1 1 2 clamp;"}
+
+
+@pytest.mark.parametrize("src,name", GOOD, ids=[g[1] for g in GOOD])
+def test_staged_grids(built, src, name):
+    code, log = ps.stencil_function_check(src, name)
+    if code == ps.PS_ERR_UNSUPPORTED:
+        pytest.skip("NVRTC not available: " + log)
+    assert code == ps.PS_OK
+    assert log == STAGES[name]
+
+
+def test_staging_caps_and_budget(built):
+    # halos are capped at 4 (reads beyond come from global memory); grids
+    # are staged in parameter order while the 96 KB budget lasts
+    src = r"""
+void far(const int x, const int y, const int z, PSGrid3DDouble a, PSGrid3DDouble b,
+         PSGrid3DDouble c, PSGrid3DDouble out) {
+  PSGridEmit(out, PSGridGet(a, x + 6, y, z - 4) + PSGridGet(b, x, y + 2, z + 3)
+                  + PSGridGet(c, x - 1, y, z));
+}
+"""
+    code, log = ps.stencil_function_check(src, "far")
+    if code == ps.PS_ERR_UNSUPPORTED:
+        pytest.skip("NVRTC not available: " + log)
+    assert code == ps.PS_OK, log
+    # a (11 planes x 72 x 16 x 8 B = 101 KB) is over the budget alone; b
+    # (9 x 64 x 20 x 8 B = 92 KB) fits, after which c (25 KB) does not
+    assert log == "staged b 0 2 3 clamp;"
+
+
 @pytest.mark.parametrize("src,name,why", [
     ("void f(const int x, PSGrid1DFloat a, PSGrid1DFloat b) { PSGridEmit(b, nope); }", "f",
      "does not compile"),

@@ -28,6 +28,15 @@ def rt():
     ps.clear_error()
 
 
+@pytest.fixture(autouse=True, params=["tiled", "plain"])
+def entry(request, monkeypatch):
+    # Every test runs on both generated entries: the tiled one (grids read
+    # at neighbour offsets staged in shared memory) and the plain one
+    # (PS_FUNCTION_TILED=0).  Both must give the same bits.
+    monkeypatch.setenv("PS_FUNCTION_TILED", "1" if request.param == "tiled" else "0")
+    return request.param
+
+
 def _bits(a):
     return a.view({4: np.uint32, 8: np.uint64}[a.dtype.itemsize])
 
@@ -295,6 +304,85 @@ def test_scalars_of_every_type_against_oracle(rt, oracle):
     assert np.array_equal(_bits(b.copyout()), _bits(ref))
     a.free()
     b.free()
+
+
+def _weighted_source(name, offsets, periodic, dtype="Float", ctype="float"):
+    get = "PSGridGetPeriodic" if periodic else "PSGridGet"
+    params = ", ".join("%s w%d" % (ctype, i) for i in range(len(offsets)))
+    terms = []
+    for i, (dx, dy, dz) in enumerate(offsets):
+        co = ["x", "y", "z"]
+        for j, d in enumerate((dx, dy, dz)):
+            if d:
+                co[j] += (" + %d" % d) if d > 0 else (" - %d" % -d)
+        terms.append("w%d * %s(a, %s)" % (i, get, ", ".join(co)))
+    return ("void %s(const int x, const int y, const int z, PSGrid3D%s a, PSGrid3D%s b, %s) {\n"
+            "  PSGridEmit(b, %s);\n}\n" % (name, dtype, dtype, params, " + ".join(terms)))
+
+
+FAR = [(0, 0, 0), (6, 0, 0), (-4, 0, 0), (0, 2, 0), (0, -3, 0), (0, 0, 4), (0, 0, -1),
+       (1, 1, 1), (-1, 2, -1), (3, -1, 0)]
+
+
+@pytest.mark.parametrize("periodic", [False, True], ids=["clamp-free", "periodic"])
+def test_staged_reads_with_wide_and_capped_halos(rt, oracle, periodic):
+    # Offsets up to 6 in x (past the halo cap of 4: those reads come from
+    # global memory), partial 64 x 16 tiles, an odd domain origin, z chunks;
+    # periodic reads wrap at every face.  Oracle: the same left-to-right
+    # weighted sum as a point stencil.
+    rng = np.random.default_rng(21)
+    shape = (37, 45, 150)
+    nz, ny, nx = shape
+    src = rng.uniform(-1, 1, size=shape).astype(np.float32)
+    w = [float(v) for v in rng.uniform(-1, 1, size=len(FAR)).astype(np.float32)]
+    if periodic:
+        dom = (0, nx, 0, ny, 0, nz)
+    else:
+        dom = (5, nx - 6, 3, ny - 2, 1, nz - 4)
+    ref = np.zeros(shape, np.float32)
+    oracle.points(src, ref, dom, FAR, weights=w, boundary=1 if periodic else 0)
+    code, log = ps.stencil_function_check(_weighted_source("far", FAR, periodic), "far")
+    assert code == ps.PS_OK
+    assert log == "staged a 4 3 4 %s;" % ("periodic" if periodic else "clamp")
+    k = ps.stencil_function(_weighted_source("far", FAR, periodic), "far")
+    a, b = _grid(src), _grid(np.zeros(shape, np.float32))
+    ps.stencil_run([ps.stencil_map(k, ps.domain(*dom), [a, b], w)])
+    assert np.array_equal(_bits(b.copyout()), _bits(ref))
+    a.free()
+    b.free()
+
+
+def test_staged_double_grid_beside_an_unstaged_one(rt, oracle):
+    # two input grids: the one read at offsets is staged (double), the one
+    # read at the centre only is not; the emitted grid never is
+    rng = np.random.default_rng(22)
+    shape = (20, 33, 70)
+    nz, ny, nx = shape
+    src = rng.uniform(-1, 1, size=shape)
+    scale = rng.uniform(0.5, 2.0, size=shape)
+    pts = [(0, 0, 0), (1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)]
+    dom = (1, nx - 1, 1, ny - 1, 1, nz - 1)
+    sums = np.zeros(shape)
+    oracle.points(src, sums, dom, pts, weights=[1.0] * 7)
+    ref = src.copy() * 0
+    sl = (slice(1, nz - 1), slice(1, ny - 1), slice(1, nx - 1))
+    ref[sl] = sums[sl] * scale[sl]
+    code = r"""
+void s7(const int x, const int y, const int z, PSGrid3DDouble a, PSGrid3DDouble s,
+        PSGrid3DDouble out) {
+  double v = PSGridGet(a, x, y, z) + PSGridGet(a, x + 1, y, z) + PSGridGet(a, x - 1, y, z)
+      + PSGridGet(a, x, y + 1, z) + PSGridGet(a, x, y - 1, z) + PSGridGet(a, x, y, z + 1)
+      + PSGridGet(a, x, y, z - 1);
+  PSGridEmit(out, v * PSGridGet(s, x, y, z));
+}
+"""
+    assert ps.stencil_function_check(code, "s7") == (ps.PS_OK, "staged a 1 1 1 clamp;")
+    k = ps.stencil_function(code, "s7")
+    a, sg, out = _grid(src), _grid(scale), _grid(np.zeros(shape))
+    ps.stencil_run([ps.stencil_map(k, ps.domain(*dom), [a, sg, out])])
+    assert np.array_equal(_bits(out.copyout()), _bits(ref))
+    for g in (a, sg, out):
+        g.free()
 
 
 def test_function_ids_are_cached_and_errors_reported(rt):

@@ -187,37 +187,35 @@ def test_loss_and_adam(rt):
     assert np.allclose(tw.cpu().numpy(), ref, rtol=1e-5, atol=1e-6)
 
 
-def test_pool_and_upsample(rt):
+@pytest.mark.parametrize("shape,flips", [((9, 6, 5), (0, 1, 6)), ((9, 6, 6), (8, 13, 15))])
+def test_pool_and_upsample(rt, shape, flips):
     from physis_gb300 import warmstart as ws
     rng = np.random.default_rng(5)
-    shape = (9, 6, 5)
     insts = [ws.make_instance(rng, shape) for _ in range(3)]
     st = ws.Stack(insts, shape, nsx=2)
     p = np.zeros(st.gshape, np.float32)
     for b in range(3):
         p[st.slot(b)] = rng.normal(size=shape)
     st.grids[0].copyin(p)
-    f = st.fields(4, wscale=0.5, pscale=2.0, with_p=True)
     zc, yc, xc = ws.coarse_shape(shape, 4)
-    x = torch.empty(3 * zc * yc * xc * 16, dtype=torch.bfloat16, device="cuda")
-    t = torch.empty(3 * zc * yc * xc, dtype=torch.float32, device="cuda")
     L = ps.lib()
-    assert L.PSWarmStartPool(ctypes.byref(f), _p(x), None) == 0
-    assert L.PSWarmStartPoolTarget(ctypes.byref(f), _p(t), None) == 0
-    ps.synchronize()
-    xin = _np_bf(x, (3, zc, yc, xc, 16))
-    tt = t.cpu().numpy().reshape(3, zc, yc, xc)
-    for b, inst in enumerate(insts):
-        feats = [nn.pool(np.log(inst["a0"].astype(np.float64)), 4),
-                 nn.pool(np.log(inst["a1"].astype(np.float64)), 4),
-                 nn.pool(np.log(inst["a2"].astype(np.float64)), 4),
-                 nn.pool(inst["wrk1"].astype(np.float64), 4) * 0.5,
-                 nn.pool(inst["bnd"].astype(np.float64), 4)]
-        for c, ref in enumerate(feats):
-            assert _within_one_bf16_step(xin[b, ..., c], ref), c
-        assert np.all(xin[b, ..., 5:] == 0)
-        assert np.allclose(tt[b], nn.centre_sample(p[st.slot(b)].astype(np.float64), 4) * 2.0,
-                           rtol=1e-5, atol=1e-6)
+    for flip in flips:
+        f = st.fields(4, wscale=0.5, pscale=2.0, with_p=True, flip=flip)
+        x = torch.empty(3 * zc * yc * xc * 16, dtype=torch.bfloat16, device="cuda")
+        t = torch.empty(3 * zc * yc * xc, dtype=torch.float32, device="cuda")
+        assert L.PSWarmStartPool(ctypes.byref(f), _p(x), None) == 0
+        assert L.PSWarmStartPoolTarget(ctypes.byref(f), _p(t), None) == 0
+        ps.synchronize()
+        xin = _np_bf(x, (3, zc, yc, xc, 16))
+        tt = t.cpu().numpy().reshape(3, zc, yc, xc)
+        for b, inst in enumerate(insts):
+            feats = nn.pool_features(nn.mirror_instance(inst, flip), 4, 0.5)
+            for c in range(nn.POOL_CHANNELS):
+                assert _within_one_bf16_step(xin[b, ..., c], feats[..., c]), (flip, c)
+            assert np.all(xin[b, ..., nn.POOL_CHANNELS:] == 0)
+            pm = nn.mirror(p[st.slot(b)].astype(np.float64), flip)
+            assert np.allclose(tt[b], nn.centre_sample(pm, 4) * 2.0, rtol=1e-5, atol=1e-6), flip
+    f = st.fields(4, wscale=0.5, pscale=2.0, with_p=True)
     coarse = rng.normal(size=(3, zc, yc, xc)).astype(np.float32)
     ct = torch.tensor(coarse.ravel(), device="cuda")
     assert L.PSWarmStartUpsample(ctypes.byref(f), _p(ct), ctypes.c_void_p(st.grids[1].dev_ptr),
@@ -227,6 +225,27 @@ def test_pool_and_upsample(rt):
     for b, inst in enumerate(insts):
         ref = nn.upsample(coarse[b].astype(np.float64), shape, 4) / 2.0 * inst["bnd"]
         assert np.allclose(up[st.slot(b)], ref, rtol=1e-5, atol=1e-6)
+    st.free()
+
+
+def test_mirror_argument_checks(rt):
+    # the x/y swap needs a square x-y section; upsampling writes the stored
+    # instance, so it takes no mirror
+    from physis_gb300 import warmstart as ws
+    rng = np.random.default_rng(7)
+    shape = (9, 6, 5)
+    st = ws.Stack([ws.make_instance(rng, shape)], shape, nsx=1)
+    zc, yc, xc = ws.coarse_shape(shape, 4)
+    x = torch.empty(zc * yc * xc * 16, dtype=torch.bfloat16, device="cuda")
+    L = ps.lib()
+    assert L.PSWarmStartPool(ctypes.byref(st.fields(4, flip=8)), _p(x), None) != 0
+    assert L.PSWarmStartPool(ctypes.byref(st.fields(4, flip=16)), _p(x), None) != 0
+    ct = torch.zeros(zc * yc * xc, dtype=torch.float32, device="cuda")
+    assert L.PSWarmStartUpsample(ctypes.byref(st.fields(4, flip=1)), _p(ct),
+                                 ctypes.c_void_p(st.grids[1].dev_ptr), None) != 0
+    assert ps.last_error()[0] == 2  # PS_ERR_INVALID_ARGUMENT
+    ps.clear_error()
+    ps.synchronize()
     st.free()
 
 
@@ -243,7 +262,7 @@ def test_network_gradients_match_oracle(rt, conv_form):
     net = ws.Net(seed=3)
     dims = (2, 5, 4, 6)
     x = nn.from_bf16(nn.to_bf16(rng.normal(size=dims + (16,))))
-    x[..., 5:] = 0.0
+    x[..., ws.CIN:] = 0.0
     t = rng.normal(size=dims).astype(np.float32)
     ws_ = [nn.from_bf16(nn.to_bf16(w.cpu().numpy())) for w in net.w]
     for l in range(ws.LAYERS):  # make the masters BF16-exact

@@ -87,3 +87,53 @@ def test_pool_and_upsample():
     cs = nn.centre_sample(f2, 4)
     assert cs.shape == (2, 2, 2)
     assert np.isclose(cs[0, 0, 0], f2[1:3, 1:3, 1:3].mean())
+
+
+def test_mirror_images_solve_the_mirrored_problem():
+    # The 19-point operator with c_i = a_i and b = 0 weighs both neighbours
+    # of a cell along an axis with that cell's a_i, and the Dirichlet faces
+    # are symmetric: Jacobi sweeps of a mirrored instance give the mirrored
+    # iterate (to rounding: the mirrored sum runs in another order).  This is
+    # what lets one solve stand for 16 training pairs.
+    from oracle import pyoracle as po
+    from physis_gb300 import warmstart as ws
+    rng = np.random.default_rng(11)
+    shape = (10, 7, 7)
+    inst = ws.make_instance(rng, shape)
+
+    def jacobi(fields, sweeps=30):
+        arr = [np.ascontiguousarray(a, np.float32) for a in ws.himeno_arrays(fields)]
+        p0 = np.zeros(shape, np.float32)
+        p1 = np.zeros(shape, np.float32)
+        dom = (1, shape[2] - 1, 1, shape[1] - 1, 1, shape[0] - 1)
+        for _ in range(sweeps):
+            po.himeno19([p0, p1] + arr, dom, ws.OMEGA)
+            p0, p1 = p1, p0
+        return p0
+
+    base = jacobi(inst)
+    assert np.abs(base).max() > 0
+    for flip in (1, 2, 4, 8, 15):
+        got = jacobi(nn.mirror_instance(inst, flip))
+        assert np.allclose(got, nn.mirror(base, flip), rtol=1e-5, atol=1e-6 * np.abs(base).max()), flip
+    # a1 and a2 (y and x coefficients) must trade places under the swap:
+    # without it the swap is not a symmetry
+    wrong = nn.mirror_instance(inst, 8)
+    wrong["a1"], wrong["a2"] = wrong["a2"], wrong["a1"]
+    assert not np.allclose(jacobi(wrong), nn.mirror(base, 8), rtol=1e-3)
+
+
+def test_pool_features_definition():
+    rng = np.random.default_rng(12)
+    inst = {k: np.exp(rng.uniform(-0.7, 0.7, size=(6, 5, 5))) for k in ("a0", "a1", "a2")}
+    inst["wrk1"] = rng.normal(size=(6, 5, 5))
+    inst["bnd"] = np.ones((6, 5, 5))
+    feats = nn.pool_features(inst, 2, 0.5)
+    assert feats.shape == (3, 3, 3, nn.POOL_CHANNELS)
+    blk = (slice(0, 2), slice(0, 2), slice(2, 4))
+    a = [inst[k][blk] for k in ("a0", "a1", "a2")]
+    w = inst["wrk1"][blk]
+    assert np.isclose(feats[0, 0, 1, 5], (w * 3 / (a[0] + a[1] + a[2])).mean() * 0.5)
+    assert np.isclose(feats[0, 0, 1, 7], -np.log((1 / a[1]).mean()))
+    # partial block at the far x edge (one column)
+    assert np.isclose(feats[0, 0, 2, 0], np.log(inst["a0"][0:2, 0:2, 4:5]).mean())
