@@ -837,7 +837,10 @@ def run_gpu_points(args, dist):
             "config": {"workload": label, "grid": [N, N, N],
                        "launch_shape": (list(ps.get_launch_shape(k)[:2])
                                         if args.workload.startswith("points")
-                                        else "64x4 threads, one per (x, y), z-chunked"),
+                                        else ("64x4 threads, one per (x, y), z-chunked"
+                                              if os.environ.get("PS_FUNCTION_TILED") == "0"
+                                              else "64x16 tiles of 256 threads, z-chunked, "
+                                                   "staged grids in shared memory")),
                        "l2": "inputs larger than L2" if N >= 256 else "fits L2"},
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,

@@ -146,14 +146,18 @@ typedef int PSIndex;
 template <typename T> struct __PSGridArg {
   T *p; long long row; long long plane; int nx; int ny; int nz; int rank; long long cur;
 };
-// What the stencil function sees.  A grid the tiled entry staged in shared
-// memory (staged == 1) answers reads inside its window -- x in [sx0, sx0 + sw),
-// y in [sy0, sy0 + sh), z within rz of the current plane sz -- from plane
-// pointer pl[z - sz + 4]; every other read goes to global memory.
+// What the stencil function sees.  For a grid the tiled entry staged in
+// shared memory (staged == 1) the entry also records the cell being computed
+// (cx, cy, cz) and, for each plane offset d within rz, a pointer c[d + 4] to
+// that cell's position in the staged plane z + d; a read at (cx + dx, cy +
+// dy, cz + dz) with |dx| <= rx, |dy| <= ry, |dz| <= rz is then
+// c[dz + 4][dy * sw + dx].  With the function inlined, reads written as x +
+// const make every test and index a constant; any other read is tested at
+// run time and falls back to global memory outside the window.
 template <typename T> struct __PSGridDev {
   T *p; long long row; long long plane; int nx; int ny; int nz; int rank; long long cur;
-  int staged, sx0, sy0, sz, sw, sh, rz;
-  const T *pl[9];
+  int staged, rx, ry, rz, sw, cx, cy, cz;
+  const T *c[9];
 };
 template <typename T> __device__ __forceinline__ __PSGridDev<T> __ps_dev(const __PSGridArg<T> &a) {
   __PSGridDev<T> g;
@@ -170,13 +174,13 @@ __PS_GRID_TYPES(Int, int)
 __PS_GRID_TYPES(Long, long long)
 template <typename T>
 __device__ __forceinline__ bool __ps_in_stage(const __PSGridDev<T> &g, int x, int y, int z) {
-  const int dz = z - g.sz;
-  return g.staged && dz >= -g.rz && dz <= g.rz && (unsigned)(x - g.sx0) < (unsigned)g.sw &&
-         (unsigned)(y - g.sy0) < (unsigned)g.sh;
+  const int dx = x - g.cx, dy = y - g.cy, dz = z - g.cz;
+  return g.staged && dx >= -g.rx && dx <= g.rx && dy >= -g.ry && dy <= g.ry && dz >= -g.rz &&
+         dz <= g.rz;
 }
 template <typename T>
 __device__ __forceinline__ T __ps_staged(const __PSGridDev<T> &g, int x, int y, int z) {
-  return g.pl[z - g.sz + 4][(y - g.sy0) * g.sw + (x - g.sx0)];
+  return g.c[z - g.cz + 4][(y - g.cy) * g.sw + (x - g.cx)];
 }
 template <typename T> __device__ __forceinline__ T __ps_get(const __PSGridDev<T> &g, int x) {
   return g.p[x];
@@ -225,17 +229,20 @@ template <bool PER> __device__ __forceinline__ int __ps_fit(int v, int n) {
   return min(max(v, 0), n - 1);
 }
 // Plane zp (unwrapped) of the W x H window at (x0 - RX, y0 - RY) into its
-// ring slot, one cp.async per cell; cells outside the grid wrap (PER) or
-// clamp.
+// ring slot: warp w copies rows w, w + 8, ..., lanes stride the row, one
+// cp.async per cell; cells outside the grid wrap (PER) or clamp.
 template <typename T, int W, int H, int S, int RX, int RY, bool PER>
 __device__ __forceinline__ void __ps_stage(T *ring, const __PSGridArg<T> &a, int x0, int y0,
                                            int zp) {
   T *dst = ring + __ps_slot<S>(zp) * (W * H);
   const T *src = a.p + (long long)__ps_fit<PER>(zp, a.nz) * a.plane;
-  for (int e = threadIdx.x; e < W * H; e += 256) {
-    const int r = e / W, c = e - r * W;
-    const int gy = __ps_fit<PER>(y0 - RY + r, a.ny), gx = __ps_fit<PER>(x0 - RX + c, a.nx);
-    psg::cp_async_small<(int)sizeof(T)>(dst + e, src + (long long)gy * a.row + gx);
+  const int lane = threadIdx.x & 31;
+  for (int r = threadIdx.x >> 5; r < H; r += 8) {
+    const T *srow = src + (long long)__ps_fit<PER>(y0 - RY + r, a.ny) * a.row;
+    T *drow = dst + r * W;
+#pragma unroll
+    for (int c = lane; c < W; c += 32)
+      psg::cp_async_small<(int)sizeof(T)>(drow + c, srow + __ps_fit<PER>(x0 - RX + c, a.nx));
   }
 }
 )PSJIT";
@@ -427,12 +434,18 @@ std::string entry_source(const JitKernel &k) {
 // ---- the tiled entry ---------------------------------------------------------
 // A CTA of 256 threads owns a 64 x 16 (x, y) tile and a chunk of z.  Grids
 // the stencil reads at neighbour offsets (and never emits to) are staged:
-// each z step copies one plane of the tile plus halo into a ring of 2 rz + 3
-// shared-memory planes with cp.async, one plane ahead of the compute, and the
-// function's reads inside the window come from there.  The reads themselves
+// each z step copies one plane of the tile plus halo into a ring of
+// shared-memory planes with cp.async, kAhead planes ahead of the compute, and
+// the function's reads inside the window come from there.  The reads themselves
 // are unchanged, so every result is bit-identical to the plain entry's.
 constexpr int kTileX = 64, kTileY = 16;
+constexpr int kAhead = 3;                   // planes in flight ahead of the compute
 constexpr size_t kStageBudget = 96 * 1024;  // two or more CTAs per SM
+
+// Ring planes of a grid staged with z halo rz: the 2 rz + 1 planes a step
+// reads, kAhead in flight, and one more so that a plane is never refilled
+// while a thread still one step behind reads it.
+int ring_planes(int rz) { return 2 * rz + 2 + kAhead; }
 
 // Splits the argument list of the call whose '(' is at src[open] into its
 // top-level arguments; npos-safe (returns false if unbalanced).
@@ -524,7 +537,7 @@ void choose_stages(JitKernel *k) {
     st.rz = r[2];
     st.periodic = periodic;
     st.esz = (p.type == kFloat || p.type == kInt) ? 4 : 8;
-    st.bytes = (size_t)(2 * st.rz + 3) * (kTileX + 2 * st.rx) * (kTileY + 2 * st.ry) * st.esz;
+    st.bytes = (size_t)ring_planes(st.rz) * (kTileX + 2 * st.rx) * (kTileY + 2 * st.ry) * st.esz;
     st.bytes = (st.bytes + 15) / 16 * 16;
     if (k->stage_smem + st.bytes > kStageBudget) continue;
     st.off = k->stage_smem;
@@ -550,41 +563,54 @@ std::string tiled_entry_source(const JitKernel &k) {
   for (size_t i = 0; i < k.params.size(); ++i)
     if (k.params[i].grid)
       s += "  auto g" + std::to_string(i) + " = __ps_dev(a" + std::to_string(i) + ");\n";
-  std::string stage_next;
+  // prologue: the planes step zs reads (one commit group), then the planes
+  // ahead of it one group each; step z adds plane z + rz + kAhead and waits
+  // until at most kAhead groups are pending, i.e. plane z + rz has landed.
+  std::string first, ahead, next;
   for (size_t j = 0; j < k.stages.size(); ++j) {
     const JitStage &st = k.stages[j];
     const std::string i = std::to_string(st.param), sj = std::to_string(j);
     const std::string T = scalar_ctype(k.params[st.param].type);
-    const int W = kTileX + 2 * st.rx, H = kTileY + 2 * st.ry, S = 2 * st.rz + 3;
-    const std::string tpl = "<" + T + ", " + std::to_string(W) + ", " + std::to_string(H) +
-                            ", " + std::to_string(S) + ", " + std::to_string(st.rx) + ", " +
-                            std::to_string(st.ry) + ", " + (st.periodic ? "true" : "false") +
-                            ">";
+    const int W = kTileX + 2 * st.rx, H = kTileY + 2 * st.ry, S = ring_planes(st.rz);
+    const std::string rz = std::to_string(st.rz);
+    const std::string stage = "__ps_stage<" + T + ", " + std::to_string(W) + ", " +
+                              std::to_string(H) + ", " + std::to_string(S) + ", " +
+                              std::to_string(st.rx) + ", " + std::to_string(st.ry) + ", " +
+                              (st.periodic ? "true" : "false") + ">(s" + sj + ", a" + i +
+                              ", x0, y0, ";
     s += "  " + T + " *s" + sj + " = reinterpret_cast<" + T + " *>(__ps_sm + " +
          std::to_string(st.off) + ");\n";
-    s += "  for (int d = -" + std::to_string(st.rz) + "; d <= " + std::to_string(st.rz) +
-         "; ++d) __ps_stage" + tpl + "(s" + sj + ", a" + i + ", x0, y0, zs + d);\n";
-    s += "  g" + i + ".staged = 1; g" + i + ".sx0 = x0 - " + std::to_string(st.rx) + "; g" + i +
-         ".sy0 = y0 - " + std::to_string(st.ry) + "; g" + i + ".sw = " + std::to_string(W) +
-         "; g" + i + ".sh = " + std::to_string(H) + "; g" + i + ".rz = " +
-         std::to_string(st.rz) + ";\n";
-    stage_next += "      __ps_stage" + tpl + "(s" + sj + ", a" + i + ", x0, y0, z + 1 + " +
-                  std::to_string(st.rz) + ");\n";
+    s += "  g" + i + ".staged = 1; g" + i + ".rx = " + std::to_string(st.rx) + "; g" + i +
+         ".ry = " + std::to_string(st.ry) + "; g" + i + ".rz = " + rz + "; g" + i + ".sw = " +
+         std::to_string(W) + ";\n";
+    first += "  for (int d = -" + rz + "; d <= " + rz + "; ++d) " + stage + "zs + d);\n";
+    ahead += "    if (zs + a < ze) " + stage + "zs + " + rz + " + a);\n";
+    next += "      " + stage + "z + " + rz + " + " + std::to_string(kAhead) + ");\n";
   }
-  s += "  psg::cp_async_commit();\n"
-       "  for (int z = zs; z < ze; ++z) {\n"
-       "    if (z + 1 < ze) {\n" + stage_next + "    }\n"
+  s += first + "  psg::cp_async_commit();\n";
+  s += "  for (int a = 1; a < " + std::to_string(kAhead) + "; ++a) {\n" + ahead +
+       "    psg::cp_async_commit();\n  }\n";
+  s += "  for (int z = zs; z < ze; ++z) {\n"
+       "    if (z + " + std::to_string(kAhead) + " < ze) {\n" + next + "    }\n"
        "    psg::cp_async_commit();\n"
-       "    psg::cp_async_wait<1>();\n"
+       "    psg::cp_async_wait<" + std::to_string(kAhead) + ">();\n"
        "    __syncthreads();\n";
+  // per step: each staged grid's plane pointers; per cell: the cell's
+  // coordinates and its position in those planes
+  std::string cell;
   for (size_t j = 0; j < k.stages.size(); ++j) {
     const JitStage &st = k.stages[j];
     const std::string g = "g" + std::to_string(st.param), sj = std::to_string(j);
-    const int W = kTileX + 2 * st.rx, H = kTileY + 2 * st.ry, S = 2 * st.rz + 3;
-    s += "    " + g + ".sz = z;\n";
-    s += "    for (int d = -" + std::to_string(st.rz) + "; d <= " + std::to_string(st.rz) +
-         "; ++d) " + g + ".pl[d + 4] = s" + sj + " + __ps_slot<" + std::to_string(S) +
-         ">(z + d) * " + std::to_string(W * H) + ";\n";
+    const int W = kTileX + 2 * st.rx, S = ring_planes(st.rz);
+    const std::string rz = std::to_string(st.rz);
+    s += "    const " + scalar_ctype(k.params[st.param].type) + " *pl" + sj + "[9];\n";
+    s += "    for (int d = -" + rz + "; d <= " + rz + "; ++d) pl" + sj + "[d + 4] = s" + sj +
+         " + __ps_slot<" + std::to_string(S) + ">(z + d) * " +
+         std::to_string(W * (kTileY + 2 * st.ry)) + ";\n";
+    cell += "          " + g + ".cx = x; " + g + ".cy = y; " + g + ".cz = z;\n";
+    cell += "          for (int d = -" + rz + "; d <= " + rz + "; ++d) " + g + ".c[d + 4] = pl" +
+            sj + "[d + 4] + (y - y0 + " + std::to_string(st.ry) + ") * " + std::to_string(W) +
+            " + (x - x0 + " + std::to_string(st.rx) + ");\n";
   }
   s += "#pragma unroll\n"
        "    for (int jy = 0; jy < " + std::to_string(kTileY / 8) + "; ++jy) {\n"
@@ -592,7 +618,7 @@ std::string tiled_entry_source(const JitKernel &k) {
        "#pragma unroll\n"
        "      for (int jx = 0; jx < " + std::to_string(kTileX / 32) + "; ++jx) {\n"
        "        const int x = x0 + lane + 32 * jx;\n"
-       "        if (x < dmax0 && y < dmax1) {\n";
+       "        if (x < dmax0 && y < dmax1) {\n" + cell;
   for (size_t i = 0; i < k.params.size(); ++i) {
     if (!k.params[i].grid) continue;
     const std::string g = "g" + std::to_string(i);
@@ -648,6 +674,16 @@ bool jit_build(const char *source, const char *name, JitKernel *k, std::vector<c
   const std::string base =
       std::string(kPrelude) + "#line 1 \"stencil\"\n" + k->source + "\n" + entry_source(*k);
   std::string log;
+  // PS_JIT_DUMP=<dir> writes the generated program to <dir>/<name>.cu (for
+  // building it offline with nvcc to read its resource usage).
+  if (const char *dir = getenv("PS_JIT_DUMP")) {
+    const std::string path = std::string(dir) + "/" + k->name + ".cu";
+    if (FILE *f = fopen(path.c_str(), "w")) {
+      const std::string text = base + (k->stages.empty() ? "" : tiled_entry_source(*k));
+      fwrite(text.data(), 1, text.size(), f);
+      fclose(f);
+    }
+  }
   // Both entries in one program; should the tiled one not compile, the plain
   // entry alone (the stencil then runs untiled).
   if (!k->stages.empty() && nvrtc_compile(base + tiled_entry_source(*k), image, &log))
@@ -734,11 +770,27 @@ cudaError_t jit_launch(const JitKernel &k, const Box &dom, int color, const Grid
   if (tiled) {
     const long long ntx = (nxd + kTileX - 1) / kTileX, nty = (nyd + kTileY - 1) / kTileY;
     const long long tiles = ntx * nty;
-    const long long want = (long long)k.tiled_occ * sm_count;
-    long long chunks = (want + tiles - 1) / tiles;
-    chunks = std::max(1LL, std::min(chunks, (long long)(nzd + 7) / 8));  // z chunks >= 8 planes
-    const int zlen = (int)((nzd + chunks - 1) / chunks);
-    chunks = (nzd + zlen - 1) / zlen;
+    // z chunks: the count whose waves of resident CTAs finish with the least
+    // idle time, counting each chunk's warm-up planes (2 rz + kAhead) as work
+    const long long want = std::max(1LL, (long long)k.tiled_occ * sm_count);
+    int ovh = kAhead;
+    for (const JitStage &st : k.stages) ovh = std::max(ovh, 2 * st.rz + kAhead);
+    const long long c0 = std::max(1LL, (want + tiles - 1) / tiles);
+    const long long cmax = std::max(1LL, std::min(16 * c0, (long long)(nzd + 7) / 8));
+    long long chunks = 1;
+    int zlen = nzd;
+    double best = -1.0;
+    for (long long c = std::min(c0, cmax); c <= cmax; ++c) {
+      const int zl = (int)((nzd + c - 1) / c);
+      const long long cc = (nzd + zl - 1) / zl;
+      const long long waves = (tiles * cc + want - 1) / want;
+      const double eff = (double)tiles * nzd / ((double)want * waves * (zl + ovh));
+      if (eff > best + 1e-9) {
+        best = eff;
+        chunks = cc;
+        zlen = zl;
+      }
+    }
     if (tiles > 0x7fffffffLL || chunks > 65535) return cudaErrorInvalidConfiguration;
     gx = (unsigned)tiles;
     gy = (unsigned)chunks;

@@ -60,9 +60,10 @@ void far(const int x, const int y, const int z, PSGrid3DDouble a, PSGrid3DDouble
     if code == ps.PS_ERR_UNSUPPORTED:
         pytest.skip("NVRTC not available: " + log)
     assert code == ps.PS_OK, log
-    # a (11 planes x 72 x 16 x 8 B = 101 KB) is over the budget alone; b
-    # (9 x 64 x 20 x 8 B = 92 KB) fits, after which c (25 KB) does not
-    assert log == "staged b 0 2 3 clamp;"
+    # rings of 2 rz + 5 planes: a (13 planes x 72 x 16 x 8 B = 117 KB) and b
+    # (11 x 64 x 20 x 8 B = 110 KB) are over the budget; c (5 x 66 x 16 x 8 B
+    # = 41 KB) fits
+    assert log == "staged c 1 0 0 clamp;"
 
 
 @pytest.mark.parametrize("src,name,why", [

@@ -364,7 +364,7 @@ def test_staged_double_grid_beside_an_unstaged_one(rt, oracle):
     dom = (1, nx - 1, 1, ny - 1, 1, nz - 1)
     sums = np.zeros(shape)
     oracle.points(src, sums, dom, pts, weights=[1.0] * 7)
-    ref = src.copy() * 0
+    ref = np.zeros(shape)
     sl = (slice(1, nz - 1), slice(1, ny - 1), slice(1, nx - 1))
     ref[sl] = sums[sl] * scale[sl]
     code = r"""
