@@ -229,13 +229,24 @@ template <bool PER> __device__ __forceinline__ int __ps_fit(int v, int n) {
   return min(max(v, 0), n - 1);
 }
 // Plane zp (unwrapped) of the W x H window at (x0 - RX, y0 - RY) into its
-// ring slot: warp w copies rows w, w + 8, ..., lanes stride the row, one
-// cp.async per cell; cells outside the grid wrap (PER) or clamp.
+// ring slot.  vec (the CTA's window lies inside the grid in x and every
+// window row starts on a 16-byte boundary): 16-byte cp.async chunks, rows
+// clamped or wrapped in y.  Otherwise one cp.async per cell, warp w copying
+// rows w, w + 8, ..., cells outside the grid wrapped (PER) or clamped.
 template <typename T, int W, int H, int S, int RX, int RY, bool PER>
 __device__ __forceinline__ void __ps_stage(T *ring, const __PSGridArg<T> &a, int x0, int y0,
-                                           int zp) {
+                                           bool vec, int zp) {
   T *dst = ring + __ps_slot<S>(zp) * (W * H);
   const T *src = a.p + (long long)__ps_fit<PER>(zp, a.nz) * a.plane;
+  if (vec) {
+    constexpr int V = 16 / (int)sizeof(T), NV = W / V;
+    for (int e = threadIdx.x; e < NV * H; e += 256) {
+      const int r = e / NV, c = e - r * NV;
+      const T *srow = src + (long long)__ps_fit<PER>(y0 - RY + r, a.ny) * a.row + (x0 - RX);
+      psg::cp_async16(dst + r * W + c * V, srow + c * V);
+    }
+    return;
+  }
   const int lane = threadIdx.x & 31;
   for (int r = threadIdx.x >> 5; r < H; r += 8) {
     const T *srow = src + (long long)__ps_fit<PER>(y0 - RY + r, a.ny) * a.row;
@@ -244,6 +255,13 @@ __device__ __forceinline__ void __ps_stage(T *ring, const __PSGridArg<T> &a, int
     for (int c = lane; c < W; c += 32)
       psg::cp_async_small<(int)sizeof(T)>(drow + c, srow + __ps_fit<PER>(x0 - RX + c, a.nx));
   }
+}
+// Whether a window of width W at x0 - RX can be staged in 16-byte chunks.
+template <typename T, int W, int RX>
+__device__ __forceinline__ bool __ps_vec_ok(const __PSGridArg<T> &a, int x0) {
+  const T *row0 = a.p + (x0 - RX);
+  return x0 - RX >= 0 && x0 - RX + W <= a.nx &&
+         ((unsigned long long)row0 & 15) == 0 && ((a.row * (long long)sizeof(T)) & 15) == 0;
 }
 )PSJIT";
 
@@ -537,7 +555,9 @@ void choose_stages(JitKernel *k) {
     st.rz = r[2];
     st.periodic = periodic;
     st.esz = (p.type == kFloat || p.type == kInt) ? 4 : 8;
-    st.bytes = (size_t)ring_planes(st.rz) * (kTileX + 2 * st.rx) * (kTileY + 2 * st.ry) * st.esz;
+    const int v = 16 / st.esz;  // the window's x halo: rx rounded up to 16 bytes
+    st.rxw = (st.rx + v - 1) / v * v;
+    st.bytes = (size_t)ring_planes(st.rz) * (kTileX + 2 * st.rxw) * (kTileY + 2 * st.ry) * st.esz;
     st.bytes = (st.bytes + 15) / 16 * 16;
     if (k->stage_smem + st.bytes > kStageBudget) continue;
     st.off = k->stage_smem;
@@ -571,16 +591,18 @@ std::string tiled_entry_source(const JitKernel &k) {
     const JitStage &st = k.stages[j];
     const std::string i = std::to_string(st.param), sj = std::to_string(j);
     const std::string T = scalar_ctype(k.params[st.param].type);
-    const int W = kTileX + 2 * st.rx, H = kTileY + 2 * st.ry, S = ring_planes(st.rz);
-    const std::string rz = std::to_string(st.rz);
+    const int W = kTileX + 2 * st.rxw, H = kTileY + 2 * st.ry, S = ring_planes(st.rz);
+    const std::string rz = std::to_string(st.rz), vj = "v" + sj;
     const std::string stage = "__ps_stage<" + T + ", " + std::to_string(W) + ", " +
                               std::to_string(H) + ", " + std::to_string(S) + ", " +
-                              std::to_string(st.rx) + ", " + std::to_string(st.ry) + ", " +
+                              std::to_string(st.rxw) + ", " + std::to_string(st.ry) + ", " +
                               (st.periodic ? "true" : "false") + ">(s" + sj + ", a" + i +
-                              ", x0, y0, ";
+                              ", x0, y0, " + vj + ", ";
     s += "  " + T + " *s" + sj + " = reinterpret_cast<" + T + " *>(__ps_sm + " +
          std::to_string(st.off) + ");\n";
-    s += "  g" + i + ".staged = 1; g" + i + ".rx = " + std::to_string(st.rx) + "; g" + i +
+    s += "  const bool " + vj + " = __ps_vec_ok<" + T + ", " + std::to_string(W) + ", " +
+         std::to_string(st.rxw) + ">(a" + i + ", x0);\n";
+    s += "  g" + i + ".staged = 1; g" + i + ".rx = " + std::to_string(st.rxw) + "; g" + i +
          ".ry = " + std::to_string(st.ry) + "; g" + i + ".rz = " + rz + "; g" + i + ".sw = " +
          std::to_string(W) + ";\n";
     first += "  for (int d = -" + rz + "; d <= " + rz + "; ++d) " + stage + "zs + d);\n";
@@ -601,7 +623,7 @@ std::string tiled_entry_source(const JitKernel &k) {
   for (size_t j = 0; j < k.stages.size(); ++j) {
     const JitStage &st = k.stages[j];
     const std::string g = "g" + std::to_string(st.param), sj = std::to_string(j);
-    const int W = kTileX + 2 * st.rx, S = ring_planes(st.rz);
+    const int W = kTileX + 2 * st.rxw, S = ring_planes(st.rz);
     const std::string rz = std::to_string(st.rz);
     s += "    const " + scalar_ctype(k.params[st.param].type) + " *pl" + sj + "[9];\n";
     s += "    for (int d = -" + rz + "; d <= " + rz + "; ++d) pl" + sj + "[d + 4] = s" + sj +
@@ -610,7 +632,7 @@ std::string tiled_entry_source(const JitKernel &k) {
     cell += "          " + g + ".cx = x; " + g + ".cy = y; " + g + ".cz = z;\n";
     cell += "          for (int d = -" + rz + "; d <= " + rz + "; ++d) " + g + ".c[d + 4] = pl" +
             sj + "[d + 4] + (y - y0 + " + std::to_string(st.ry) + ") * " + std::to_string(W) +
-            " + (x - x0 + " + std::to_string(st.rx) + ");\n";
+            " + (x - x0 + " + std::to_string(st.rxw) + ");\n";
   }
   s += "#pragma unroll\n"
        "    for (int jy = 0; jy < " + std::to_string(kTileY / 8) + "; ++jy) {\n"

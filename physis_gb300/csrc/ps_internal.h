@@ -150,11 +150,13 @@ struct JitParam {
   std::string decl_type;  // the type as declared ("PSGrid3DFloat", "float")
   std::string name;       // the parameter's name
 };
-// A grid the tiled entry stages in shared memory: planes of (64 + 2 rx) x
-// (16 + 2 ry) cells around the CTA's tile, a ring of 2 rz + 3 of them.
+// A grid the tiled entry stages in shared memory: planes of (64 + 2 rxw) x
+// (16 + 2 ry) cells around the CTA's tile (rxw: rx rounded up to 16 bytes),
+// a ring of 2 rz + 5 of them.
 struct JitStage {
   int param;            // index into params
-  int rx, ry, rz;       // halo widths
+  int rx, ry, rz;       // halo widths the stencil's reads need
+  int rxw;              // x halo of the staged window
   bool periodic;        // halo cells wrap (else clamp to the grid)
   int esz;              // element size
   size_t off, bytes;    // byte range in dynamic shared memory
