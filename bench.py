@@ -696,7 +696,7 @@ def run_gpu_batch(args, dist):
     achieved = algo_bytes * steps / (ms_batch / 1e3) / 1e9
     line = {
         "metric": "GLUPS, 48 uneven fp32 grids (24 x 7-point diffusion, 24 x Himeno "
-                  "19-point) in one persistent launch per step",
+                  "19-point) in one persistent launch per kernel family per step",
         "value": value, "unit": "GLUPS", "n_gpus": 1, "steps": steps, "warmup": 4,
         "ms_per_step": ms_batch / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",

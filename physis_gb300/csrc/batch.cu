@@ -12,7 +12,10 @@
 // the shared per-item body (s7_body.cuh / himeno_body.cuh) with that
 // problem's parameters and tensor maps, both read from global memory.
 // Problem kinds: the 7-point family (DIFFUSION7, SUM7, COPY; 1, 2 or 4 rows
-// per thread) and the plain Himeno sweep, float grids.
+// per thread) and the plain Himeno sweep, float grids.  The kernel is built
+// per family (FAM = kBatch7, kBatchHimeno) so that each launch carries only
+// its family's registers and shared memory; a batch holding both families
+// launches one of each per step.
 #include "batch.h"
 #include "himeno_body.cuh"
 #include "s7_body.cuh"
@@ -41,6 +44,7 @@ __device__ __forceinline__ bool s7_rows(const BatchProblem &bp, int parity,
                               prod, cons);
 }
 
+template <int FAM>
 __global__ void __launch_bounds__(256, 1)
 batch_kernel(const BatchProblem *__restrict__ probs, int nprob, const CUtensorMap *tmaps,
              int64_t total_items, int parity, int ns7, int nsp, int nsc) {
@@ -82,22 +86,22 @@ batch_kernel(const BatchProblem *__restrict__ probs, int nprob, const CUtensorMa
     const int tile = (int)(local - (int64_t)chunk * bp.tiles);
     const int zs = bp.dmin2 + chunk * bp.zlen;
     const int ze = min(zs + bp.zlen, bp.dmax2);
-    switch (bp.kind) {
-      case kKernelDiffusion7:
-        ok = s7_rows<kKernelDiffusion7>(bp, parity, tmaps, full7, ring7, tile, zs, ze, prod7,
-                                        cons7);
-        break;
-      case kKernelSum7:
-        ok = s7_rows<kKernelSum7>(bp, parity, tmaps, full7, ring7, tile, zs, ze, prod7, cons7);
-        break;
-      case kKernelCopy:
-        ok = s7_rows<kKernelCopy>(bp, parity, tmaps, full7, ring7, tile, zs, ze, prod7, cons7);
-        break;
-      default:
-        ok = himeno_item<false>(tmaps + bp.tmap[parity], tmaps + bp.cmap, bp.him[parity],
-                                pfull, cfull, pring, cring, tile, zs, ze, pprod, pcons, cprod,
-                                ccons, acc);
-        break;
+    if constexpr (FAM == kBatch7) {
+      switch (bp.kind) {
+        case kKernelDiffusion7:
+          ok = s7_rows<kKernelDiffusion7>(bp, parity, tmaps, full7, ring7, tile, zs, ze, prod7,
+                                          cons7);
+          break;
+        case kKernelSum7:
+          ok = s7_rows<kKernelSum7>(bp, parity, tmaps, full7, ring7, tile, zs, ze, prod7, cons7);
+          break;
+        default:
+          ok = s7_rows<kKernelCopy>(bp, parity, tmaps, full7, ring7, tile, zs, ze, prod7, cons7);
+          break;
+      }
+    } else {
+      ok = himeno_item<false>(tmaps + bp.tmap[parity], tmaps + bp.cmap, bp.him[parity], pfull,
+                              cfull, pring, cring, tile, zs, ze, pprod, pcons, cprod, ccons, acc);
     }
   }
   if (!ok && tid == 0) {
@@ -107,19 +111,26 @@ batch_kernel(const BatchProblem *__restrict__ probs, int nprob, const CUtensorMa
 
 }  // namespace
 
-size_t batch_smem_bytes(const BatchShape &sh) {
+size_t batch_smem_bytes(const BatchShape &sh, int fam) {
   const size_t r7 = (size_t)sh.ns7 * s7_stage_bytes((uint32_t)(34 * 4 * (sh.warps * sh.max_rows + 2) * 4));
   const size_t rh = (size_t)sh.nsp * h_align128((uint32_t)(kHimW * (sh.warps + 2) * 4)) +
                     (size_t)sh.nsc * kHimCoef * kHimTX * sh.warps * 4;
-  return 128 + (size_t)s7_bar_bytes(sh.ns7 + sh.nsp + sh.nsc) + (r7 > rh ? r7 : rh);
+  return 128 + (size_t)s7_bar_bytes(sh.ns7 + sh.nsp + sh.nsc) + (fam == kBatch7 ? r7 : rh);
 }
 
-int batch_occupancy(const BatchShape &sh) {
+namespace {
+const void *batch_fn(int fam) {
+  return fam == kBatch7 ? reinterpret_cast<const void *>(batch_kernel<kBatch7>)
+                        : reinterpret_cast<const void *>(batch_kernel<kBatchHimeno>);
+}
+}  // namespace
+
+int batch_occupancy(const BatchShape &sh, int fam) {
   int oc = 0;
-  const size_t smem = batch_smem_bytes(sh);
-  if (cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  const size_t smem = batch_smem_bytes(sh, fam);
+  if (cudaFuncSetAttribute(batch_fn(fam), cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oc, batch_kernel, 32 * sh.warps, smem) !=
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&oc, batch_fn(fam), 32 * sh.warps, smem) !=
           cudaSuccess) {
     cudaGetLastError();
     return 0;
@@ -128,12 +139,15 @@ int batch_occupancy(const BatchShape &sh) {
 }
 
 cudaError_t launch_batch(const BatchProblem *probs_dev, int nprob, const CUtensorMap *tmaps_dev,
-                         int64_t total_items, int parity, const BatchShape &sh, int grid,
+                         int64_t total_items, int parity, const BatchShape &sh, int grid, int fam,
                          cudaStream_t s) {
-  const size_t smem = batch_smem_bytes(sh);
-  batch_kernel<<<grid, dim3(32, sh.warps, 1), smem, s>>>(probs_dev, nprob, tmaps_dev,
-                                                         total_items, parity, sh.ns7, sh.nsp,
-                                                         sh.nsc);
+  const size_t smem = batch_smem_bytes(sh, fam);
+  if (fam == kBatch7)
+    batch_kernel<kBatch7><<<grid, dim3(32, sh.warps, 1), smem, s>>>(
+        probs_dev, nprob, tmaps_dev, total_items, parity, sh.ns7, sh.nsp, sh.nsc);
+  else
+    batch_kernel<kBatchHimeno><<<grid, dim3(32, sh.warps, 1), smem, s>>>(
+        probs_dev, nprob, tmaps_dev, total_items, parity, sh.ns7, sh.nsp, sh.nsc);
   return cudaGetLastError();
 }
 

@@ -26,10 +26,15 @@ struct BatchShape {
   int nsp, nsc;  // Himeno p ring and coefficient ring stages
 };
 
-size_t batch_smem_bytes(const BatchShape &sh);
-int batch_occupancy(const BatchShape &sh);  // CTAs per SM (0 on error)
+// Kernel families: one launch runs the problems of one family.
+constexpr int kBatch7 = 0;       // DIFFUSION7, SUM7, COPY
+constexpr int kBatchHimeno = 1;  // HIMENO19
+
+size_t batch_smem_bytes(const BatchShape &sh, int fam);
+int batch_occupancy(const BatchShape &sh, int fam);  // CTAs per SM (0 on error)
+// probs_dev[0 .. nprob) are the family's problems, item_begin counted from 0.
 cudaError_t launch_batch(const BatchProblem *probs_dev, int nprob, const CUtensorMap *tmaps_dev,
-                         int64_t total_items, int parity, const BatchShape &sh, int grid,
+                         int64_t total_items, int parity, const BatchShape &sh, int grid, int fam,
                          cudaStream_t s);
 
 }  // namespace psg

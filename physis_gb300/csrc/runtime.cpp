@@ -97,6 +97,10 @@ struct Map {
 struct Runtime {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // a second stream for the Himeno launch of a batch step, forked from and
+  // joined back into `stream` by the two events
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
   int sm_count = 0;
   bool trace = false;
   int *dev_err = nullptr;
@@ -1165,11 +1169,14 @@ struct Batch {
   std::vector<const Grid *> grids;    // every grid the batch touches
   std::vector<void *> ptrs;           // their storage when the device tables were built
   psg::BatchShape shape{};
-  psg::BatchProblem *probs_dev = nullptr;
+  psg::BatchProblem *probs_dev = nullptr;  // the 7-point family's problems, then Himeno's
   CUtensorMap *tmaps_dev = nullptr;
-  int64_t total_items = 0;
-  int grid = 0;
-  cudaGraphExec_t graph = nullptr;    // maps_per_run x kGraphUnroll launches
+  // per kernel family (psg::kBatch7, psg::kBatchHimeno): its problems
+  // probs_dev[prob_off .. prob_off + nprob), their items, the launch's grid
+  int nprob[2] = {0, 0}, prob_off[2] = {0, 0}, grid[2] = {0, 0};
+  int64_t total_items[2] = {0, 0};
+  cudaGraphExec_t graph = nullptr;    // maps_per_run x kGraphUnroll steps
+  long long graph_launches = 0;       // kernels one replay of graph runs
 };
 std::vector<Batch> g_batches;
 // {warps, max rows (computed per batch), 7-point stages, Himeno p / coef stages}
@@ -1207,14 +1214,36 @@ bool batch_build(Batch &b) {
     if (m->kernel != PS_KERNEL_HIMENO19 && rows[r] > b.shape.max_rows)
       b.shape.max_rows = rows[r];
   }
-  const int occ = psg::batch_occupancy(b.shape);
-  if (occ < 1) return fail(PS_ERR_CUDA, "batch kernel does not fit on an SM");
-  const int resident = rt->sm_count * occ;
+  // problems ordered by kernel family (each family is one launch), runs in
+  // their given order inside a family
+  auto family = [&](int r) {
+    return b.maps[(size_t)r * M]->kernel == PS_KERNEL_HIMENO19 ? psg::kBatchHimeno
+                                                               : psg::kBatch7;
+  };
+  std::vector<int> order;
+  for (int f = 0; f < 2; ++f) {
+    b.nprob[f] = 0;
+    b.prob_off[f] = (int)order.size();
+    b.total_items[f] = 0;
+    for (int r = 0; r < b.nruns; ++r)
+      if (family(r) == f) {
+        order.push_back(r);
+        ++b.nprob[f];
+      }
+  }
+  int resident[2] = {0, 0};
+  for (int f = 0; f < 2; ++f) {
+    if (!b.nprob[f]) continue;
+    const int occ = psg::batch_occupancy(b.shape, f);
+    if (occ < 1) return fail(PS_ERR_CUDA, "batch kernel does not fit on an SM");
+    resident[f] = rt->sm_count * occ;
+  }
   std::vector<psg::BatchProblem> probs(b.nruns);
   std::vector<CUtensorMap> tmaps;
-  int64_t item = 0;
-  for (int r = 0; r < b.nruns; ++r) {
-    psg::BatchProblem &bp = probs[r];
+  for (int i = 0; i < b.nruns; ++i) {
+    const int r = order[i];
+    const int fam = family(r);
+    psg::BatchProblem &bp = probs[i];
     memset(&bp, 0, sizeof(bp));
     const Map *m0 = b.maps[(size_t)r * M];
     const Grid *g = m0->grids[0];
@@ -1225,10 +1254,10 @@ bool batch_build(Batch &b) {
     const int tiles_x = (m0->dom.max[0] - xbase + 127) / 128;
     bp.tiles = tiles_x * ((m0->dom.max[1] - m0->dom.min[1] + tyy - 1) / tyy);
     const int nzd = m0->dom.max[2] - m0->dom.min[2];
-    bp.zlen = psg::choose_zchunk(bp.tiles, nzd, resident);
+    bp.zlen = psg::choose_zchunk(bp.tiles, nzd, resident[fam]);
     bp.items = (int64_t)bp.tiles * ((nzd + bp.zlen - 1) / bp.zlen);
-    bp.item_begin = item;
-    item += bp.items;
+    bp.item_begin = b.total_items[fam];
+    b.total_items[fam] += bp.items;
     bp.dmin2 = m0->dom.min[2];
     bp.dmax2 = m0->dom.max[2];
     for (int par = 0; par < 2; ++par) {
@@ -1299,8 +1328,8 @@ bool batch_build(Batch &b) {
       }
     }
   }
-  b.total_items = item;
-  b.grid = (int)std::min<int64_t>(resident, std::max<int64_t>(item, 1));
+  for (int f = 0; f < 2; ++f)
+    b.grid[f] = (int)std::min<int64_t>(resident[f], std::max<int64_t>(b.total_items[f], 1));
   if (!cuda_ok(cudaMalloc(&b.probs_dev, sizeof(psg::BatchProblem) * probs.size()), "cudaMalloc") ||
       !cuda_ok(cudaMalloc(&b.tmaps_dev, sizeof(CUtensorMap) * tmaps.size()), "cudaMalloc") ||
       !cuda_ok(cudaMemcpyAsync(b.probs_dev, probs.data(), sizeof(psg::BatchProblem) * probs.size(),
@@ -1314,11 +1343,25 @@ bool batch_build(Batch &b) {
   return true;
 }
 
+// One step of every run: one launch per kernel family present.  With both
+// families the Himeno launch runs on the side stream, concurrently with the
+// 7-point one, so each fills the SMs the other leaves idle at its tail.
 bool batch_launch(Batch &b, int parity) {
-  cudaError_t e = psg::launch_batch(b.probs_dev, b.nruns, b.tmaps_dev, b.total_items, parity,
-                                    b.shape, b.grid, rt->stream);
-  if (!cuda_ok(e, "batch launch")) return false;
-  ++rt->launches;
+  const bool both = b.nprob[0] && b.nprob[1];
+  if (both && (!cuda_ok(cudaEventRecord(rt->fork, rt->stream), "cudaEventRecord") ||
+               !cuda_ok(cudaStreamWaitEvent(rt->side, rt->fork, 0), "cudaStreamWaitEvent")))
+    return false;
+  for (int f = 0; f < 2; ++f) {
+    if (!b.nprob[f]) continue;
+    cudaStream_t s = (both && f == psg::kBatchHimeno) ? rt->side : rt->stream;
+    cudaError_t e = psg::launch_batch(b.probs_dev + b.prob_off[f], b.nprob[f], b.tmaps_dev,
+                                      b.total_items[f], parity, b.shape, b.grid[f], f, s);
+    if (!cuda_ok(e, "batch launch")) return false;
+    ++rt->launches;
+  }
+  if (both && (!cuda_ok(cudaEventRecord(rt->join, rt->side), "cudaEventRecord") ||
+               !cuda_ok(cudaStreamWaitEvent(rt->stream, rt->join, 0), "cudaStreamWaitEvent")))
+    return false;
   return true;
 }
 
@@ -1523,6 +1566,9 @@ void PSInitV(int trace) {
   }
   if (!cuda_ok(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking),
                "cudaStreamCreate") ||
+      !cuda_ok(cudaStreamCreateWithFlags(&r->side, cudaStreamNonBlocking), "cudaStreamCreate") ||
+      !cuda_ok(cudaEventCreateWithFlags(&r->fork, cudaEventDisableTiming), "cudaEventCreate") ||
+      !cuda_ok(cudaEventCreateWithFlags(&r->join, cudaEventDisableTiming), "cudaEventCreate") ||
       !cuda_ok(cudaMalloc(&r->dev_err, sizeof(int)), "cudaMalloc") ||
       !cuda_ok(cudaMalloc(&r->partials, sizeof(uint64_t) * kMaxPartials), "cudaMalloc") ||
       !cuda_ok(cudaMalloc(&r->ticket, sizeof(unsigned)), "cudaMalloc") ||
@@ -1569,6 +1615,9 @@ void PSFinalize(void) {
   cudaFree(rt->ticket);
   cudaFree(rt->results);
   for (int i = 0; i < kNumEvents; ++i) cudaEventDestroy(rt->events[i]);
+  cudaEventDestroy(rt->fork);
+  cudaEventDestroy(rt->join);
+  cudaStreamDestroy(rt->side);
   cudaStreamDestroy(rt->stream);
   delete rt;
   rt = nullptr;
@@ -2336,12 +2385,13 @@ void PSBatchRun(int batch, int iter) {
         if (graph) cudaGraphDestroy(graph);
       }
       cudaGetLastError();
+      b.graph_launches = rt->launches - l0;  // kernels in one replay
       rt->launches = l0;
     }
     if (b.graph) {
       for (; i + kGraphUnroll <= iter; i += kGraphUnroll) {
         if (!cuda_ok(cudaGraphLaunch(b.graph, rt->stream), "cudaGraphLaunch")) return;
-        rt->launches += (long long)M * kGraphUnroll;
+        rt->launches += b.graph_launches;
       }
     }
   }
@@ -2355,7 +2405,8 @@ void PSSetBatchShape(int warps, int rows, int ns7, int nsp, int nsc) {
   psg::BatchShape sh{warps, 4, ns7, nsp, nsc};
   if (warps < 1 || warps > 8 || !(rows == 1 || rows == 2 || rows == 4) || ns7 < 2 ||
       ns7 > 8 || nsp < 3 || nsp > 8 || nsc < 1 || nsc > 4 ||
-      psg::batch_smem_bytes(sh) > 227 * 1024) {
+      psg::batch_smem_bytes(sh, psg::kBatch7) > 227 * 1024 ||
+      psg::batch_smem_bytes(sh, psg::kBatchHimeno) > 227 * 1024) {
     fail(PS_ERR_INVALID_ARGUMENT, "PSSetBatchShape: warps %d ns7 %d nsp %d nsc %d", warps,
          ns7, nsp, nsc);
     return;

@@ -600,7 +600,8 @@ def test_batch_of_uneven_runs_bit_exact(rt, oracle, iters):
     b = ps.batch_create(runs)
     n0 = ps.launch_count()
     ps.batch_run(b, iters)
-    assert ps.launch_count() - n0 == 2 * iters  # one launch per step for all runs
+    # one launch per kernel family (7-point, Himeno) per step for all runs
+    assert ps.launch_count() - n0 == 2 * 2 * iters
     for ga, gb, ra, rb in refs:
         assert np.array_equal(_bits(ga.copyout()), _bits(ra))
         assert np.array_equal(_bits(gb.copyout()), _bits(rb))
