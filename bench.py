@@ -332,6 +332,8 @@ def run_gpu(args, dist):
     if args.temporal > 1:
         tw, tr, tn = (int(v) for v in args.tshape.split(","))
         ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, args.temporal, warps=tw, rows=tr, ns=tn)
+    if args.fma:
+        ps.set_fma(True)
     m1 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g1, g2], COEF)
     m2 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g2, g1], COEF)
     K, W = args.steps, args.warmup
@@ -390,6 +392,27 @@ def run_gpu(args, dist):
     L.PSHostFree(hin)
     L.PSHostFree(hout)
 
+    # the same run with temporal blocking (k = 2 steps per pass): bit-exact,
+    # and with contracted multiply-adds (within 1e-5 of REF)
+    temporal = None
+    if args.temporal == 1:
+        temporal = {"k": 2, "tshape": "8,4,3", "steps": K}
+        for key, fma in (("glups_bit_exact", False), ("glups_fma", True)):
+            ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 2, warps=8, rows=4, ns=3)
+            ps.set_fma(fma)
+            steps(W)
+            ps.synchronize()
+            dist.barrier()
+            L.PSEventRecord(0)
+            steps(K)
+            L.PSEventRecord(1)
+            ps.synchronize()
+            tms = dist.reduce(L.PSEventElapsedMs(0, 1), "MAX")
+            temporal[key] = dist.ws * cells * K / (tms / 1e3) / 1e9
+        ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 1)
+        ps.set_fma(False)
+        ps.check()
+
     peak, peak_kind = measured_peaks()
     achieved = cells * BYTES_PER_LUP / (ms / K / 1e3) / 1e9
     traffic = profiled_traffic()
@@ -421,6 +444,8 @@ def run_gpu(args, dist):
                                  "ctas_per_sm": shape_used[4] or "auto"},
                 "e2e_job": "PSGridCopyin(pinned) + K steps + PSGridCopyout(pinned)",
                 "temporal_k": args.temporal,
+                "temporal_tshape": args.tshape if args.temporal > 1 else None,
+                "fma": bool(args.fma),
             },
             "e2e": {"value": e2e, "unit": "GLUPS",
                     "h2d_bytes_per_step": nbytes / K,
@@ -435,6 +460,7 @@ def run_gpu(args, dist):
             "clocks": clk,
             "cpu_baseline": cpu,
             "reference_cuda_kernels": ref_cuda,
+            "temporal_blocking": temporal,
         }
         print(json.dumps(line), flush=True)
     g1.free()
@@ -1022,6 +1048,9 @@ def main():
                     help="diffusion: temporal blocking depth k (1 = plain sweeps)")
     ap.add_argument("--tshape", default="8,4,3",
                     help="warps,rows,ring stages of the temporal passes")
+    ap.add_argument("--fma", action="store_true",
+                    help="diffusion: temporal passes contract multiply-adds "
+                         "(PSSetFusedMultiplyAdd; results within 1e-5 of REF)")
     ap.add_argument("--ws-train", type=int, default=4096)
     ap.add_argument("--ws-held", type=int, default=256)
     ap.add_argument("--ws-steps", type=int, default=25600,

@@ -143,6 +143,16 @@ void PSGetLaunchShape(int kernel, PSLaunchShape *shape);
 void PSSetTemporalBlocking(int kernel, int k, const PSLaunchShape *shape);
 void PSGetTemporalBlocking(int kernel, int *k, PSLaunchShape *shape);
 
+/* Contraction (default 0: off).  With 1, temporal passes evaluate each
+ * update's left-to-right sum as one multiply and six fused multiply-adds
+ * instead of seven multiplies and six adds.  Results then differ from the
+ * REF target, and from plain sweeps, by rounding only: within 1e-5 relative
+ * per cell, the tolerance the tests hold them to.  Plain sweeps stay
+ * bit-exact either way.  With contraction on, autotuner trials may mix the
+ * two roundings. */
+void PSSetFusedMultiplyAdd(int on);
+int PSGetFusedMultiplyAdd(void);
+
 /* Autotuner (replaces the reference's online trial of OPT_* variants and
  * block sizes, translator/reference_translator.cc:610-935).  When on
  * (PSSetAutotune(1) or PS_AUTOTUNE=1 at PSInit), the first iterations of a

@@ -53,7 +53,8 @@ PSGridDevicePtr PSGridPitch PSGridElemSize PSGridType PSGridCopyinAsync
 PSGridCopyoutAsync PSHostAlloc PSHostFree PSSynchronize PSGetStream
 PSEventRecord PSEventElapsedMs PSGetLaunchCount PSGetSMCount PSSetLaunchShape
 PSGetLaunchShape PSTestFailNextAllocs PSTestDeviceWaitTimeout PSReduceNoAlloc
-PSSetTemporalBlocking PSGetTemporalBlocking PSSetAutotune PSSetTuneCachePath
+PSSetTemporalBlocking PSGetTemporalBlocking PSSetFusedMultiplyAdd PSGetFusedMultiplyAdd
+PSSetAutotune PSSetTuneCachePath
 PSLoadTuneCache PSClearTuning PSGetStencilPlan PSBatchCreate PSBatchRun PSBatchFree
 PSSetBatchShape __PSStencilMapRedBlack __PSStencilMapRed __PSStencilMapBlack
 PSStencilMapColorV PSPointStencilNew PSStencilFunctionNew
@@ -386,6 +387,12 @@ def set_temporal(kernel, k, warps=0, rows=0, ns=0, ctas_per_sm=0):
     """Temporal blocking depth k (1 = off) and the passes' launch shape."""
     sh = PSLaunchShape(warps, rows, ns, 0, ctas_per_sm)
     lib().PSSetTemporalBlocking(kernel, k, ctypes.byref(sh))
+    check()
+
+
+def set_fma(on):
+    """Allow temporal passes to contract multiply-adds (PSSetFusedMultiplyAdd)."""
+    lib().PSSetFusedMultiplyAdd(1 if on else 0)
     check()
 
 

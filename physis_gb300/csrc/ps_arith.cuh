@@ -24,12 +24,19 @@ struct RN<float> {
   static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
   static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
   static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+  // a * b + c rounded once (kernels that may contract)
+  static __device__ __forceinline__ float fma(float a, float b, float c) {
+    return __fmaf_rn(a, b, c);
+  }
 };
 template <>
 struct RN<double> {
   static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
   static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
   static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ double fma(double a, double b, double c) {
+    return __fma_rn(a, b, c);
+  }
 };
 // Integer grids wrap modulo 2^32 / 2^64 like the REF target's C arithmetic
 // on two's-complement hosts; compute in unsigned to keep that defined.

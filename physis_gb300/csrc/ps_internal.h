@@ -90,6 +90,7 @@ struct Temporal7Args {
   GridView in, out;
   double coef[7];  // map argument order: ce cw cn cs ct cb cc
   int k;
+  bool fma;        // contract each multiply-add (else bit-exact to k plain steps)
 };
 int temporal7_max_k(int esz);
 size_t temporal7_smem_bytes(int esz, const MarchConfig &cfg, int k);

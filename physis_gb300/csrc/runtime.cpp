@@ -116,6 +116,7 @@ struct Runtime {
   MarchConfig tshapes[kNumKernels];        // launch shape of temporal passes
   std::vector<TmapEntry> tmaps;
   int fail_allocs = 0;
+  bool fma = false;  // temporal passes may contract multiply-adds
   bool autotune = false;
   std::string tune_path;  // JSON-lines cache file ("" = in memory only)
   std::string gpu_name;
@@ -626,6 +627,7 @@ bool launch_t7(const Map &m, const GridView &in, const GridView &out, int k) {
   a.in = in;
   a.out = out;
   a.k = k;
+  a.fma = rt->fma;
   for (int i = 0; i < 7; ++i) a.coef[i] = m.scalars[i];
   const MarchConfig cfg = m.has_plan ? m.plan.tshape : rt->tshapes[shape_slot(m.kernel)];
   const int vec = 16 / in.esz;
@@ -2164,6 +2166,16 @@ void PSSetTemporalBlocking(int kernel, int k, const PSLaunchShape *shape) {
   }
   rt->tshapes[kernel] = c;
   rt->tblock[kernel] = k;
+}
+
+void PSSetFusedMultiplyAdd(int on) {
+  if (!need_rt("PSSetFusedMultiplyAdd")) return;
+  rt->fma = on != 0;
+}
+
+int PSGetFusedMultiplyAdd(void) {
+  if (!need_rt("PSGetFusedMultiplyAdd")) return 0;
+  return rt->fma ? 1 : 0;
 }
 
 void PSGetTemporalBlocking(int kernel, int *k, PSLaunchShape *shape) {

@@ -423,6 +423,42 @@ def test_temporal_blocking_bit_exact(rt, oracle, k, warps, rows, ns, shape, iter
     assert np.array_equal(_bits(b), _bits(r2))
 
 
+@pytest.mark.parametrize("k,warps,rows,ns", [(2, 8, 4, 3), (3, 8, 2, 3), (5, 4, 4, 3)])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_temporal_blocking_with_fma_within_tolerance(rt, oracle, k, warps, rows, ns, dtype):
+    # Contracted temporal passes: within 1e-5 relative per cell of the REF
+    # target and of an FP64 evaluation; not bit-identical to it (the fused
+    # kernel really ran); plain sweeps stay bit-exact with contraction on.
+    if dtype == np.float64 and k > 3:
+        pytest.skip("double grids block at most 3 steps per pass")
+    shape = (37, 45, 70)
+    iters = 6
+    init = synth.uniform(shape, 12).astype(dtype)
+    ps.set_fma(True)
+    ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, k, warps=warps, rows=rows, ns=ns)
+    try:
+        a, b = run_pingpong(ps.PS_KERNEL_DIFFUSION7, init, ps.full_domain(shape), DIFF_COEF,
+                            iters, dtype)
+        ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 1)
+        pa, pb = run_pingpong(ps.PS_KERNEL_DIFFUSION7, init, ps.full_domain(shape), DIFF_COEF,
+                              iters, dtype)
+    finally:
+        ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 1)
+        ps.set_fma(False)
+    nz, ny, nx = shape
+    dom = (0, nx, 0, ny, 0, nz)
+    r1, r2 = init.copy(), np.zeros_like(init)
+    oracle.run7(oracle.V_DIFFUSION7, r1, r2, dom, DIFF_COEF, iter=iters)
+    f1, f2 = init.astype(np.float64), np.zeros(shape)
+    oracle.run7(oracle.V_DIFFUSION7, f1, f2, dom, DIFF_COEF, iter=iters)
+    for got, ref, ref64 in ((a, r1, f1), (b, r2, f2)):
+        assert np.allclose(got, ref, rtol=1e-5, atol=0)
+        assert np.allclose(got, ref64, rtol=1e-5, atol=0)
+    assert not np.array_equal(_bits(a), _bits(r1))
+    assert np.array_equal(_bits(pa), _bits(r1))
+    assert np.array_equal(_bits(pb), _bits(r2))
+
+
 @pytest.mark.parametrize("k", [2, 3])
 def test_temporal_blocking_double(rt, oracle, k):
     shape = (19, 33, 70)
