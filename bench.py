@@ -410,6 +410,22 @@ def run_gpu(args, dist):
             tms = dist.reduce(L.PSEventElapsedMs(0, 1), "MAX")
             temporal[key] = dist.ws * cells * K / (tms / 1e3) / 1e9
         ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 1)
+        # the autotuner's choice (plain shapes and k = 2..4) with contraction
+        # on: its trials run inside the warm-up, then K timed steps
+        ps.set_autotune(True)
+        steps(max(W, 200))
+        ps.synchronize()
+        tuned, shape_t, k_t, tshape_t = ps.stencil_plan(m1)
+        dist.barrier()
+        L.PSEventRecord(0)
+        steps(K)
+        L.PSEventRecord(1)
+        ps.synchronize()
+        tms = dist.reduce(L.PSEventElapsedMs(0, 1), "MAX")
+        temporal["autotuned_fma"] = {"glups": dist.ws * cells * K / (tms / 1e3) / 1e9,
+                                     "tuned": tuned, "k": k_t, "launch_shape": list(shape_t),
+                                     "temporal_shape": list(tshape_t)}
+        ps.set_autotune(False)
         ps.set_fma(False)
         ps.check()
 

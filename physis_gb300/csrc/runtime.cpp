@@ -872,7 +872,8 @@ std::string run_key(const std::vector<Map *> &ms) {
       k += buf;
     }
   }
-  if (ms.size() == 2 && pair_eligible(*ms[0], *ms[1])) k += "pair;";
+  // temporal candidates time differently with contraction on
+  if (ms.size() == 2 && pair_eligible(*ms[0], *ms[1])) k += rt->fma ? "pair-fma;" : "pair;";
   snprintf(buf, sizeof(buf), "%s/%dsm", rt->gpu_name.c_str(), rt->sm_count);
   return k + buf;
 }
