@@ -954,8 +954,9 @@ def run_gpu_warmstart(args, dist):
     # comparison (counted in the output).
     reset()
     zero = st.solve(1e-6, echunk, args.ws_max_sweeps)
+    pm = args.ws_predict_mirrors
     reset()
-    ws.predict_into(net, st, scales, factor)
+    ws.predict_into(net, st, scales, factor, pm)
     r_warm0 = st.residuals()
     warm = st.solve(1e-6, echunk, args.ws_max_sweeps)
     both = (zero > 0) & (warm > 0)
@@ -967,7 +968,7 @@ def run_gpu_warmstart(args, dist):
         torch.cuda.synchronize()
         t = time.perf_counter()
         if warm_start:
-            ws.predict_into(net, st, scales, factor)
+            ws.predict_into(net, st, scales, factor, pm)
         st.sweeps(n)
         ps.synchronize()
         return time.perf_counter() - t
@@ -1016,6 +1017,7 @@ def run_gpu_warmstart(args, dist):
                               "-> Catmull-Rom",
                    "epochs": epochs, "adam_steps": epochs * per_epoch, "batch": 32,
                    "mirror_images": len(data.flips),
+                   "prediction_mirror_images": len(ws.mirror_images(shape, pm)),
                    "l2": f"held-out stack: 14 arrays, {stack_gb:.1f} GB in all, > L2"},
         "compared_instances": int(both.sum()),
         "below_1e-6_unreachable": {"zero_start": int((zero <= 0).sum()),
@@ -1073,6 +1075,8 @@ def main():
                     help="warm start: Adam steps (minibatches of 32) of training")
     ap.add_argument("--ws-mirrors", type=int, default=16,
                     help="warm start: training pairs per solved instance (its mirror images)")
+    ap.add_argument("--ws-predict-mirrors", type=int, default=16,
+                    help="warm start: mirror images whose predictions are averaged")
     ap.add_argument("--ws-nx", type=int, default=33)
     ap.add_argument("--ws-ny", type=int, default=33)
     ap.add_argument("--ws-nz", type=int, default=65)

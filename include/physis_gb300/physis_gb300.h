@@ -346,8 +346,10 @@ typedef struct PSWarmStartFields {
   float wscale, pscale;
   /* Mirror image the pooling calls read (0: the instance itself): bits 0, 1,
    * 2 mirror x, y, z; bit 3 swaps x and y together with a2 and a1, the x
-   * and y coefficients (needs inx == iny).  With c_i = a_i and b = 0 the mirrored fields' solution is
-   * the mirrored solution.  PSWarmStartUpsample needs 0. */
+   * and y coefficients (needs inx == iny).  With c_i = a_i and b = 0 the
+   * mirrored fields' solution is the mirrored solution.  For the upsampling
+   * calls, `coarse` is a prediction for this mirror image; they write the
+   * stored instance. */
   int flip;
 } PSWarmStartFields;
 
@@ -363,6 +365,10 @@ int PSWarmStartPoolTarget(const PSWarmStartFields *f, float *out, void *stream);
  * Catmull-Rom interpolation per axis from coarse cell centres at
  * (c + 0.5) * factor - 0.5 (clamped). */
 int PSWarmStartUpsample(const PSWarmStartFields *f, const float *coarse, float *p, void *stream);
+/* The same added to p (p += ...): averaging the predictions for several
+ * mirror images (pscale times their count) gives one warm start. */
+int PSWarmStartUpsampleAdd(const PSWarmStartFields *f, const float *coarse, float *p,
+                           void *stream);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop

@@ -206,6 +206,21 @@ def mirror(field, flip):
     return np.ascontiguousarray(a)
 
 
+def unmirror(field, flip):
+    """The inverse of mirror(): a field given in mirror-image coordinates,
+    back in the stored instance's."""
+    a = np.asarray(field)
+    if flip & 4:
+        a = a[::-1, :, :]
+    if flip & 2:
+        a = a[:, ::-1, :]
+    if flip & 1:
+        a = a[:, :, ::-1]
+    if flip & 8:
+        a = a.transpose(0, 2, 1)
+    return np.ascontiguousarray(a)
+
+
 def mirror_instance(inst, flip):
     """The mirrored instance: every field mirrored, a2 and a1 exchanged under
     the x/y swap (the 19-point sweep weighs the z neighbours with a0, the y

@@ -60,7 +60,7 @@ PSSetBatchShape __PSStencilMapRedBlack __PSStencilMapRed __PSStencilMapBlack
 PSStencilMapColorV PSPointStencilNew PSStencilFunctionNew
 PSStencilFunctionCheck PSWarmStartConv PSWarmStartWeightGrad PSWarmStartPrepareWeights
 PSWarmStartAdam PSWarmStartLoss PSWarmStartPool PSWarmStartPoolTarget
-PSWarmStartUpsample""".split()
+PSWarmStartUpsample PSWarmStartUpsampleAdd""".split()
 
 
 class PSDomain(ctypes.Structure):
@@ -192,9 +192,10 @@ def lib():
     L.PSWarmStartPool.argtypes = [fp, vp, vp]
     L.PSWarmStartPoolTarget.argtypes = [fp, vp, vp]
     L.PSWarmStartUpsample.argtypes = [fp, vp, vp, vp]
+    L.PSWarmStartUpsampleAdd.argtypes = [fp, vp, vp, vp]
     for name in ("PSWarmStartConv", "PSWarmStartWeightGrad", "PSWarmStartPrepareWeights",
                  "PSWarmStartAdam", "PSWarmStartLoss", "PSWarmStartPool",
-                 "PSWarmStartPoolTarget", "PSWarmStartUpsample"):
+                 "PSWarmStartPoolTarget", "PSWarmStartUpsample", "PSWarmStartUpsampleAdd"):
         getattr(L, name).restype = i
     _lib = L
     return L

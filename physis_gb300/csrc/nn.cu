@@ -569,16 +569,23 @@ __device__ __forceinline__ void catmull_rom(float t, float (&w)[4]) {
 // Coarse prediction (FP32, one value per coarse cell) -> fine p:
 // Catmull-Rom cubic interpolation per axis from coarse centres at
 // (c + 0.5) f - 0.5 (positions clamped to [0, nc - 1], neighbour indices to
-// the coarse grid), divided by pscale, times bnd.  Writes every fine cell of
-// every instance.
+// the coarse grid), divided by pscale, times bnd.  Writes (or, with add,
+// adds to) every fine cell of every instance.  With a mirror (flip != 0) the
+// coarse grid is a prediction for that mirror image: stored cell (z, y, x)
+// reads it at its mirror-image coordinates.
 __global__ void upsample_kernel(PoolArgs a, const float *__restrict__ coarse,
-                                float *__restrict__ p) {
+                                float *__restrict__ p, bool add) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long n = (long long)a.batch * a.inz * a.iny * a.inx;
   if (i >= n) return;
   const int x = (int)(i % a.inx), y = (int)((i / a.inx) % a.iny);
   const int z = (int)((i / ((long long)a.inx * a.iny)) % a.inz);
   const int b = (int)(i / ((long long)a.inx * a.iny * a.inz));
+  // mirror-image coordinates of stored cell (z, y, x): undo vmap
+  int xm = (a.flip & 8) ? y : x, ym = (a.flip & 8) ? x : y, zm = z;
+  if (a.flip & 1) xm = a.inx - 1 - xm;
+  if (a.flip & 2) ym = a.iny - 1 - ym;
+  if (a.flip & 4) zm = a.inz - 1 - zm;
   auto axis = [&](int j, int nc, int (&idx)[4], float (&w)[4]) {
     float pos = ((float)j + 0.5f) / (float)a.f - 0.5f;
     pos = fminf(fmaxf(pos, 0.f), (float)(nc - 1));
@@ -588,9 +595,9 @@ __global__ void upsample_kernel(PoolArgs a, const float *__restrict__ coarse,
   };
   int iz[4], iy[4], ix[4];
   float wz[4], wy[4], wx[4];
-  axis(z, a.zc, iz, wz);
-  axis(y, a.yc, iy, wy);
-  axis(x, a.xc, ix, wx);
+  axis(zm, a.zc, iz, wz);
+  axis(ym, a.yc, iy, wy);
+  axis(xm, a.xc, ix, wx);
   const float *c = coarse + (long long)b * a.zc * a.yc * a.xc;
   float v = 0.f;
   for (int kz = 0; kz < 4; ++kz) {
@@ -604,7 +611,8 @@ __global__ void upsample_kernel(PoolArgs a, const float *__restrict__ coarse,
     v += wz[kz] * vy;
   }
   const long long k = fine_index(a, b, z, y, x);
-  p[k] = v / a.pscale * a.bnd[k];
+  const float u = v / a.pscale * a.bnd[k];
+  p[k] = add ? p[k] + u : u;
 }
 
 }  // namespace
@@ -720,11 +728,11 @@ int nn_pool_target(const NNFields &f, float *out, cudaStream_t s) {
   return (int)cudaGetLastError();
 }
 
-int nn_upsample(const NNFields &f, const float *coarse, float *p, cudaStream_t s) {
+int nn_upsample(const NNFields &f, const float *coarse, float *p, bool add, cudaStream_t s) {
   const PoolArgs a = pool_args(f);
   const long long n = (long long)a.batch * a.inz * a.iny * a.inx;
-  if (n <= 0 || a.flip) return -1;
-  upsample_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, coarse, p);
+  if (n <= 0) return -1;
+  upsample_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, coarse, p, add);
   return (int)cudaGetLastError();
 }
 

@@ -235,7 +235,7 @@ int nn_mse(const float *pred, const float *tgt, long long n, void *dy, double *p
            cudaStream_t s);
 int nn_pool_inputs(const NNFields &f, void *out, cudaStream_t s);
 int nn_pool_target(const NNFields &f, float *out, cudaStream_t s);
-int nn_upsample(const NNFields &f, const float *coarse, float *p, cudaStream_t s);
+int nn_upsample(const NNFields &f, const float *coarse, float *p, bool add, cudaStream_t s);
 
 // ---- Reductions (reduce.cu) ----------------------------------------------
 // Reduces every element of g with op.  The 8-byte result is written to

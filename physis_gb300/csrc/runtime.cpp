@@ -2305,8 +2305,16 @@ int PSWarmStartPoolTarget(const PSWarmStartFields *f, float *out, void *stream) 
 int PSWarmStartUpsample(const PSWarmStartFields *f, const float *coarse, float *p, void *stream) {
   if (!ws_fields_ok(f, "PSWarmStartUpsample", false) || !coarse || !p)
     return PS_ERR_INVALID_ARGUMENT;
-  return ws_status(psg::nn_upsample(ws_fields(f), coarse, p, ws_stream(stream)),
+  return ws_status(psg::nn_upsample(ws_fields(f), coarse, p, false, ws_stream(stream)),
                    "PSWarmStartUpsample");
+}
+
+int PSWarmStartUpsampleAdd(const PSWarmStartFields *f, const float *coarse, float *p,
+                           void *stream) {
+  if (!ws_fields_ok(f, "PSWarmStartUpsampleAdd", false) || !coarse || !p)
+    return PS_ERR_INVALID_ARGUMENT;
+  return ws_status(psg::nn_upsample(ws_fields(f), coarse, p, true, ws_stream(stream)),
+                   "PSWarmStartUpsampleAdd");
 }
 
 int PSReduceNoAlloc(const void *data, size_t pitch, int nx, int ny, int nz, int type,

@@ -449,21 +449,27 @@ def train(net, data, epochs, batch, lr, log=None, seed=0):
     return history, time.perf_counter() - t0
 
 
-def predict_into(net, stack, data_scales, factor):
+def predict_into(net, stack, data_scales, factor, mirrors=1):
     """Warm start: pool the stack's fields, run the network, upsample into
-    the stack's p0 (p1 too, so the first sweep starts from it)."""
+    the stack's p0 (p1 too, so the first sweep starts from it).  With
+    mirrors > 1 the prediction is the mean of the network's predictions for
+    that many mirror images of each instance, each mapped back to the
+    instance (the network is not mirror-equivariant, so their errors partly
+    cancel)."""
     import torch
     wscale, pscale = data_scales
     zc, yc, xc = coarse_shape(stack.shape, factor)
     n = stack.count
     L = ps.lib()
-    f = stack.fields(factor, wscale, pscale)
+    flips = mirror_images(stack.shape, mirrors)
     x = torch.empty(n * zc * yc * xc * C, dtype=torch.bfloat16, device="cuda")
-    _ok(L.PSWarmStartPool(ctypes.byref(f), _p(x), net.stream()))
-    pred = net.forward(x, (n, zc, yc, xc))
-    for g in (stack.grids[0], stack.grids[1]):
-        _ok(L.PSWarmStartUpsample(ctypes.byref(f), _p(pred), ctypes.c_void_p(g.dev_ptr),
-                                  net.stream()))
+    for i, flip in enumerate(flips):
+        f = stack.fields(factor, wscale, pscale * len(flips), flip=flip)
+        _ok(L.PSWarmStartPool(ctypes.byref(f), _p(x), net.stream()))
+        pred = net.forward(x, (n, zc, yc, xc))
+        up = L.PSWarmStartUpsample if i == 0 else L.PSWarmStartUpsampleAdd
+        for g in (stack.grids[0], stack.grids[1]):
+            _ok(up(ctypes.byref(f), _p(pred), ctypes.c_void_p(g.dev_ptr), net.stream()))
     torch.cuda.synchronize()
 
 

@@ -225,12 +225,25 @@ def test_pool_and_upsample(rt, shape, flips):
     for b, inst in enumerate(insts):
         ref = nn.upsample(coarse[b].astype(np.float64), shape, 4) / 2.0 * inst["bnd"]
         assert np.allclose(up[st.slot(b)], ref, rtol=1e-5, atol=1e-6)
+    # predictions for mirror images, added into the stored instances
+    for flip in flips:
+        f = st.fields(4, wscale=0.5, pscale=2.0, with_p=True, flip=flip)
+        cm = rng.normal(size=(3, zc, yc, xc)).astype(np.float32)
+        cmt = torch.tensor(cm.ravel(), device="cuda")
+        before = st.grids[1].copyout()
+        assert L.PSWarmStartUpsampleAdd(ctypes.byref(f), _p(cmt),
+                                        ctypes.c_void_p(st.grids[1].dev_ptr), None) == 0
+        ps.synchronize()
+        up = st.grids[1].copyout()
+        for b, inst in enumerate(insts):
+            ref = nn.unmirror(nn.upsample(cm[b].astype(np.float64), shape, 4), flip)
+            ref = before[st.slot(b)] + ref / 2.0 * inst["bnd"]
+            assert np.allclose(up[st.slot(b)], ref, rtol=1e-5, atol=1e-5), flip
     st.free()
 
 
 def test_mirror_argument_checks(rt):
-    # the x/y swap needs a square x-y section; upsampling writes the stored
-    # instance, so it takes no mirror
+    # the x/y swap needs a square x-y section; flip codes are 0..15
     from physis_gb300 import warmstart as ws
     rng = np.random.default_rng(7)
     shape = (9, 6, 5)
@@ -241,8 +254,8 @@ def test_mirror_argument_checks(rt):
     assert L.PSWarmStartPool(ctypes.byref(st.fields(4, flip=8)), _p(x), None) != 0
     assert L.PSWarmStartPool(ctypes.byref(st.fields(4, flip=16)), _p(x), None) != 0
     ct = torch.zeros(zc * yc * xc, dtype=torch.float32, device="cuda")
-    assert L.PSWarmStartUpsample(ctypes.byref(st.fields(4, flip=1)), _p(ct),
-                                 ctypes.c_void_p(st.grids[1].dev_ptr), None) != 0
+    assert L.PSWarmStartUpsampleAdd(ctypes.byref(st.fields(4, flip=9)), _p(ct),
+                                    ctypes.c_void_p(st.grids[1].dev_ptr), None) != 0
     assert ps.last_error()[0] == 2  # PS_ERR_INVALID_ARGUMENT
     ps.clear_error()
     ps.synchronize()

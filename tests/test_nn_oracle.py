@@ -137,3 +137,9 @@ def test_pool_features_definition():
     assert np.isclose(feats[0, 0, 1, 7], -np.log((1 / a[1]).mean()))
     # partial block at the far x edge (one column)
     assert np.isclose(feats[0, 0, 2, 0], np.log(inst["a0"][0:2, 0:2, 4:5]).mean())
+
+
+def test_unmirror_inverts_mirror():
+    a = np.arange(4 * 5 * 5).reshape(4, 5, 5)
+    for flip in range(16):
+        assert np.array_equal(nn.unmirror(nn.mirror(a, flip), flip), a), flip
