@@ -986,6 +986,28 @@ def run_gpu_warmstart(args, dist):
     ok_zero = int((r_zero_end[both] <= 1e-6).sum())
     ok_warm = int((r_end[both] <= 1e-6).sum())
 
+    # Ceiling of the coarse representation (--ws-ceiling): the held-out
+    # instances solved on to 1e-7, their exact block-centre samples upsampled
+    # as a perfect network output would be, and the sweeps to 1e-6 from there.
+    ceiling = None
+    if args.ws_ceiling:
+        import ctypes
+        reset()
+        st.solve(1e-7, echunk * 8, args.ws_max_sweeps * 2)
+        zc, yc, xc = ws.coarse_shape(shape, factor)
+        exact = torch.empty(st.count * zc * yc * xc, dtype=torch.float32, device="cuda")
+        fe = st.fields(factor, 1.0, 1.0, True)
+        ws._ok(ps.lib().PSWarmStartPoolTarget(ctypes.byref(fe), ws._p(exact), None))
+        for g in (st.grids[0], st.grids[1]):
+            ws._ok(ps.lib().PSWarmStartUpsample(ctypes.byref(fe), ws._p(exact),
+                                                ctypes.c_void_p(g.dev_ptr), None))
+        ps.synchronize()
+        best = st.solve(1e-6, echunk, args.ws_max_sweeps)
+        ok = both & (best > 0)
+        ceiling = {"sweeps_mean": float(best[ok].mean()),
+                   "sweeps_ratio_mean": float(zero[ok].mean() / best[ok].mean()),
+                   "what": "warm start from the exact solution's block-centre samples"}
+
     # tensor roofline of the network's forward pass over the training set
     zc, yc, xc = data.dims1
     nvox = data.x.shape[0] * zc * yc * xc
@@ -1031,6 +1053,7 @@ def run_gpu_warmstart(args, dist):
         "training": {"seconds": train_s, "loss_first_epoch": hist[0],
                      "loss_last_epoch": hist[-1]},
         "network_forward_ms": fwd_ms,
+        "representation_ceiling": ceiling,
         "dataset": {"seconds": data_s, "solve_seconds": data.solve_seconds,
                     "target_sweeps_mean": float(data.sweeps.mean())},
         "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s",
@@ -1077,6 +1100,9 @@ def main():
                     help="warm start: training pairs per solved instance (its mirror images)")
     ap.add_argument("--ws-predict-mirrors", type=int, default=16,
                     help="warm start: mirror images whose predictions are averaged")
+    ap.add_argument("--ws-ceiling", action="store_true",
+                    help="warm start: also time the solve from the exact solution's "
+                         "block-centre samples (the coarse representation's ceiling)")
     ap.add_argument("--ws-nx", type=int, default=33)
     ap.add_argument("--ws-ny", type=int, default=33)
     ap.add_argument("--ws-nz", type=int, default=65)
