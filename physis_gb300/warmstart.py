@@ -4,7 +4,8 @@ No counterpart in the reference.  A small 3D convolutional network predicts
 the solution of a variable-coefficient Jacobi solve from its coefficient and
 source fields; Jacobi then iterates from that prediction to the same
 residual tolerance, so the plain zero-start solve stays both the fallback
-and the judge (a bad prediction costs sweeps, it cannot change the answer).
+and the yardstick (a bad prediction costs sweeps, it cannot change the
+answer).
 
 Pieces, all on the GPU through libphysis_gb300's C ABI:
 * instances (seeded, built on the host): coefficients a0, a1, a2 log-uniform
