@@ -229,11 +229,10 @@ template <bool PER> __device__ __forceinline__ int __ps_fit(int v, int n) {
   return min(max(v, 0), n - 1);
 }
 // Plane zp (unwrapped) of the W x H window at (x0 - RX, y0 - RY) into its
-// ring slot.  vec (every window row starts on a 16-byte boundary): 16-byte
-// cp.async chunks, except chunks that reach past an x face of the grid,
-// which copy cell by cell; rows clamp or wrap in y.  Otherwise one cp.async
-// per cell, warp w copying rows w, w + 8, ...  Cells outside the grid wrap
-// (PER) or clamp.
+// ring slot.  vec (the CTA's window lies inside the grid in x and every
+// window row starts on a 16-byte boundary): 16-byte cp.async chunks, rows
+// clamped or wrapped in y.  Otherwise one cp.async per cell, warp w copying
+// rows w, w + 8, ..., cells outside the grid wrapped (PER) or clamped.
 template <typename T, int W, int H, int S, int RX, int RY, bool PER>
 __device__ __forceinline__ void __ps_stage(T *ring, const __PSGridArg<T> &a, int x0, int y0,
                                            bool vec, int zp) {
@@ -243,16 +242,8 @@ __device__ __forceinline__ void __ps_stage(T *ring, const __PSGridArg<T> &a, int
     constexpr int V = 16 / (int)sizeof(T), NV = W / V;
     for (int e = threadIdx.x; e < NV * H; e += 256) {
       const int r = e / NV, c = e - r * NV;
-      const T *srow = src + (long long)__ps_fit<PER>(y0 - RY + r, a.ny) * a.row;
-      const int gx = x0 - RX + c * V;
-      T *d = dst + r * W + c * V;
-      if (gx >= 0 && gx + V <= a.nx) {
-        psg::cp_async16(d, srow + gx);
-      } else {
-#pragma unroll
-        for (int v = 0; v < V; ++v)
-          psg::cp_async_small<(int)sizeof(T)>(d + v, srow + __ps_fit<PER>(gx + v, a.nx));
-      }
+      const T *srow = src + (long long)__ps_fit<PER>(y0 - RY + r, a.ny) * a.row + (x0 - RX);
+      psg::cp_async16(dst + r * W + c * V, srow + c * V);
     }
     return;
   }
@@ -265,11 +256,12 @@ __device__ __forceinline__ void __ps_stage(T *ring, const __PSGridArg<T> &a, int
       psg::cp_async_small<(int)sizeof(T)>(drow + c, srow + __ps_fit<PER>(x0 - RX + c, a.nx));
   }
 }
-// Whether every row of a window at x0 - RX starts on a 16-byte boundary.
-template <typename T, int RX>
+// Whether a window of width W at x0 - RX can be staged in 16-byte chunks.
+template <typename T, int W, int RX>
 __device__ __forceinline__ bool __ps_vec_ok(const __PSGridArg<T> &a, int x0) {
-  const long long start = (long long)(unsigned long long)a.p + (long long)(x0 - RX) * (long long)sizeof(T);
-  return (start & 15) == 0 && ((a.row * (long long)sizeof(T)) & 15) == 0;
+  const T *row0 = a.p + (x0 - RX);
+  return x0 - RX >= 0 && x0 - RX + W <= a.nx &&
+         ((unsigned long long)row0 & 15) == 0 && ((a.row * (long long)sizeof(T)) & 15) == 0;
 }
 )PSJIT";
 
@@ -608,8 +600,8 @@ std::string tiled_entry_source(const JitKernel &k) {
                               ", x0, y0, " + vj + ", ";
     s += "  " + T + " *s" + sj + " = reinterpret_cast<" + T + " *>(__ps_sm + " +
          std::to_string(st.off) + ");\n";
-    s += "  const bool " + vj + " = __ps_vec_ok<" + T + ", " + std::to_string(st.rxw) + ">(a" +
-         i + ", x0);\n";
+    s += "  const bool " + vj + " = __ps_vec_ok<" + T + ", " + std::to_string(W) + ", " +
+         std::to_string(st.rxw) + ">(a" + i + ", x0);\n";
     s += "  g" + i + ".staged = 1; g" + i + ".rx = " + std::to_string(st.rxw) + "; g" + i +
          ".ry = " + std::to_string(st.ry) + "; g" + i + ".rz = " + rz + "; g" + i + ".sw = " +
          std::to_string(W) + ";\n";
