@@ -165,13 +165,22 @@ def profiled_traffic():
 # CPU legs (the oracle is the checker and the CPU baseline only)
 # ---------------------------------------------------------------------------
 
+def host_threads():
+    """Host cores this process may use.  torchrun sets OMP_NUM_THREADS=1 for
+    its ranks; the CPU legs (rank 0 alone) take every core regardless."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
+
 def cpu_sweeps(seconds, nthreads=0, zslab=None):
     """Times oracle sweeps of the 512^3 workload on host cores until about
     `seconds` have elapsed.  With zslab, each sweep covers z in [0, zslab)
     of the full grid (a bounded sample).  Returns (glups, sweeps, threads)."""
     from oracle import pyoracle
     from physis_gb300 import synth
-    nt = nthreads if nthreads > 0 else pyoracle.num_threads()
+    nt = nthreads if nthreads > 0 else host_threads()
     f1 = synth.uniform((N, N, N), 1)
     f2 = np.zeros_like(f1)
     zs = zslab or N
@@ -194,7 +203,7 @@ def run_reference(args, dist):
         return
     from oracle import pyoracle
     from physis_gb300 import synth
-    nt = pyoracle.num_threads()
+    nt = host_threads()
     zs = 32  # each step: one sweep over z in [0,32) of the 512^3 field
     f1 = synth.uniform((N, N, N), 1)
     f2 = np.zeros_like(f1)
@@ -578,7 +587,7 @@ def run_gpu_himeno(args, dist):
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
         from oracle import pyoracle
-        nt = pyoracle.num_threads()
+        nt = host_threads()
         g = [a.copy() for a in arrays]
         zs = 64
         d = (1, nx - 1, 1, ny - 1, 1, zs + 1)
