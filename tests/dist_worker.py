@@ -19,7 +19,9 @@ def main():
     out = {"rank": d.rank, "max": mx, "sum": sm}
     d.barrier()
     d.close()
-    print(json.dumps(out), flush=True)
+    # one file per rank: the ranks share stdout, where lines can interleave
+    with open(os.path.join(sys.argv[1], "rank%d.json" % d.rank), "w") as f:
+        json.dump(out, f)
 
 
 if __name__ == "__main__":

@@ -30,11 +30,11 @@ def _json_lines(text):
     return [json.loads(l) for l in text.splitlines() if l.startswith("{")]
 
 
-def test_barrier_and_reductions_over_two_ranks():
-    r = _torchrun([os.path.join("tests", "dist_worker.py")])
+def test_barrier_and_reductions_over_two_ranks(tmp_path):
+    r = _torchrun([os.path.join("tests", "dist_worker.py"), str(tmp_path)])
     assert r.returncode == 0, r.stderr[-2000:]
-    lines = _json_lines(r.stdout)
-    assert sorted(l["rank"] for l in lines) == [0, 1]
+    lines = [json.load(open(tmp_path / ("rank%d.json" % k))) for k in (0, 1)]
+    assert [l["rank"] for l in lines] == [0, 1]
     for l in lines:
         assert l["max"] == 2.5 and l["sum"] == 30.0
 
