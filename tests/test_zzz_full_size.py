@@ -1,0 +1,151 @@
+"""Parity at the full benchmark sizes, through properties that do not depend
+on the size (the oracle would need minutes of CPU time there).
+
+* 7-point diffusion, 512^3 float, 1000 steps (the bench's headline run):
+  the sweep conserves the grid's sum up to the coefficients' float sum
+  (every cell's value leaves with total weight cc + cw + ce + ... because the
+  clamped faces reuse the centre and cw = ce, cn = cs, ct = cb); values stay
+  inside the initial range times that factor; the FP64 reduction equals a
+  host FP64 sum; temporal blocking (k = 2) gives the same bits as the plain
+  sweeps; contracted temporal passes stay within 1e-5 relative per cell.
+* Himeno 19-point, 257 x 257 x 513 float (the bench's set-up): the fused
+  residual never grows from sweep to sweep (damped Jacobi on this symmetric
+  system contracts the residual in the 2-norm); the fused sweep writes the
+  same bits as the plain sweep; the fused FP64 residual equals the residual
+  recomputed on the host in the REF expression order.
+This file runs last in the GPU suite (its name sorts last): it holds up to 2 GB
+of device memory for a few seconds.
+"""
+import numpy as np
+import pytest
+
+import physis_gb300 as ps
+from physis_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+COEF = (0.1, 0.1, 0.1, 0.1, 0.1, 0.1, 0.4)  # ce cw cn cs ct cb cc
+
+
+@pytest.fixture(scope="module")
+def rt():
+    ps.build()
+    ps.init()
+    yield ps
+    ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 1)
+    ps.set_fma(False)
+    ps.clear_error()
+
+
+def _bits(a):
+    return a.view(np.uint32)
+
+
+def test_diffusion_512_cubed_1000_steps(rt):
+    n, steps = 512, 1000
+    shape = (n, n, n)
+    init = synth.uniform(shape, 1)
+    g1, g2 = ps.Grid(shape), ps.Grid(shape)
+    dom = ps.full_domain(shape)
+    m1 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g1, g2], COEF)
+    m2 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g2, g1], COEF)
+
+    def run(k=1, fma=False, n_steps=steps):
+        ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, k, warps=8, rows=4, ns=3)
+        ps.set_fma(fma)
+        try:
+            g1.copyin(init)
+            g2.copyin(init)
+            ps.stencil_run([m1, m2], n_steps // 2)
+        finally:
+            ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 1)
+            ps.set_fma(False)
+        return g1.copyout()
+
+    plain = run()
+    growth = float(np.sum([np.float64(np.float32(c)) for c in COEF])) ** steps
+    sum0 = float(init.sum(dtype=np.float64))
+    host = float(plain.sum(dtype=np.float64))
+    dev = ps.reduce_f64(g1, ps.PS_SUM)
+    assert abs(dev - host) <= 1e-6 * abs(host)
+    # rounding drifts the sum by about -7.5e-6 over 1000 steps (measured with
+    # the oracle at 64^3 and 128^3, independent of the size); a face that
+    # lost its clamp would move it by ~2e-4 per step
+    assert abs(host / (sum0 * growth) - 1.0) < 3e-5
+    assert np.isfinite(plain).all()
+    assert plain.min() >= float(init.min()) * growth - 1e-4
+    assert plain.max() <= float(init.max()) * growth + 1e-4
+
+    temporal = run(k=2)
+    assert np.array_equal(_bits(temporal), _bits(plain))
+
+    # contraction changes each step's rounding; the difference grows by about
+    # 1.3e-8 relative per step (2.7e-6 after 200 steps in a numpy model at 64^3)
+    fused = run(k=2, fma=True, n_steps=200)
+    plain200 = run(n_steps=200)
+    assert np.allclose(fused, plain200, rtol=1e-5, atol=0)
+    g1.free()
+    g2.free()
+
+
+def _himeno_setup(nx, ny, nz):
+    import bench
+    return bench.himeno_arrays(nx, ny, nz)
+
+
+def _host_gosa(arrays):
+    """Sum of ss^2 (FP64 of float32 ss) of one sweep from arrays[0], the REF
+    expression order of himenobmtxpa_physis.c:331-361 with b = 0 (its three
+    b-terms add exact zeros)."""
+    p, a0, a1, a2, a3, c0, c1, c2, bnd, wrk1 = (arrays[0], arrays[2], arrays[3], arrays[4],
+                                                arrays[5], arrays[9], arrays[10], arrays[11],
+                                                arrays[12], arrays[13])
+    assert not arrays[6].any() and not arrays[7].any() and not arrays[8].any()
+    i = (slice(1, -1), slice(1, -1), slice(1, -1))
+    zp = (slice(2, None), slice(1, -1), slice(1, -1))
+    zm = (slice(None, -2), slice(1, -1), slice(1, -1))
+    yp = (slice(1, -1), slice(2, None), slice(1, -1))
+    ym = (slice(1, -1), slice(None, -2), slice(1, -1))
+    xp = (slice(1, -1), slice(1, -1), slice(2, None))
+    xm = (slice(1, -1), slice(1, -1), slice(None, -2))
+    s0 = a0[i] * p[zp]
+    s0 = s0 + a1[i] * p[yp]
+    s0 = s0 + a2[i] * p[xp]
+    s0 = s0 + c0[i] * p[zm]
+    s0 = s0 + c1[i] * p[ym]
+    s0 = s0 + c2[i] * p[xm]
+    s0 = s0 + wrk1[i]
+    ss = (s0 * a3[i] - p[i]) * bnd[i]
+    assert ss.dtype == np.float32
+    return float(np.square(ss.astype(np.float64)).sum())
+
+
+def test_himeno_257x257x513_residuals(rt):
+    nx, ny, nz = 257, 257, 513
+    shape = (nz, ny, nx)
+    arrays = _himeno_setup(nx, ny, nz)
+    gs = [ps.Grid(shape) for _ in range(14)]
+    for g, a in zip(gs, arrays):
+        g.copyin(a)
+    dom = ps.domain(1, nx - 1, 1, ny - 1, 1, nz - 1)
+    omega = np.float32(0.8)
+    host0 = _host_gosa(arrays)
+    order = [gs, [gs[1], gs[0]] + gs[2:]]
+    gosa = []
+    for s in range(12):
+        gosa.append(float(ps.reduce_kernel(ps.PS_SUM, ps.PS_KERNEL_HIMENO19_GOSA, dom,
+                                           order[s % 2], [omega])))
+    assert abs(gosa[0] - host0) <= 1e-5 * host0
+    for a, b in zip(gosa, gosa[1:]):
+        assert b <= a * (1 + 1e-5)
+    assert gosa[-1] < gosa[0]
+    fused = gs[0].copyout()  # 12 sweeps: the result is back in p0
+    # the same 12 sweeps with the plain kernel from the initial state
+    gs[0].copyin(arrays[0])
+    gs[1].copyin(arrays[1])
+    m1 = ps.stencil_map(ps.PS_KERNEL_HIMENO19, dom, gs, [omega])
+    m2 = ps.stencil_map(ps.PS_KERNEL_HIMENO19, dom, [gs[1], gs[0]] + gs[2:], [omega])
+    ps.stencil_run([m1, m2], 6)
+    assert np.array_equal(_bits(gs[0].copyout()), _bits(fused))
+    for g in gs:
+        g.free()
