@@ -81,3 +81,35 @@ def test_malformed_stencil_functions_are_rejected(built, src, name, why):
         pytest.skip("NVRTC not available: " + log)
     assert code == ps.PS_ERR_INVALID_ARGUMENT
     assert why in log, log
+
+
+@pytest.mark.parametrize("src,name,staged", [
+    # int and long grids, offsets up to 2
+    ("void i5(const int x, const int y, const int z, PSGrid3DInt a, PSGrid3DInt b) {\n"
+     "  PSGridEmit(b, PSGridGet(a, x + 2, y, z) + PSGridGet(a, x, y - 2, z) * 3);\n}\n",
+     "i5", "staged a 2 2 0 clamp;"),
+    ("void l3(const int x, const int y, const int z, PSGrid3DLong a, PSGrid3DLong b) {\n"
+     "  PSGridEmit(b, PSGridGet(a, x, y, z + 1) - PSGridGet(a, x, y, z - 1));\n}\n",
+     "l3", "staged a 0 0 1 clamp;"),
+    # reads through a macro: not literal in the function body, halo 1
+    ("#define NB(g, dx) PSGridGet(g, x + dx, y, z)\n"
+     "void m3(const int x, const int y, const int z, PSGrid3DFloat a, PSGrid3DFloat b) {\n"
+     "  PSGridEmit(b, NB(a, -1) + NB(a, 0) + NB(a, 1));\n}\n",
+     "m3", ""),
+    # different index names
+    ("void ijk(const int i, const int j, const int k, PSGrid3DDouble u, PSGrid3DDouble v,\n"
+     "         double c) {\n"
+     "  PSGridEmit(v, c * (PSGridGet(u, i + 1, j, k) + PSGridGet(u, i, j, k - 3)));\n}\n",
+     "ijk", "staged u 1 0 3 clamp;"),
+    # a grid read only at the centre is not staged; an emitted one never is
+    ("void c1(const int x, const int y, const int z, PSGrid3DFloat a, PSGrid3DFloat s,\n"
+     "        PSGrid3DFloat b) {\n"
+     "  PSGridEmit(b, PSGridGet(a, x - 1, y, z) * PSGridGet(s, x, y, z));\n}\n",
+     "c1", "staged a 1 0 0 clamp;"),
+])
+def test_staging_decisions_and_compiles(built, src, name, staged):
+    code, log = ps.stencil_function_check(src, name)
+    if code == ps.PS_ERR_UNSUPPORTED:
+        pytest.skip("NVRTC not available: " + log)
+    assert code == ps.PS_OK, log
+    assert log == staged
