@@ -1,21 +1,28 @@
-"""Parity at the full benchmark sizes, through properties that do not depend
-on the size (the oracle would need minutes of CPU time there).
+"""Parity at the full benchmark sizes.  The oracle runs a few steps there
+(seconds on the host cores); longer runs are checked through properties
+that do not depend on the size.
 
-* 7-point diffusion, 512^3 float, 1000 steps (the bench's headline run):
-  the sweep conserves the grid's sum up to the coefficients' float sum
-  (every cell's value leaves with total weight cc + cw + ce + ... because the
-  clamped faces reuse the centre and cw = ce, cn = cs, ct = cb); values stay
-  inside the initial range times that factor; the FP64 reduction equals a
-  host FP64 sum; temporal blocking (k = 2) gives the same bits as the plain
-  sweeps; contracted temporal passes stay within 1e-5 relative per cell.
-* Himeno 19-point, 257 x 257 x 513 float (the bench's set-up): the fused
-  residual never grows from sweep to sweep (damped Jacobi on this symmetric
-  system contracts the residual in the 2-norm); the fused sweep writes the
-  same bits as the plain sweep; the fused FP64 residual equals the residual
-  recomputed on the host in the REF expression order.
+* 7-point diffusion, 512^3 float (the bench's headline run):
+  * 20 steps: bit-identical to the oracle;
+  * 1000 steps: the sweep conserves the grid's sum up to the coefficients'
+    float sum (every cell's value leaves with total weight cc + cw + ce + ...,
+    because the clamped faces reuse the centre and cw = ce, cn = cs, ct = cb);
+    values stay inside the initial range times that factor; the FP64
+    reduction equals a host FP64 sum; temporal blocking (k = 2) gives the same
+    bits as the plain sweeps;
+  * contracted temporal passes stay within 1e-5 relative per cell over 200
+    steps.
+* Himeno 19-point, 257 x 257 x 513 float (the bench's set-up), 12 sweeps:
+  every fused residual equals the oracle's FP64 residual of the same sweep,
+  the pressure is bit-identical to the oracle's, and the plain sweep writes
+  the same bits as the fused one.  (In float32 this residual does not fall
+  monotonically at this size: the oracle's sequence rises at sweeps 2, 3, 7
+  and 9, by up to 1 %.)
 This file runs last in the GPU suite (its name sorts last): it holds up to 2 GB
 of device memory for a few seconds.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -41,7 +48,14 @@ def _bits(a):
     return a.view(np.uint32)
 
 
-def test_diffusion_512_cubed_1000_steps(rt):
+def _threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def test_diffusion_512_cubed(rt, oracle):
     n, steps = 512, 1000
     shape = (n, n, n)
     init = synth.uniform(shape, 1)
@@ -61,6 +75,14 @@ def test_diffusion_512_cubed_1000_steps(rt):
             ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 1)
             ps.set_fma(False)
         return g1.copyout()
+
+    # 20 steps against the oracle, bit for bit
+    short = run(n_steps=20)
+    r1, r2 = init.copy(), np.zeros_like(init)
+    oracle.run7(oracle.V_DIFFUSION7, r1, r2, (0, n, 0, n, 0, n), COEF, iter=10,
+                nthreads=_threads())
+    assert np.array_equal(_bits(short), _bits(r1))
+    del r1, r2, short
 
     plain = run()
     growth = float(np.sum([np.float64(np.float32(c)) for c in COEF])) ** steps
@@ -120,26 +142,29 @@ def _host_gosa(arrays):
     return float(np.square(ss.astype(np.float64)).sum())
 
 
-def test_himeno_257x257x513_residuals(rt):
+def test_himeno_257x257x513(rt, oracle):
     nx, ny, nz = 257, 257, 513
     shape = (nz, ny, nx)
     arrays = _himeno_setup(nx, ny, nz)
     gs = [ps.Grid(shape) for _ in range(14)]
     for g, a in zip(gs, arrays):
         g.copyin(a)
-    dom = ps.domain(1, nx - 1, 1, ny - 1, 1, nz - 1)
+    domt = (1, nx - 1, 1, ny - 1, 1, nz - 1)
+    dom = ps.domain(*domt)
     omega = np.float32(0.8)
     host0 = _host_gosa(arrays)
+    ref = [a.copy() for a in arrays]
     order = [gs, [gs[1], gs[0]] + gs[2:]]
-    gosa = []
     for s in range(12):
-        gosa.append(float(ps.reduce_kernel(ps.PS_SUM, ps.PS_KERNEL_HIMENO19_GOSA, dom,
-                                           order[s % 2], [omega])))
-    assert abs(gosa[0] - host0) <= 1e-5 * host0
-    for a, b in zip(gosa, gosa[1:]):
-        assert b <= a * (1 + 1e-5)
-    assert gosa[-1] < gosa[0]
+        gosa = float(ps.reduce_kernel(ps.PS_SUM, ps.PS_KERNEL_HIMENO19_GOSA, dom,
+                                      order[s % 2], [omega]))
+        _, g64 = oracle.himeno19(ref, domt, omega, nthreads=_threads())
+        ref[0], ref[1] = ref[1], ref[0]
+        if s == 0:
+            assert abs(g64 - host0) <= 1e-12 * host0
+        assert abs(gosa - g64) <= 1e-5 * g64, s
     fused = gs[0].copyout()  # 12 sweeps: the result is back in p0
+    assert np.array_equal(_bits(fused), _bits(ref[0]))
     # the same 12 sweeps with the plain kernel from the initial state
     gs[0].copyin(arrays[0])
     gs[1].copyin(arrays[1])
