@@ -1,7 +1,7 @@
 """CPU oracle of the learned warm start's arithmetic (numpy, FP64).
 
-TEST INFRASTRUCTURE ONLY: imported by tests/ and bench.py's checks, never by
-the product.  The learned warm start has no counterpart in the reference, so
+TEST INFRASTRUCTURE ONLY: imported by tests/ and by the smoke check in
+__graft_entry__.py as the checker, never by the product.  The learned warm start has no counterpart in the reference, so
 this oracle is pinned by its own consistency checks (the analytic gradients
 below against central finite differences, tests/test_nn_oracle.py) and the
 GPU kernels are checked against it.
