@@ -88,3 +88,33 @@ def test_temporal_output_tiles_cover_the_grid_once(k, tye, nx, ny, nz):
     seen = written_cells((0, nx, 0, ny, 0, nz), 30 * vec, tyo, 0, 304, 2 * k - 1)
     assert len(seen) == nx * ny * nz
     assert all(v == 1 for v in seen.values())
+
+
+def test_batch_family_tables():
+    # runtime.cpp batch_build: problems ordered by kernel family, each
+    # family's item_begin counted from 0; batch.cu finds an item's problem by
+    # binary search over item_begin (the last problem whose first item is <=
+    # the item).  Every item of every problem is found exactly once.
+    import random
+    rnd = random.Random(3)
+    kinds = [rnd.choice(["d7", "him"]) for _ in range(48)]
+    items = [rnd.randint(1, 40) for _ in range(48)]
+    for fam in ("d7", "him"):
+        probs = [r for r in range(48) if kinds[r] == fam]
+        begin, total = [], 0
+        for r in probs:
+            begin.append(total)
+            total += items[r]
+        found = []
+        for item in range(total):
+            lo, hi = 0, len(probs) - 1
+            while lo < hi:
+                mid = (lo + hi + 1) >> 1
+                if begin[mid] <= item:
+                    lo = mid
+                else:
+                    hi = mid - 1
+            local = item - begin[lo]
+            assert 0 <= local < items[probs[lo]]
+            found.append((probs[lo], local))
+        assert sorted(found) == sorted((r, i) for r in probs for i in range(items[r]))
