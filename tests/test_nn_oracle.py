@@ -143,3 +143,16 @@ def test_unmirror_inverts_mirror():
     a = np.arange(4 * 5 * 5).reshape(4, 5, 5)
     for flip in range(16):
         assert np.array_equal(nn.unmirror(nn.mirror(a, flip), flip), a), flip
+
+
+def test_mirror_image_lists():
+    # the warm start's host helpers: a square x-y section has 16 mirror
+    # images (8 axis mirrors, then the same with x and y swapped), any other
+    # shape 8; coarse grids round up
+    from physis_gb300 import warmstart as ws
+    assert ws.mirror_images((257, 129, 129), 16) == list(range(16))
+    assert ws.mirror_images((65, 33, 31), 16) == list(range(8))
+    assert ws.mirror_images((65, 33, 33), 1) == [0]
+    assert ws.mirror_images((65, 33, 33), 0) == [0]
+    assert ws.coarse_shape((257, 129, 129), 16) == (17, 9, 9)
+    assert ws.coarse_shape((65, 33, 33), 4) == (17, 9, 9)
