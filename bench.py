@@ -20,8 +20,20 @@ Printed JSON line (one, rank 0):
   cpu_baseline  the CPU restatement of the REF target (oracle/) on the host
              cores, OpenMP over z, on a bounded sample of the same workload.
 
+Further keys of the same line (leave them out with --no-extras), each with
+its own CUDA-event timing, roofline and CPU baseline:
+  himeno     config 3: 19-point Himeno Jacobi at 257x257x513 with the fused
+             residual, max(K, 50) sweeps, 56 algorithmic bytes per interior
+             cell update;
+  batch      config 4: 48 uneven grids (half diffusion, half Himeno), 200
+             steps each, batched against 48 separate runs;
+  config1    64^3 x 100 steps + PSReduce sum (the REF program's
+             configuration), device and end to end;
+  reduce     PSReduce over a 512^3 float grid, GB/s.
+
 --impl reference times only the CPU implementation (the reference's REF
-target restated in C, all host threads) on the same metric.
+target restated in C, all host threads) on the same metric: each step one
+sweep of the whole 512^3 field.
 Multi-GPU (torchrun): independent replicas, one per GPU (the path has no
 data exchange); value is the sum over ranks.
 """
@@ -82,7 +94,11 @@ class Dist:
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """nvidia-smi clock / throttle sampling around the timed region.
+
+    start() returns once the first sample has arrived, and stop() waits for
+    one sample taken after it was called, so even a timed region shorter
+    than the 100 ms sampling period is bracketed by samples under load."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -93,7 +109,7 @@ class ClockSampler:
         self.proc = None
         self.lines = []
 
-    def start(self):
+    def start(self, wait=3.0):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
@@ -103,14 +119,22 @@ class ClockSampler:
             self.t.start()
         except OSError:
             self.proc = None
+            return
+        t0 = time.perf_counter()
+        while not self.lines and time.perf_counter() - t0 < wait:
+            time.sleep(0.005)
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
-    def stop(self):
+    def stop(self, wait=1.0):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi"]}
+        t_stop = time.perf_counter()
+        while (not self.lines or self.lines[-1][0] < t_stop) and \
+                time.perf_counter() - t_stop < wait:
+            time.sleep(0.005)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -120,7 +144,7 @@ class ClockSampler:
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
                  "sw_power_cap"]
-        for line in self.lines:
+        for _, line in self.lines:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -134,7 +158,8 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm),
+                "window": "from before the warm-up to the first sample after the timed region"}
 
 
 def measured_peaks():
@@ -204,10 +229,9 @@ def run_reference(args, dist):
     from oracle import pyoracle
     from physis_gb300 import synth
     nt = host_threads()
-    zs = 32  # each step: one sweep over z in [0,32) of the 512^3 field
     f1 = synth.uniform((N, N, N), 1)
     f2 = np.zeros_like(f1)
-    dom = (0, N, 0, N, 0, zs)
+    dom = (0, N, 0, N, 0, N)
     for _ in range(args.warmup):
         pyoracle.sweep7(pyoracle.V_DIFFUSION7, f1, f2, dom, COEF, nthreads=nt)
         f1, f2 = f2, f1
@@ -216,9 +240,9 @@ def run_reference(args, dist):
         pyoracle.sweep7(pyoracle.V_DIFFUSION7, f1, f2, dom, COEF, nthreads=nt)
         f1, f2 = f2, f1
     el = time.perf_counter() - t0
-    value = N * N * zs * args.steps / el / 1e9
-    sample = (f"one step = one REF-order sweep of z-slab [0,{zs}) of the 512^3 "
-              f"field ({N * N * zs} cells), OpenMP over z")
+    value = float(N) ** 3 * args.steps / el / 1e9
+    sample = (f"one step = one REF-order sweep of the whole {N}^3 field "
+              f"({N ** 3} cells), OpenMP over z")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "GLUPS",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -446,6 +470,18 @@ def run_gpu(args, dist):
         ref_cuda = reference_cuda_kernels(ps, g1, g2, min(K, 200))
     shape_used = ps.get_launch_shape(ps.PS_KERNEL_DIFFUSION7)
 
+    # the other headline configurations, each with its own CUDA-event timing,
+    # roofline and CPU baseline (config 3, config 4, config 1, PSReduce)
+    extras = {}
+    if not args.no_extras:
+        with_cpu = dist.rank == 0 and not args.no_cpu_baseline
+        hk = max(K, 50) + (max(K, 50) % 2)
+        extras["himeno"] = himeno_measure(ps, dist, hk, W, args.cpu_seconds / 2, with_cpu)
+        extras["batch"] = batch_measure(ps, dist, 200, False, args.cpu_seconds / 2, with_cpu)
+        if dist.rank == 0:
+            extras["config1"] = config1_measure(ps)
+            extras["reduce"] = reduce_measure(ps, cpu=with_cpu)
+
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
         glups, sweeps, nt = cpu_sweeps(args.cpu_seconds)
@@ -487,9 +523,158 @@ def run_gpu(args, dist):
             "reference_cuda_kernels": ref_cuda,
             "temporal_blocking": temporal,
         }
+        line.update(extras)
         print(json.dumps(line), flush=True)
     g1.free()
     g2.free()
+
+
+# ---------------------------------------------------------------------------
+# Config 1 (64^3 x 100 steps + PSReduce) and the grid form of PSReduce
+# ---------------------------------------------------------------------------
+
+def config1_measure(ps, reps=20):
+    """64^3 clamped diffusion, seed 0, 100 steps (50 iterations of the two
+    maps) and a PSReduce sum of the final grid, as the reference's REF
+    program runs it.  Device: CUDA events around the 100 steps.  e2e: the
+    whole job through the public API with pinned host buffers
+    (PSGridCopyin + PSStencilRun + PSReduce + PSGridCopyout), wall clock,
+    best of `reps`.  CPU: the REF port, sequential like the REF target."""
+    import ctypes
+    from oracle import pyoracle
+    from physis_gb300 import synth
+    L = ps.lib()
+    n, steps = 64, 100
+    shape = (n, n, n)
+    init = synth.uniform(shape, 0)
+    g1, g2 = ps.Grid(shape), ps.Grid(shape)
+    dom = ps.full_domain(shape)
+    m1 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g1, g2], COEF)
+    m2 = ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g2, g1], COEF)
+    nbytes = init.nbytes
+    hin, hout = L.PSHostAlloc(nbytes), L.PSHostAlloc(nbytes)
+    ctypes.memmove(hin, init.ctypes.data, nbytes)
+    total = np.zeros(1, np.float32)
+    dev_ms, job_s = [], []
+    for r in range(reps + 3):
+        L.PSGridCopyin(g1.handle, hin)
+        ps.synchronize()
+        L.PSEventRecord(0)
+        ps.stencil_run([m1, m2], steps // 2)
+        L.PSEventRecord(1)
+        ps.synchronize()
+        t0 = time.perf_counter()
+        L.PSGridCopyin(g1.handle, hin)
+        ps.stencil_run([m1, m2], steps // 2)
+        L.PSReduceGridV(total.ctypes.data_as(ctypes.c_void_p), ps.PS_SUM, g1.handle)
+        L.PSGridCopyout(g1.handle, hout)
+        el = time.perf_counter() - t0
+        if r >= 3:
+            dev_ms.append(L.PSEventElapsedMs(0, 1))
+            job_s.append(el)
+    ps.check()
+    got = np.empty_like(init)
+    ctypes.memmove(got.ctypes.data, hout, nbytes)
+    L.PSHostFree(hin)
+    L.PSHostFree(hout)
+    g1.free()
+    g2.free()
+    # the oracle: bit-exact grid, FP64 sum; then its time, sequential
+    r1, r2 = init.copy(), np.zeros_like(init)
+    t0 = time.perf_counter()
+    pyoracle.run7(pyoracle.V_DIFFUSION7, r1, r2, (0, n, 0, n, 0, n), COEF, iter=steps // 2)
+    ref_sum = pyoracle.reduce_ref(r1, pyoracle.PS_SUM)
+    cpu_s = time.perf_counter() - t0
+    exact = pyoracle.reduce_fp64(r1, pyoracle.PS_SUM)
+    cells = float(n) ** 3
+    dms = float(np.median(dev_ms))
+    js = float(min(job_s))
+    return {
+        "workload": "7-point fp32 diffusion 64^3, seed 0, 100 steps + PSReduce sum "
+                    "(the reference REF program's configuration)",
+        "value": cells * steps / (dms / 1e3) / 1e9, "unit": "GLUPS",
+        "us_per_step": dms / steps * 1e3,
+        "steps": steps, "reps": reps,
+        "e2e": {"value": cells * steps / js / 1e9, "unit": "GLUPS", "job_us": js * 1e6,
+                "h2d_bytes_per_step": nbytes / steps, "d2h_bytes_per_step": (nbytes + 4) / steps,
+                "what": "PSGridCopyin(pinned) + PSStencilRun(50 x 2 maps) + PSReduce + "
+                        "PSGridCopyout(pinned), wall clock, best of reps"},
+        "bit_exact_vs_oracle": bool(np.array_equal(got.view(np.uint32), r1.view(np.uint32))),
+        "reduce": {"value": float(total[0]), "fp64_oracle": exact,
+                   "rel_err": abs(float(total[0]) - exact) / abs(exact),
+                   "ref_fold": float(ref_sum)},
+        "roofline": {"bound": "launch/latency",
+                     "what": "1 MiB grids stay in L2; 100 dependent sweeps of 262,144 cells"},
+        "cpu_baseline": {"value": cells * steps / cpu_s / 1e9, "unit": "GLUPS", "cores": 1,
+                         "kind": "port",
+                         "sample": "the whole job (100 REF-order sweeps + REF PSReduce fold), "
+                                   "sequential as the REF target runs it"},
+    }
+
+
+def reduce_measure(ps, reps=20, cpu=True):
+    """PSReduce (grid form, PS_SUM) over a 512^3 float grid.  Device: the
+    reduction kernel launched `reps` times back to back on the runtime
+    stream (through PSReduceNoAlloc, which launches the same kernel with the
+    same CTA count) between CUDA events: 4 algorithmic bytes per element.
+    Call: wall clock of PSReduce itself (launch, 8-byte readback,
+    synchronisation).  CPU: the REF fold (sequential, as the REF target)."""
+    import ctypes
+    from physis_gb300 import synth
+    L = ps.lib()
+    n = 512
+    shape = (n, n, n)
+    init = synth.uniform(shape, 3)
+    g = ps.Grid(shape)
+    g.copyin(init)
+    slot = ps.Grid((1,), np.float64)
+    stream = L.PSGetStream()
+    for _ in range(3):
+        L.PSReduceNoAlloc(g.dev_ptr, g.pitch, n, n, n, ps.PS_FLOAT, ps.PS_SUM, slot.dev_ptr,
+                          stream)
+    ps.synchronize()
+    n0 = ps.launch_count()
+    L.PSEventRecord(0)
+    for _ in range(reps):
+        L.PSReduceNoAlloc(g.dev_ptr, g.pitch, n, n, n, ps.PS_FLOAT, ps.PS_SUM, slot.dev_ptr,
+                          stream)
+    L.PSEventRecord(1)
+    ps.synchronize()
+    ms = L.PSEventElapsedMs(0, 1) / reps
+    out = np.zeros(1, np.float32)
+    calls = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        L.PSReduceGridV(out.ctypes.data_as(ctypes.c_void_p), ps.PS_SUM, g.handle)
+        calls.append(time.perf_counter() - t0)
+    ps.check()
+    v64 = ps.reduce_f64(g, ps.PS_SUM)
+    exact = float(init.astype(np.float64).sum())
+    g.free()
+    slot.free()
+    peak, peak_kind = measured_peaks()
+    nbytes = float(n) ** 3 * 4
+    res = {
+        "workload": "PSReduce PS_SUM over a 512^3 float grid (uniform[0,1), seed 3)",
+        "value": nbytes / (ms / 1e3) / 1e9, "unit": "GB/s", "us_per_reduction": ms * 1e3,
+        "call_us_median": float(np.median(calls)) * 1e6,
+        "rel_err_vs_fp64": abs(v64 - exact) / exact,
+        "roofline": {"bound": "hbm", "achieved": nbytes / (ms / 1e3) / 1e9, "peak": peak,
+                     "unit": "GB/s", "frac": nbytes / (ms / 1e3) / 1e9 / peak,
+                     "traffic": None, "peak_source": peak_kind, "bytes_per_element": 4},
+        "l2": "512 MiB grid > L2",
+        "cpu_baseline": None,
+    }
+    if cpu:
+        from oracle import pyoracle
+        t0 = time.perf_counter()
+        pyoracle.reduce_ref(init, pyoracle.PS_SUM)
+        el = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": nbytes / el / 1e9, "unit": "GB/s", "cores": 1,
+                               "kind": "port",
+                               "sample": "one REF PSReduce fold of the whole grid "
+                                         "(sequential, as the REF target)"}
+    return res
 
 
 # ---------------------------------------------------------------------------
@@ -518,10 +703,10 @@ def himeno_arrays(nx, ny, nz):
             zero, zero, zero, one, one, one, bnd, zero]
 
 
-def run_gpu_himeno(args, dist):
-    os.environ.setdefault("PS_DEVICE", str(dist.local))
-    import physis_gb300 as ps
-    ps.init()
+def himeno_measure(ps, dist, K, W, cpu_seconds, with_cpu):
+    """Config 3: K fused-residual sweeps of the 257x257x513 Himeno set-up
+    with resident grids (CUDA events on the runtime stream), one e2e job,
+    and the REF port on host cores.  Returns the JSON object."""
     L = ps.lib()
     nx, ny, nz = HIM
     shape = (nz, ny, nx)
@@ -534,7 +719,6 @@ def run_gpu_himeno(args, dist):
     k = ps.PS_KERNEL_HIMENO19_GOSA
     m1 = ps.stencil_map(k, dom, gs, [omega])
     m2 = ps.stencil_map(k, dom, [gs[1], gs[0]] + gs[2:], [omega])
-    K, W = args.steps, args.warmup
 
     def sweeps(n):
         pairs, rem = divmod(n, 2)
@@ -585,7 +769,7 @@ def run_gpu_himeno(args, dist):
     peak, peak_kind = measured_peaks()
     achieved = lups * HIM_BYTES_PER_LUP / (ms / K / 1e3) / 1e9
     cpu = None
-    if dist.rank == 0 and not args.no_cpu_baseline:
+    if dist.rank == 0 and with_cpu:
         from oracle import pyoracle
         nt = host_threads()
         g = [a.copy() for a in arrays]
@@ -594,45 +778,54 @@ def run_gpu_himeno(args, dist):
         pyoracle.himeno19(g, d, omega, nthreads=nt)
         t0 = time.perf_counter()
         n = 0
-        while time.perf_counter() - t0 < args.cpu_seconds:
+        while time.perf_counter() - t0 < cpu_seconds:
             pyoracle.himeno19(g, d, omega, nthreads=nt)
             g[0], g[1] = g[1], g[0]
             n += 1
         el = time.perf_counter() - t0
         cpu = {"value": (nx - 2) * (ny - 2) * zs * n / el / 1e9, "unit": "GLUPS",
                "cores": nt, "kind": "port",
-               "sample": f"{n} REF-order sweeps of z in [1,{zs + 1}) "
+               "sample": f"{n} REF-order sweeps (with the residual) of z in [1,{zs + 1}) "
                          f"(oracle/ps_oracle.c, OpenMP over z)"}
-    if dist.rank == 0:
-        shape_used = ps.get_launch_shape(k)
-        line = {
-            "metric": HIM_METRIC, "value": value, "unit": "GLUPS",
-            "n_gpus": dist.ws, "steps": K, "warmup": W,
-            "ms_per_step": ms_max / K, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "Himeno benchmark set-up (deterministic), omega 0.8",
-            "config": {"workload": "Himeno 19-point Jacobi 257x257x513, interior "
-                                   "255x255x511, residual fused per sweep",
-                       "grid": [nx, ny, nz], "l2": "14 grids of 139 MB, > L2",
-                       "launch_shape": {"warps": shape_used[0], "ns": shape_used[2],
-                                        "ns2": shape_used[3]},
-                       "e2e_job": "PSGridCopyin(p) + K PSReduce kernel-form sweeps "
-                                  "(residual to host each) + PSGridCopyout(p)"},
-            "e2e": {"value": dist.ws * lups * K / e2e_max / 1e9, "unit": "GLUPS",
-                    "h2d_bytes_per_step": nbytes / K,
-                    "d2h_bytes_per_step": nbytes / K + 4,
-                    "job_seconds": e2e_max, "last_gosa": float(gosa)},
-            "gpu_launches": int(launches),
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                         "peak_source": peak_kind,
-                         "bytes_per_lup": HIM_BYTES_PER_LUP},
-            "clocks": clk,
-            "cpu_baseline": cpu,
-        }
-        print(json.dumps(line), flush=True)
+    shape_used = ps.get_launch_shape(k)
+    out = {
+        "metric": HIM_METRIC, "value": value, "unit": "GLUPS",
+        "n_gpus": dist.ws, "steps": K, "warmup": W,
+        "ms_per_step": ms_max / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "Himeno benchmark set-up (deterministic), omega 0.8",
+        "config": {"workload": "Himeno 19-point Jacobi 257x257x513, interior "
+                               "255x255x511, residual fused per sweep",
+                   "grid": [nx, ny, nz], "l2": "14 grids of 139 MB, > L2",
+                   "launch_shape": {"warps": shape_used[0], "ns": shape_used[2],
+                                    "ns2": shape_used[3]},
+                   "e2e_job": "PSGridCopyin(p) + K PSReduce kernel-form sweeps "
+                              "(residual to host each) + PSGridCopyout(p)"},
+        "e2e": {"value": dist.ws * lups * K / e2e_max / 1e9, "unit": "GLUPS",
+                "h2d_bytes_per_step": nbytes / K,
+                "d2h_bytes_per_step": nbytes / K + 4,
+                "job_seconds": e2e_max, "last_gosa": float(gosa)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": peak_kind,
+                     "bytes_per_lup": HIM_BYTES_PER_LUP},
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
     for g in gs:
         g.free()
+    return out
+
+
+def run_gpu_himeno(args, dist):
+    os.environ.setdefault("PS_DEVICE", str(dist.local))
+    import physis_gb300 as ps
+    ps.init()
+    out = himeno_measure(ps, dist, args.steps, args.warmup, args.cpu_seconds,
+                         not args.no_cpu_baseline)
+    if dist.rank == 0:
+        print(json.dumps(out), flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -653,19 +846,20 @@ def batch_dims(seed=2, n=48, xy=(32, 320), z=(32, 512)):
     return dims
 
 
-def run_gpu_batch(args, dist):
-    os.environ.setdefault("PS_DEVICE", str(dist.local))
-    import physis_gb300 as ps
+def batch_measure(ps, dist, steps_per_problem, small, cpu_seconds, with_cpu):
+    """Config 4: 48 uneven grids (24 diffusion, 24 Himeno) batched against
+    the same work as 48 separate runs, both with resident grids, one e2e
+    job, and the REF port on host cores over a bounded sample.  Returns the
+    JSON object."""
     from physis_gb300 import synth
-    ps.init()
     L = ps.lib()
-    if args.batch_small:
+    if small:
         dims = batch_dims(xy=(16, 64), z=(16, 64))
         label = "48 small grids, X,Y,Z in [16,64] (multiples of 8)"
     else:
         dims = batch_dims()
         label = "48 grids, X,Y in [32,320], Z in [32,512] (multiples of 8)"
-    runs, grids, inputs = [], [], []
+    runs, grids, inputs, host = [], [], [], []
     lups = 0.0
     algo_bytes = 0.0
     for i, (nx, ny, nz) in enumerate(dims):
@@ -679,6 +873,7 @@ def run_gpu_batch(args, dist):
                          ps.stencil_map(ps.PS_KERNEL_DIFFUSION7, dom, [g2, g1], COEF)])
             grids.append([g1, g2])
             inputs.append([(g1, init)])
+            host.append(("diffusion", init))
             lups += float(nx) * ny * nz
             algo_bytes += 8.0 * nx * ny * nz
         else:  # Himeno 19-point, config-3 coefficients, p uniform
@@ -694,11 +889,11 @@ def run_gpu_batch(args, dist):
                                         [gs[1], gs[0]] + gs[2:], [0.8])])
             grids.append(gs)
             inputs.append([(gs[0], init), (gs[1], init)])
+            host.append(("himeno", arrays))
             n_in = float(nx - 2) * (ny - 2) * (nz - 2)
             lups += n_in
             algo_bytes += 56.0 * n_in
-    K = args.steps  # time steps per problem (even)
-    it = max(1, K // 2)
+    it = max(1, steps_per_problem // 2)
     b = ps.batch_create(runs)
     ps.batch_run(b, 2)  # warm-up (also builds the graph cache on longer runs)
     ps.synchronize()
@@ -740,33 +935,73 @@ def run_gpu_batch(args, dist):
         L.PSGridCopyoutAsync(g.handle, h)
     ps.synchronize()
     e2e_s = time.perf_counter() - t0
+    ps.check()
     nbytes = sum(n for _, _, n in pinned)
     for _, h, _ in pinned:
         L.PSHostFree(h)
+    cpu = None
+    if with_cpu and dist.rank == 0:
+        # REF-order sweeps of the problems in batch order, one sweep each,
+        # until the time budget is used (a bounded sample of the workload)
+        from oracle import pyoracle
+        nt = host_threads()
+        done_lups, t0 = 0.0, time.perf_counter()
+        n_sw = 0
+        while time.perf_counter() - t0 < cpu_seconds:
+            kind, a = host[n_sw % len(host)]
+            if kind == "diffusion":
+                nz, ny, nx = a.shape
+                pyoracle.sweep7(pyoracle.V_DIFFUSION7, a, np.empty_like(a),
+                                (0, nx, 0, ny, 0, nz), COEF, nthreads=nt)
+                done_lups += float(a.size)
+            else:
+                nz, ny, nx = a[0].shape
+                g = [x.copy() if j < 2 else x for j, x in enumerate(a)]
+                pyoracle.himeno19(g, (1, nx - 1, 1, ny - 1, 1, nz - 1), np.float32(0.8),
+                                  nthreads=nt)
+                done_lups += float(nx - 2) * (ny - 2) * (nz - 2)
+            n_sw += 1
+        el = time.perf_counter() - t0
+        cpu = {"value": done_lups / el / 1e9, "unit": "GLUPS", "cores": nt, "kind": "port",
+               "sample": f"{n_sw} REF-order sweeps, one per problem in batch order "
+                         f"(oracle/ps_oracle.c, OpenMP over z)"}
     peak, peak_kind = measured_peaks()
     achieved = algo_bytes * steps / (ms_batch / 1e3) / 1e9
-    line = {
+    out = {
         "metric": "GLUPS, 48 uneven fp32 grids (24 x 7-point diffusion, 24 x Himeno "
-                  "19-point) in one persistent launch per kernel family per step",
+                  "19-point) batched",
         "value": value, "unit": "GLUPS", "n_gpus": 1, "steps": steps, "warmup": 4,
         "ms_per_step": ms_batch / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic uniform[0,1) fields, dims from SplitMix64 seed 2",
         "config": {"workload": label,
                    "cells": lups, "separate_runs_glups": lups * steps / (ms_sep / 1e3) / 1e9,
-                   "batch_over_separate": ms_sep / ms_batch},
+                   "batch_over_separate": ms_sep / ms_batch,
+                   "l2": "inputs larger than L2 (about 13 GB of grids)" if not small
+                         else "fits L2"},
         "e2e": {"value": lups * steps / e2e_s / 1e9, "unit": "GLUPS",
                 "h2d_bytes_per_step": nbytes / steps, "d2h_bytes_per_step": nbytes / steps},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "peak_source": peak_kind},
         "clocks": clk,
+        "cpu_baseline": cpu,
     }
-    print(json.dumps(line), flush=True)
     ps.batch_free(b)
     for gs in grids:
         for g in gs:
             g.free()
+    return out
+
+
+def run_gpu_batch(args, dist):
+    os.environ.setdefault("PS_DEVICE", str(dist.local))
+    import physis_gb300 as ps
+    ps.init()
+    out = batch_measure(ps, dist, args.steps, args.batch_small, args.cpu_seconds,
+                        not args.no_cpu_baseline)
+    if dist.rank == 0:
+        print(json.dumps(out), flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -1081,6 +1316,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="diffusion: leave out the himeno/batch/config1/reduce keys")
     ap.add_argument("--warps", type=int, default=0)
     ap.add_argument("--rows", type=int, default=0)
     ap.add_argument("--ns", type=int, default=0)

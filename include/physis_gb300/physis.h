@@ -158,6 +158,35 @@ void PSGridFree(void *g);
 /* include/physis/physis_user.h:93 */
 PSIndex PSGridDim(void *g, int d);
 
+/* include/physis/physis_user.h:81 (PSGridSet(g, x[, y[, z]], v)) and the
+ * target entry it becomes, __PSGridSet(g, &v, x, ...)
+ * (include/physis/physis_cuda.h:137, runtime/libphysis_rt_cuda.cc:162-177):
+ * writes one element from the host.  __PSGridSet takes as many PSIndex
+ * arguments as the grid has dimensions and `buf` pointing at one element of
+ * the grid's type.  The PSGridSet macro converts v to the grid's element
+ * type as a C assignment would.  Indices are bounds-checked (the reference
+ * does not check).  The element lands after every run already issued and
+ * the call returns once it is on the GPU, like the reference's blocking
+ * cudaMemcpy. */
+void __PSGridSet(void *g, const void *buf, ...);
+void __PSGridSetScalar(void *g, int nidx, PSIndex i, PSIndex j, PSIndex k, int is_float,
+                       double vf, long long vi);
+#define PS__NARG(...) PS__NARG_(__VA_ARGS__, 4, 3, 2, 1, 0)
+#define PS__NARG_(a, b, c, d, n, ...) n
+#define PS__CAT(a, b) PS__CAT_(a, b)
+#define PS__CAT_(a, b) a##b
+/* 1 when v has a floating type: (v*0 + 1)/2 is 0 in integer arithmetic and
+ * 0.5 (NaN for an infinite or NaN v) in floating arithmetic. */
+#define PS__IS_FLOAT(v) ((((v) * 0 + 1) / 2) != 0)
+#define PS__SETV(v) PS__IS_FLOAT(v), (PS__IS_FLOAT(v) ? (double)(v) : 0.0), \
+                    (PS__IS_FLOAT(v) ? 0LL : (long long)(v))
+#define PS__GRIDSET2(g, i, v) __PSGridSetScalar((g), 1, (PSIndex)(i), 0, 0, PS__SETV(v))
+#define PS__GRIDSET3(g, i, j, v) __PSGridSetScalar((g), 2, (PSIndex)(i), (PSIndex)(j), 0, \
+                                                   PS__SETV(v))
+#define PS__GRIDSET4(g, i, j, k, v) __PSGridSetScalar((g), 3, (PSIndex)(i), (PSIndex)(j), \
+                                                      (PSIndex)(k), PS__SETV(v))
+#define PSGridSet(g, ...) PS__CAT(PS__GRIDSET, PS__NARG(__VA_ARGS__))(g, __VA_ARGS__)
+
 /* include/physis/physis_common.h:105-111 (libphysis_rt_ref.cc:91-109). */
 PSDomain1D PSDomain1DNew(PSIndex minx, PSIndex maxx);
 PSDomain2D PSDomain2DNew(PSIndex minx, PSIndex maxx, PSIndex miny, PSIndex maxy);

@@ -39,6 +39,11 @@ void PSInitV(int trace);
  * for i >= ndims are ignored.  Returns NULL on failure. */
 void *PSGridNewV(int type, int ndims, const PSIndex *dims);
 
+/* __PSGridSet(g, value, idx[0], ..., idx[rank-1]) with a status: value
+ * points at one element of the grid's type.  Returns PS_OK or the error
+ * code (an index outside the grid is PS_ERR_INVALID_ARGUMENT). */
+int PSGridSetV(void *g, const PSIndex *idx, const void *value);
+
 /* __PSStencilMap(kernel, *dom, grids[0..ngrids), scalars[0..nscalars)). */
 PSStencil PSStencilMapV(int kernel, const PSDomain3D *dom, int ngrids,
                         void *const *grids, int nscalars,
@@ -197,11 +202,12 @@ void PSSetBatchShape(int warps, int rows, int ns7, int nsp, int nsc);
 
 /* No counterpart in the reference.  PSReduce over a grid that the caller
  * holds in device memory, for callers that must not allocate GPU memory:
- * code recording a CUDA graph or stream capture (an allocation cannot be
- * captured and would synchronise the device), latency-bound loops that
- * cannot afford the synchronisation an allocation implies, and processes
- * whose device memory is already owned by another allocator.  It needs no
- * PSInit and calls no cudaMalloc, cudaFree or allocating library routine.
+ * latency-bound loops that cannot afford the device-wide synchronisation a
+ * cudaMalloc/cudaFree implies, and processes whose device memory is already
+ * owned by another allocator (a framework's caching pool that has reserved
+ * the free memory), where a further cudaMalloc fails or fragments it.  It
+ * needs no PSInit and calls no cudaMalloc, cudaFree or allocating library
+ * routine.
  *
  * data   : element (x,y,z) at data + (z*ny + y)*pitch + x*esz; 16-byte
  *          aligned, pitch a multiple of 16 bytes (grids of this library
@@ -212,13 +218,18 @@ void PSSetBatchShape(int warps, int rows, int ns7, int nsp, int nsc);
  *          the 32-bit wrapped result, long grids as is);
  * stream : a cudaStream_t (NULL: the legacy default stream).  The call is
  *          asynchronous on that stream.
- * Scratch: a static device array of 2048 per-CTA partials plus a ticket,
- * held by every GPU that loads the library until exit.  A launch that
- * would need more partial slots than that is rejected (PS_ERR_UNSUPPORTED;
- * a 152-SM GB300 needs at most 1216).  All calls share the array: calls
- * whose work overlaps on the GPU race.  The first call on a device looks up
- * the array's device address (cudaGetSymbolAddress) and loads the module
- * there; make that first call before any stream capture.
+ * Scratch: a static device array of 2048 per-CTA partials plus a ticket
+ * (16 KiB), held by every GPU that loads the library until exit.  A launch
+ * that would need more partial slots than that is rejected
+ * (PS_ERR_UNSUPPORTED; a 152-SM GB300 needs at most 1216).  All calls share
+ * the array and it keeps the last call's contents (the ticket is cleared on
+ * the stream before each launch): calls whose work overlaps on the GPU race.
+ * Set-up: the first call on a device (and the first after the device's
+ * context was destroyed, e.g. by cudaDeviceReset) looks up the array's
+ * device address with cudaGetSymbolAddress, which loads the module into the
+ * current context; make that call before any stream capture.  Set-up from
+ * several host threads at once is serialised by a lock; after it, calls
+ * take no lock.
  * Returns PS_OK or an error code (also recorded for PSGetLastError). */
 int PSReduceNoAlloc(const void *data, size_t pitch, int nx, int ny, int nz, int type,
                     int op, void *result, void *stream);

@@ -45,7 +45,7 @@ EXPORTED = """PSInit PSFinalize PSPrintInternalInfo
 PSGrid1DFloatNew PSGrid1DDoubleNew PSGrid1DIntNew PSGrid1DLongNew
 PSGrid2DFloatNew PSGrid2DDoubleNew PSGrid2DIntNew PSGrid2DLongNew
 PSGrid3DFloatNew PSGrid3DDoubleNew PSGrid3DIntNew PSGrid3DLongNew
-PSGridCopyin PSGridCopyout PSGridFree PSGridDim
+PSGridCopyin PSGridCopyout PSGridFree PSGridDim __PSGridSet __PSGridSetScalar PSGridSetV
 PSDomain1DNew PSDomain2DNew PSDomain3DNew __PSStencilMap PSStencilRun PSReduce
 PSInitV PSGridNewV PSStencilMapV PSStencilRunV PSReduceGridV PSReduceKernelV
 PSReduceGridF64 PSGetLastError PSGetLastErrorString PSGetErrorName PSClearError
@@ -123,6 +123,8 @@ def lib():
     L.PSGridFree.argtypes = [vp]
     L.PSGridDim.argtypes = [vp, i]
     L.PSGridDim.restype = ctypes.c_int32
+    L.PSGridSetV.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), vp]
+    L.PSGridSetV.restype = i
     L.PSDomain3DNew.argtypes = [ctypes.c_int32] * 6
     L.PSDomain3DNew.restype = PSDomain
     L.PSStencilMapV.argtypes = [i, ctypes.POINTER(PSDomain), i,
@@ -269,6 +271,16 @@ class Grid:
         lib().PSGridCopyout(self.handle, out.ctypes.data_as(ctypes.c_void_p))
         check()
         return out
+
+    def set(self, index, value):
+        """PSGridSet: one element; index is (x, y, z) truncated to the
+        grid's rank (x first, as the reference's PSGridSet takes it)."""
+        idx = (ctypes.c_int32 * 3)(*(list(index) + [0] * (3 - len(index))))
+        v = np.array([value], dtype=self.dtype)
+        rc = lib().PSGridSetV(self.handle, idx, v.ctypes.data_as(ctypes.c_void_p))
+        if rc != PS_OK:
+            check()
+            raise PSError(rc, "PSGridSetV failed")
 
     def free(self):
         if self.handle:

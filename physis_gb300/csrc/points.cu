@@ -15,16 +15,17 @@
 // so that every shared-memory access of a warp is conflict-free) and
 // warps*RY rows high; work items are (z-chunk, tile) pairs in chunk-major
 // order taken round-robin by a persistent grid, as in the 7-point kernels.
-// * Each z-plane of the tile plus its x/y halo is copied into a ring of
-//   shared-memory planes with cp.async: 16-byte copies for the aligned chunks
-//   inside the grid, element copies through the boundary map for the chunks
-//   that cross an edge.  The boundary rule is applied once, at load time
-//   (periodic halo cells are fetched from the opposite face, clamped ones
-//   from the face), so the compute loop is the same for every rule.
-//   (TMA box loads cannot wrap, hence cp.async here.)
+// * Each z-plane of the tile plus its x/y halo arrives in a ring of
+//   shared-memory planes by one TMA 3D box load (mbarrier per stage, bounded
+//   waits).  A box cannot wrap and fills cells outside the grid with zeros,
+//   so on the edge tiles of periodic and clamped stencils those halo cells
+//   are then rewritten through the boundary map (periodic cells from the
+//   opposite face, clamped ones from the face); the compute loop is the same
+//   for every rule.  Grids without a tensor map are staged with cp.async
+//   through the boundary map instead (16-byte copies inside the grid,
+//   element copies across an edge).
 // * The ring holds rzl + rzh + 1 planes for the stencil's z extent plus
-//   kPrefetch planes in flight; one commit group per plane, and
-//   cp.async.wait_group keeps kPrefetch planes outstanding.
+//   planes in flight ahead of the newest one a step reads.
 // * The sweep body (points_body.cuh) is compiled two ways: here with the
 //   point table (shared-memory offset, plane lag, weight) copied to shared
 //   memory once per CTA and walked in order, and by jit.cpp with NVRTC per

@@ -15,7 +15,11 @@
 // finish (atomic ticket) combines them in a fixed order: FP64 for floating
 // grids, wrapping integer arithmetic for integer grids (the REF fold wraps the
 // same way).  The result is deterministic run to run.
+#include <atomic>
+#include <mutex>
 #include <type_traits>
+
+#include <cuda.h>
 
 #include "physis_gb300/physis_gb300.h"
 #include "ps_device.cuh"
@@ -275,15 +279,49 @@ static __device__ __align__(256) uint64_t g_noalloc_scratch[kNoAllocMaxPartials 
 
 namespace {
 
-// Device address of g_noalloc_scratch and SM count, per device ordinal,
-// looked up on the first call made with that device current.
+// Device address of g_noalloc_scratch and the SM count, per device ordinal,
+// for the CUDA context that was current when they were looked up.  A device
+// reset destroys that context and the module with it; the array may then
+// sit elsewhere, so the entry is keyed by the context's process-unique id
+// (cuCtxGetId) and looked up again when the current context differs.
 struct NoAllocDevice {
-  bool ready;
-  uint64_t *scratch;
-  int sm_count;
+  std::atomic<unsigned long long> ctx_id{0};  // 0: not set up
+  uint64_t *scratch = nullptr;
+  int sm_count = 0;
 };
 constexpr int kNoAllocMaxDevices = 64;
 NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
+std::mutex g_noalloc_setup;  // first calls from several host threads
+
+// The current context's id through the driver entry points the runtime
+// exposes (the library does not link libcuda).  0 when unavailable.
+unsigned long long current_context_id() {
+  typedef CUresult (*GetCurrent)(CUcontext *);
+  typedef CUresult (*GetId)(CUcontext, unsigned long long *);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(fn);
+    fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(fn);
+    cudaGetLastError();
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx ||
+      get_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
 
 }  // namespace
 
@@ -311,9 +349,13 @@ int reduce_noalloc(const void *data, size_t pitch, int nx, int ny, int nz, int t
     return PS_ERR_NO_DEVICE;
   }
   NoAllocDevice &d = g_noalloc_dev[dev];
-  if (!d.ready) {
-    // Set-up, once per device, with that device current: the host-side name
-    // g_noalloc_scratch is not a device address, so look the address up.
+  unsigned long long ctx = current_context_id();
+  if (ctx == 0 || d.ctx_id.load(std::memory_order_acquire) != ctx) {
+    std::lock_guard<std::mutex> lock(g_noalloc_setup);
+    // Set-up with the device current: the host-side name g_noalloc_scratch
+    // is not a device address, so look the address up.  This also loads
+    // the module into the context, and creates the primary context if none
+    // exists yet (so the id is read again afterwards).
     uint64_t *ptr = nullptr;
     if (cudaGetSymbolAddress(reinterpret_cast<void **>(&ptr), g_noalloc_scratch) !=
         cudaSuccess) {
@@ -329,7 +371,9 @@ int reduce_noalloc(const void *data, size_t pitch, int nx, int ny, int nz, int t
     }
     d.scratch = ptr;
     d.sm_count = sms;
-    d.ready = true;
+    // Without a context id (driver entry points unavailable) the lookup is
+    // simply repeated on every call.
+    d.ctx_id.store(current_context_id(), std::memory_order_release);
   }
   GridView g;
   g.ptr = const_cast<void *>(data);

@@ -1706,6 +1706,74 @@ void PSGridFree(void *g) {
   delete p;
 }
 
+// One element of a grid from the host: the grid's rank of indices (x first),
+// bounds-checked, then a stream-ordered copy of the element, so it lands
+// after every stencil run already issued and before any later one.
+static int grid_set(void *g, const PSIndex *idx, const void *buf, const char *fn) {
+  Grid *p = as_grid(g, fn);
+  if (!p) return g_err;
+  if (!idx || !buf) {
+    fail(PS_ERR_INVALID_ARGUMENT, "%s: NULL index or value", fn);
+    return PS_ERR_INVALID_ARGUMENT;
+  }
+  PSIndex c[3] = {0, 0, 0};
+  for (int d = 0; d < p->ndims; ++d) {
+    if (idx[d] < 0 || idx[d] >= p->dim[d]) {
+      fail(PS_ERR_INVALID_ARGUMENT, "%s: index %d of dimension %d outside [0, %d)", fn,
+           (int)idx[d], d, (int)p->dim[d]);
+      return PS_ERR_INVALID_ARGUMENT;
+    }
+    c[d] = idx[d];
+  }
+  char *dst = static_cast<char *>(p->dev) +
+              ((size_t)c[2] * p->dim[1] + c[1]) * p->pitch + (size_t)c[0] * p->esz;
+  if (!cuda_ok(cudaMemcpyAsync(dst, buf, p->esz, cudaMemcpyHostToDevice, rt->stream), fn) ||
+      !cuda_ok(cudaStreamSynchronize(rt->stream), fn))
+    return g_err;
+  return PS_OK;
+}
+
+int PSGridSetV(void *g, const PSIndex *idx, const void *value) {
+  return grid_set(g, idx, value, "PSGridSetV");
+}
+
+void __PSGridSet(void *g, const void *buf, ...) {
+  Grid *p = as_grid(g, "__PSGridSet");
+  if (!p) return;
+  PSIndex idx[3] = {0, 0, 0};
+  va_list vl;
+  va_start(vl, buf);
+  for (int d = 0; d < p->ndims; ++d) idx[d] = va_arg(vl, PSIndex);
+  va_end(vl);
+  grid_set(g, idx, buf, "__PSGridSet");
+}
+
+void __PSGridSetScalar(void *g, int nidx, PSIndex i, PSIndex j, PSIndex k, int is_float,
+                       double vf, long long vi) {
+  Grid *p = as_grid(g, "PSGridSet");
+  if (!p) return;
+  if (nidx != p->ndims) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSGridSet: %d indices for a %d-dimensional grid", nidx,
+         p->ndims);
+    return;
+  }
+  // The value converted to the element type as a C assignment would.
+  union {
+    float f;
+    double d;
+    int32_t i;
+    int64_t l;
+  } v;
+  switch (p->type) {
+    case PS_FLOAT: v.f = is_float ? (float)vf : (float)vi; break;
+    case PS_DOUBLE: v.d = is_float ? vf : (double)vi; break;
+    case PS_INT: v.i = is_float ? (int32_t)vf : (int32_t)vi; break;
+    default: v.l = is_float ? (int64_t)vf : (int64_t)vi; break;
+  }
+  const PSIndex idx[3] = {i, j, k};
+  grid_set(g, idx, &v, "PSGridSet");
+}
+
 PSIndex PSGridDim(void *g, int d) {
   Grid *p = as_grid(g, "PSGridDim");
   if (!p) return 0;

@@ -24,6 +24,7 @@ def _declared_functions():
     for h in ("physis.h", "physis_gb300.h"):
         src = open(os.path.join(INC, "physis_gb300", h)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        src = src.replace("\\\n", " ")  # macro continuation lines
         src = re.sub(r"^\s*#.*$", "", src, flags=re.M)
         for m in re.finditer(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(([^;{}]*)\)\s*;", src):
             name = m.group(1)

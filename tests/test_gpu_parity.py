@@ -397,6 +397,97 @@ def test_reference_style_c_program_runs(rt, tmp_path):
     assert "sum %f" % (7 * total) in r.stderr
 
 
+# The reference's examples/test_set.c, written against this library's
+# header: PSGridSet(g, i, j, k, v) over a 2x2x2 float grid, then a copy-out
+# check (i is x, the fastest index), plus the same for int and 1D/2D grids
+# with values of other types converted on assignment.
+GRIDSET_PROGRAM = r"""
+#include <stdio.h>
+#include <stdlib.h>
+#include "physis_gb300/physis.h"
+#include "physis_gb300/physis_gb300.h"
+#define N 2
+#define IDX3(x, y, z) ((x) + (y) * N + (z) * N * N)
+int main(int argc, char *argv[]) {
+  int i, j, k, bad = 0;
+  float v = 0;
+  PSInit(&argc, &argv, 3, N, N, N);
+  PSGrid3DFloat g = PSGrid3DFloatNew(N, N, N);
+  float *out = (float *)malloc(sizeof(float) * N * N * N);
+  for (i = 0; i < N; ++i)
+    for (j = 0; j < N; ++j)
+      for (k = 0; k < N; ++k) {
+        PSGridSet(g, i, j, k, v);
+        ++v;
+      }
+  PSGridCopyout(g, out);
+  v = 0;
+  for (i = 0; i < N; ++i)
+    for (j = 0; j < N; ++j)
+      for (k = 0; k < N; ++k) {
+        if (out[IDX3(i, j, k)] != v) ++bad;
+        ++v;
+      }
+  {
+    PSGrid2DInt h = PSGrid2DIntNew(3, 2);
+    PSGrid1DDouble d = PSGrid1DDoubleNew(4);
+    int ho[6];
+    double dd[4];
+    long big = 1234567L;
+    PSGridSet(h, 2, 1, 7.9);   /* converted like an int assignment: 7 */
+    PSGridSet(h, 0, 0, big);
+    PSGridSet(d, 3, 0.1f);     /* a float value, widened */
+    PSGridCopyout(h, ho);
+    PSGridCopyout(d, dd);
+    if (ho[5] != 7 || ho[0] != 1234567 || ho[1] != 0) ++bad;
+    if (dd[3] != (double)0.1f || dd[0] != 0.0) ++bad;
+    PSGridSet(h, 3, 0, 1);     /* x outside [0, 3): rejected, recorded */
+    if (PSGetLastError() != PS_ERR_INVALID_ARGUMENT) ++bad;
+    PSClearError();
+  }
+  printf("%s %d\n", bad ? "FAIL" : "OK", bad);
+  PSFinalize();
+  return bad != 0;
+}
+"""
+
+
+def test_grid_set_reference_example(rt, tmp_path):
+    import subprocess
+    from test_abi import compile_c_program
+    exe = compile_c_program(tmp_path, GRIDSET_PROGRAM, "gridset")
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr + r.stdout
+    assert r.stdout.strip() == "OK 0"
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int32, np.int64])
+def test_grid_set_orders_with_stencil_runs(rt, oracle, dtype):
+    # A PSGridSet issued between runs lands after the first and before the
+    # second: the result equals the oracle run with the same edit between.
+    shape = (12, 9, 20)
+    init = _iota(20, dtype)[:12, :9, :20].copy() if dtype in (np.int32, np.int64) else \
+        synth.uniform(shape, 4).astype(dtype)
+    g1, g2 = ps.Grid(shape, dtype), ps.Grid(shape, dtype)
+    g1.copyin(init)
+    g2.copyin(np.zeros(shape, dtype))
+    dom = ps.domain(1, 19, 1, 8, 1, 11)
+    m1 = ps.stencil_map(ps.PS_KERNEL_SUM7, dom, [g1, g2])
+    m2 = ps.stencil_map(ps.PS_KERNEL_SUM7, dom, [g2, g1])
+    ps.stencil_run([m1, m2], 1)
+    g1.set((5, 4, 6), 77)
+    ps.stencil_run([m1], 1)
+    r1, r2 = init.copy(), np.zeros(shape, dtype)
+    lim = (1, 19, 1, 8, 1, 11)
+    oracle.run7(oracle.V_SUM7, r1, r2, lim, (), iter=1)
+    r1[6, 4, 5] = 77
+    oracle.sweep7(oracle.V_SUM7, r1, r2, lim)
+    assert np.array_equal(_bits(g1.copyout()), _bits(r1))
+    assert np.array_equal(_bits(g2.copyout()), _bits(r2))
+    g1.free()
+    g2.free()
+
+
 # ---- temporal blocking -------------------------------------------------------
 
 TEMPORAL = [  # (k, warps, rows, ns)

@@ -1,14 +1,14 @@
 """PSReduceNoAlloc: the reduction for callers that cannot allocate GPU memory.
 
-Some callers of this library may not call cudaMalloc: code recording a CUDA
-graph or stream capture (an allocation is not capturable and synchronises the
-device), latency-bound loops, and processes whose device memory belongs to
-another allocator.  PSReduceNoAlloc reduces a grid the caller already holds
-in device memory and writes the 8-byte result to device memory the caller
-passes, using only a static device array as scratch.  These tests check that
-it agrees with the allocating entry point (PSReduce through a grid handle)
-on two calls in a row, and that it rejects bad arguments before touching a
-GPU.
+Some callers of this library may not call cudaMalloc: latency-bound loops
+that cannot afford the device-wide synchronisation an allocation implies, and
+processes whose device memory belongs to another allocator (a caching pool
+that has reserved the free memory).  PSReduceNoAlloc reduces a grid the
+caller already holds in device memory and writes the 8-byte result to device
+memory the caller passes, using only a static device array as scratch.
+These tests check that it agrees with the allocating entry point (PSReduce
+through a grid handle) on two calls in a row, and that it rejects bad
+arguments before touching a GPU.
 
 This file is collected last on purpose (tests/test_zz_*): if it fails, a
 run that stops at the first failure has already run every other test.
