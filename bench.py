@@ -172,8 +172,9 @@ def measured_peaks():
 
 
 def profiled_traffic():
-    """dram bytes per launch of the sweep kernel from the committed ncu
-    summary (profiles/diffusion7_512.md, line `traffic_bytes_per_launch:`)."""
+    """dram bytes (read + write) of one 512^3 launch of the sweep kernel,
+    from the committed ncu summary of a full-size capture
+    (profiles/diffusion7_512.md, line `traffic_bytes_per_launch:`)."""
     p = os.path.join(ROOT, "profiles", "diffusion7_512.md")
     if not os.path.exists(p):
         return None
@@ -425,28 +426,27 @@ def run_gpu(args, dist):
     L.PSHostFree(hin)
     L.PSHostFree(hout)
 
-    # the same run with temporal blocking (k = 2 steps per pass): bit-exact,
-    # and with contracted multiply-adds (within 1e-5 of REF)
+    # the same run with temporal blocking: k = 2 steps per pass on a fixed
+    # shape, then the autotuner's choice among plain shapes and temporal
+    # depths (its trials run inside the warm-up, then K timed steps).  Both
+    # bit-exact (no contraction: contracted passes drift past 1e-5 of REF
+    # before the 1000 steps of this workload, so they are not reported).
     temporal = None
-    if args.temporal == 1:
-        temporal = {"k": 2, "tshape": "8,4,3", "steps": K}
-        for key, fma in (("glups_bit_exact", False), ("glups_fma", True)):
-            ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 2, warps=8, rows=4, ns=3)
-            ps.set_fma(fma)
-            steps(W)
-            ps.synchronize()
-            dist.barrier()
-            L.PSEventRecord(0)
-            steps(K)
-            L.PSEventRecord(1)
-            ps.synchronize()
-            tms = dist.reduce(L.PSEventElapsedMs(0, 1), "MAX")
-            temporal[key] = dist.ws * cells * K / (tms / 1e3) / 1e9
+    if args.temporal == 1 and not args.no_extras:
+        temporal = {"k": 2, "tshape": "8,4,3", "steps": K, "bit_exact": True}
+        ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 2, warps=8, rows=4, ns=3)
+        steps(W)
+        ps.synchronize()
+        dist.barrier()
+        L.PSEventRecord(0)
+        steps(K)
+        L.PSEventRecord(1)
+        ps.synchronize()
+        tms = dist.reduce(L.PSEventElapsedMs(0, 1), "MAX")
+        temporal["glups"] = dist.ws * cells * K / (tms / 1e3) / 1e9
         ps.set_temporal(ps.PS_KERNEL_DIFFUSION7, 1)
-        # the autotuner's choice (plain shapes and k = 2..4) with contraction
-        # on: its trials run inside the warm-up, then K timed steps
         ps.set_autotune(True)
-        steps(max(W, 200))
+        steps(max(W, 400))
         ps.synchronize()
         tuned, shape_t, k_t, tshape_t = ps.stencil_plan(m1)
         dist.barrier()
@@ -455,11 +455,10 @@ def run_gpu(args, dist):
         L.PSEventRecord(1)
         ps.synchronize()
         tms = dist.reduce(L.PSEventElapsedMs(0, 1), "MAX")
-        temporal["autotuned_fma"] = {"glups": dist.ws * cells * K / (tms / 1e3) / 1e9,
-                                     "tuned": tuned, "k": k_t, "launch_shape": list(shape_t),
-                                     "temporal_shape": list(tshape_t)}
+        temporal["autotuned"] = {"glups": dist.ws * cells * K / (tms / 1e3) / 1e9,
+                                 "tuned": tuned, "k": k_t, "launch_shape": list(shape_t),
+                                 "temporal_shape": list(tshape_t)}
         ps.set_autotune(False)
-        ps.set_fma(False)
         ps.check()
 
     peak, peak_kind = measured_peaks()
@@ -1156,8 +1155,9 @@ def measured_bf16_tflops():
 
 def run_gpu_warmstart(args, dist):
     """Train the warm-start network on solved instances, then time the
-    held-out Jacobi solves to relative residual 1e-6 from zero and from the
-    network's prediction (prediction time included)."""
+    held-out Jacobi solves to relative residual 1e-6 from zero, from the
+    network's prediction, and from the prediction followed by learned
+    restarts (prediction and restart time included)."""
     import torch
     import physis_gb300 as ps
     from physis_gb300 import warmstart as ws
@@ -1169,12 +1169,13 @@ def run_gpu_warmstart(args, dist):
         shape, factor, nsx, per_stack, chunk = (257, 129, 129), 16, 16, 64, 2000
     else:
         shape, factor, nsx, per_stack, chunk = (args.ws_nz, args.ws_ny, args.ws_nx), 4, 15, 300, 256
+    snapshots = [int(v) for v in args.ws_snapshots.split(",") if v.strip()]
     rng = np.random.default_rng(5)
     workers = min(16, os.cpu_count() or 1)
     t0 = time.perf_counter()
     data = ws.Dataset(rng, args.ws_train, shape, factor, nsx=nsx, per_stack=per_stack, tol=1e-7,
                       chunk=chunk, max_sweeps=args.ws_max_sweeps, workers=workers,
-                      mirrors=args.ws_mirrors)
+                      mirrors=args.ws_mirrors, snapshots=snapshots)
     data_s = time.perf_counter() - t0
     net = ws.Net(seed=1)
     per_epoch = max(1, data.x.shape[0] // 32)
@@ -1192,43 +1193,54 @@ def run_gpu_warmstart(args, dist):
         st.grids[1].copyin(zeros)
 
     scales = (data.wscale, data.pscale)
-    # Sweep counts, checked every 32 sweeps.  Float32 Jacobi has a residual
-    # floor near 1e-7 * ||p|| / ||ss(0)||; instances whose floor lies above
-    # 1e-6 never get there from either start and are left out of the
+    pm = args.ws_predict_mirrors
+    K, nu = args.ws_restarts, args.ws_nu
+    # Sweep counts, checked every `echunk` sweeps.  Float32 Jacobi has a
+    # residual floor near 1e-7 * ||p|| / ||ss(0)||; instances whose floor lies
+    # above 1e-6 never get there from any start and are left out of the
     # comparison (counted in the output).
     reset()
     zero = st.solve(1e-6, echunk, args.ws_max_sweeps)
-    pm = args.ws_predict_mirrors
-    reset()
-    ws.predict_into(net, st, scales, factor, pm)
-    r_warm0 = st.residuals()
-    warm = st.solve(1e-6, echunk, args.ws_max_sweeps)
-    both = (zero > 0) & (warm > 0)
-    nz_sw, nw_sw = int(zero[both].max()), int(warm[both].max())
+    modes = {"single": 0}
+    if K > 0:
+        modes["restarts"] = K
+    counts, r_start = {}, {}
+    for name, k in modes.items():
+        reset()
+        used = ws.predict_into(net, st, scales, factor, pm, restarts=k, nu=nu)
+        r_start[name] = st.residuals()
+        c = st.solve(1e-6, echunk, args.ws_max_sweeps)
+        counts[name] = np.where(c > 0, c + used, c)
+    both = zero > 0
+    for c in counts.values():
+        both &= c > 0
+    nz_sw = int(zero[both].max())
+    final_sw = {name: int((counts[name][both] - modes[name] * nu).max()) for name in modes}
 
-    def timed(warm_start, n):
+    def timed(k, n):
         reset()
         ps.synchronize()
         torch.cuda.synchronize()
         t = time.perf_counter()
-        if warm_start:
-            ws.predict_into(net, st, scales, factor, pm)
+        if k is not None:
+            ws.predict_into(net, st, scales, factor, pm, restarts=k, nu=nu)
         st.sweeps(n)
         ps.synchronize()
         return time.perf_counter() - t
 
-    for _ in range(max(args.warmup, 3) // 3):  # warm-up of both paths
-        timed(False, 32)
-        timed(True, 32)
+    for _ in range(max(args.warmup, 3) // 3):  # warm-up of every path
+        timed(None, 32)
+        for k in modes.values():
+            timed(k, 32)
     reps = 1 if args.ws_full else 2
-    tz = min(timed(False, nz_sw) for _ in range(reps))
-    r_zero_end = st.residuals()
-    tw = min(timed(True, nw_sw) for _ in range(reps))
-    r_end = st.residuals()  # after the warm timed run
-    # instances at or below 1e-6 after the timed runs (a few whose float32
-    # floor lies just under 1e-6 can drift back above it between checks)
-    ok_zero = int((r_zero_end[both] <= 1e-6).sum())
-    ok_warm = int((r_end[both] <= 1e-6).sum())
+    tz = min(timed(None, nz_sw) for _ in range(reps))
+    ok_zero = int((st.residuals()[both] <= 1e-6).sum())
+    secs, oks = {}, {}
+    for name, k in modes.items():
+        secs[name] = min(timed(k, final_sw[name]) for _ in range(reps))
+        # instances at or below 1e-6 after the timed run (a few whose float32
+        # floor lies just under 1e-6 can drift back above it between checks)
+        oks[name] = int((st.residuals()[both] <= 1e-6).sum())
 
     # Ceiling of the coarse representation (--ws-ceiling): the held-out
     # instances solved on to 1e-7, their exact block-centre samples upsampled
@@ -1250,7 +1262,8 @@ def run_gpu_warmstart(args, dist):
         ok = both & (best > 0)
         ceiling = {"sweeps_mean": float(best[ok].mean()),
                    "sweeps_ratio_mean": float(zero[ok].mean() / best[ok].mean()),
-                   "what": "warm start from the exact solution's block-centre samples"}
+                   "what": "single-shot warm start from the exact solution's block-centre "
+                           "samples"}
 
     # tensor roofline of the network's forward pass over the training set
     zc, yc, xc = data.dims1
@@ -1267,13 +1280,25 @@ def run_gpu_warmstart(args, dist):
     peak, peak_kind = measured_bf16_tflops()
     tflops = flops / (fwd_ms / 1e3) / 1e12
     st.free()
+    head = "restarts" if "restarts" in modes else "single"
+
+    def mode_out(name):
+        return {"sweeps_mean": float(counts[name][both].mean()),
+                "sweeps_max": int(counts[name][both].max()),
+                "seconds": secs[name], "speedup_wall": tz / secs[name],
+                "sweeps_ratio_mean": float(zero[both].mean() / counts[name][both].mean()),
+                "at_1e-6_after_timed_run": oks[name],
+                "initial_residual_median": float(np.median(r_start[name])),
+                "restarts": modes[name], "sweeps_per_restart": nu if modes[name] else 0}
+
     line = {
         "metric": "Poisson time-to-1e-6 resid, learned vs plain (speed-up of the warm start)",
-        "value": tz / tw, "unit": "x", "n_gpus": 1, "steps": args.ws_held,
-        "warmup": max(args.warmup, 3), "ms_per_step": tw / args.ws_held * 1e3,
+        "value": tz / secs[head], "unit": "x", "n_gpus": 1, "steps": args.ws_held,
+        "warmup": max(args.warmup, 3), "ms_per_step": secs[head] / args.ws_held * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16",
         "data": f"synthetic seeded instances (seed 5), {args.ws_train} solved for training "
-                f"(x {len(data.flips)} mirror images), {args.ws_held} held out",
+                f"(x {len(data.flips)} mirror images, + {len(snapshots)} solve iterates each "
+                f"for the restarts), {args.ws_held} held out",
         "config": {"workload": f"learned warm start, 19-point Jacobi {shape[2]}x{shape[1]}x"
                                f"{shape[0]} (x,y,z" +
                                ("; the specified size)" if args.ws_full
@@ -1281,19 +1306,18 @@ def run_gpu_warmstart(args, dist):
                    "pool_factor": factor, "sweep_count_resolution": echunk,
                    "network": f"pool {factor}^3 (9 channels) -> 6 conv 3x3x3 x16 (BF16, FP32 acc.) "
                               "-> Catmull-Rom",
+                   "headline": head,
                    "epochs": epochs, "adam_steps": epochs * per_epoch, "batch": 32,
-                   "mirror_images": len(data.flips),
+                   "mirror_images": len(data.flips), "training_snapshots": snapshots,
                    "prediction_mirror_images": len(ws.mirror_images(shape, pm)),
                    "l2": f"held-out stack: 14 arrays, {stack_gb:.1f} GB in all, > L2"},
         "compared_instances": int(both.sum()),
         "below_1e-6_unreachable": {"zero_start": int((zero <= 0).sum()),
-                                   "warm_start": int((warm <= 0).sum())},
+                                   **{name: int((counts[name] <= 0).sum()) for name in modes}},
         "zero_start": {"sweeps_mean": float(zero[both].mean()), "sweeps_max": nz_sw,
                        "seconds": tz, "at_1e-6_after_timed_run": ok_zero},
-        "warm_start": {"sweeps_mean": float(warm[both].mean()), "sweeps_max": nw_sw,
-                       "seconds": tw, "at_1e-6_after_timed_run": ok_warm,
-                       "initial_residual_median": float(np.median(r_warm0))},
-        "sweeps_ratio_mean": float(zero[both].mean() / warm[both].mean()),
+        "warm_start": mode_out("single"),
+        "warm_start_restarts": mode_out("restarts") if "restarts" in modes else None,
         "training": {"seconds": train_s, "loss_first_epoch": hist[0],
                      "loss_last_epoch": hist[-1]},
         "network_forward_ms": fwd_ms,
@@ -1317,7 +1341,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
-                    help="diffusion: leave out the himeno/batch/config1/reduce keys")
+                    help="diffusion: leave out the temporal/himeno/batch/config1/reduce "
+                         "keys (the plain sweep alone, e.g. for a profiler)")
     ap.add_argument("--warps", type=int, default=0)
     ap.add_argument("--rows", type=int, default=0)
     ap.add_argument("--ns", type=int, default=0)
@@ -1353,6 +1378,13 @@ def main():
     ap.add_argument("--ws-ny", type=int, default=33)
     ap.add_argument("--ws-nz", type=int, default=65)
     ap.add_argument("--ws-max-sweeps", type=int, default=12000)
+    ap.add_argument("--ws-restarts", type=int, default=3,
+                    help="warm start: learned restarts after the prediction (0: single shot)")
+    ap.add_argument("--ws-nu", type=int, default=32,
+                    help="warm start: Jacobi sweeps before each learned restart (even)")
+    ap.add_argument("--ws-snapshots", default="32,128,512,2048",
+                    help="warm start: sweep counts of the target solves whose iterates "
+                         "train the restarts (comma-separated, even)")
     ap.add_argument("--ws-full", action="store_true",
                     help="config 5 at the specified 129x129x257 (use --ws-train/--ws-held "
                          "to size it, e.g. 128/32, and --ws-max-sweeps 100000)")

@@ -363,6 +363,15 @@ typedef struct PSWarmStartFields {
    * calls, `coarse` is a prediction for this mirror image; they write the
    * stored instance. */
   int flip;
+  /* Per-instance scale s[b] (NULL: 1): the pooling calls multiply the source
+   * channels (and PoolTarget its target) by s[b], the upsampling calls
+   * divide the prediction by it.  The equation is linear in the source, so
+   * a residual source of any size can be brought to the network's input
+   * range (PSWarmStartResidualSource computes such scales). */
+  const float *inst_scale;
+  /* PoolTarget only (NULL: none): the target is p - p_sub, the error of an
+   * iterate p_sub against the solution p. */
+  const float *p_sub;
 } PSWarmStartFields;
 
 /* Network input: per factor^3 block of each instance (of its mirror image),
@@ -381,6 +390,18 @@ int PSWarmStartUpsample(const PSWarmStartFields *f, const float *coarse, float *
  * mirror images (pscale times their count) gives one warm start. */
 int PSWarmStartUpsampleAdd(const PSWarmStartFields *f, const float *coarse, float *p,
                            void *stream);
+/* Residual source of the iterate f->p for the correction problem.  The
+ * 19-point residual (examples/himeno/himenobmtxpa_original.c:331-334) with
+ * c_i = a_i, b = 0 is ss = (s0 a3 - p) bnd; r = ss / a3 is the source, in
+ * wrk1's units, of the same equation for the error p* - p.  Writes r for
+ * every cell of every instance into `r` (the fields' stacked layout; 0 on
+ * the faces) and inst_scale[b] = target_rms / rms(r over instance b's
+ * interior) (0 where r vanishes).  work: work_len doubles of caller scratch,
+ * at least one per instance (64 per instance is used when given).  Pooling r
+ * as wrk1 with these scales and upsampling the network's output with them
+ * adds the network's prediction of the error: a learned restart. */
+int PSWarmStartResidualSource(const PSWarmStartFields *f, float *r, float *inst_scale,
+                              float target_rms, double *work, int work_len, void *stream);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop

@@ -60,7 +60,7 @@ PSSetBatchShape __PSStencilMapRedBlack __PSStencilMapRed __PSStencilMapBlack
 PSStencilMapColorV PSPointStencilNew PSStencilFunctionNew
 PSStencilFunctionCheck PSWarmStartConv PSWarmStartWeightGrad PSWarmStartPrepareWeights
 PSWarmStartAdam PSWarmStartLoss PSWarmStartPool PSWarmStartPoolTarget
-PSWarmStartUpsample PSWarmStartUpsampleAdd""".split()
+PSWarmStartUpsample PSWarmStartUpsampleAdd PSWarmStartResidualSource""".split()
 
 
 class PSDomain(ctypes.Structure):
@@ -83,7 +83,8 @@ class PSWarmStartFields(ctypes.Structure):
                 ("pitch", ctypes.c_longlong), ("ny", ctypes.c_int), ("inx", ctypes.c_int),
                 ("iny", ctypes.c_int), ("inz", ctypes.c_int), ("nsx", ctypes.c_int),
                 ("factor", ctypes.c_int), ("batch", ctypes.c_int), ("wscale", ctypes.c_float),
-                ("pscale", ctypes.c_float), ("flip", ctypes.c_int)]
+                ("pscale", ctypes.c_float), ("flip", ctypes.c_int),
+                ("inst_scale", ctypes.c_void_p), ("p_sub", ctypes.c_void_p)]
 
 
 class PSError(RuntimeError):
@@ -195,9 +196,11 @@ def lib():
     L.PSWarmStartPoolTarget.argtypes = [fp, vp, vp]
     L.PSWarmStartUpsample.argtypes = [fp, vp, vp, vp]
     L.PSWarmStartUpsampleAdd.argtypes = [fp, vp, vp, vp]
+    L.PSWarmStartResidualSource.argtypes = [fp, vp, vp, ctypes.c_float, vp, i, vp]
     for name in ("PSWarmStartConv", "PSWarmStartWeightGrad", "PSWarmStartPrepareWeights",
                  "PSWarmStartAdam", "PSWarmStartLoss", "PSWarmStartPool",
-                 "PSWarmStartPoolTarget", "PSWarmStartUpsample", "PSWarmStartUpsampleAdd"):
+                 "PSWarmStartPoolTarget", "PSWarmStartUpsample", "PSWarmStartUpsampleAdd",
+                 "PSWarmStartResidualSource"):
         getattr(L, name).restype = i
     _lib = L
     return L

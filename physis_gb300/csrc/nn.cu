@@ -464,7 +464,13 @@ struct PoolArgs {
   int batch;
   int flip;
   float wscale, pscale;
+  const float *inst_scale;  // per-instance source/solution scale (NULL: 1)
+  const float *p_sub;       // pool_target: subtract this grid from p (NULL: none)
 };
+
+__device__ __forceinline__ float inst_scale_of(const PoolArgs &a, int b) {
+  return a.inst_scale ? a.inst_scale[b] : 1.f;
+}
 
 __device__ __forceinline__ long long fine_index(const PoolArgs &a, int b, int z, int y, int x) {
   const int ox = (b % a.nsx) * a.inx, oz = (b / a.nsx) * a.inz;
@@ -518,13 +524,14 @@ __global__ void pool_inputs_kernel(PoolArgs a, __nv_bfloat16 *__restrict__ out) 
         ++cnt;
       }
   const float inv = 1.f / (float)cnt;
+  const float ws = a.wscale * inst_scale_of(a, b);
   __nv_bfloat16 *row = out + i * kC;
   row[0] = __float2bfloat16_rn(s[0] * inv);
   row[1] = __float2bfloat16_rn(s[1] * inv);
   row[2] = __float2bfloat16_rn(s[2] * inv);
-  row[3] = __float2bfloat16_rn(s[3] * inv * a.wscale);
+  row[3] = __float2bfloat16_rn(s[3] * inv * ws);
   row[4] = __float2bfloat16_rn(s[4] * inv);
-  row[5] = __float2bfloat16_rn(s[5] * inv * a.wscale);
+  row[5] = __float2bfloat16_rn(s[5] * inv * ws);
   for (int c = 6; c < 9; ++c) row[c] = __float2bfloat16_rn(-logf(s[c] * inv));
   for (int c = kPoolChannels; c < kC; ++c) row[c] = __float2bfloat16_rn(0.f);
 }
@@ -552,8 +559,11 @@ __global__ void pool_target_kernel(PoolArgs a, float *__restrict__ out) {
   float s = 0.f;
   for (int k = 0; k < 2; ++k)
     for (int j = 0; j < 2; ++j)
-      for (int m = 0; m < 2; ++m) s += a.p[vmap(a, b, zs[k], ys[j], xs[m])];
-  out[i] = s * 0.125f * a.pscale;
+      for (int m = 0; m < 2; ++m) {
+        const long long c = vmap(a, b, zs[k], ys[j], xs[m]);
+        s += a.p_sub ? a.p[c] - a.p_sub[c] : a.p[c];
+      }
+  out[i] = s * 0.125f * a.pscale * inst_scale_of(a, b);
 }
 
 // Catmull-Rom weights of points -1, 0, 1, 2 at t in [0, 1] past point 0
@@ -611,8 +621,69 @@ __global__ void upsample_kernel(PoolArgs a, const float *__restrict__ coarse,
     v += wz[kz] * vy;
   }
   const long long k = fine_index(a, b, z, y, x);
-  const float u = v / a.pscale * a.bnd[k];
+  const float sc = inst_scale_of(a, b);
+  const float u = sc != 0.f ? v / (a.pscale * sc) * a.bnd[k] : 0.f;
   p[k] = add ? p[k] + u : u;
+}
+
+// Residual source of the current pressure p, for the correction problem:
+// with c_i = a_i and b = 0 the 19-point Himeno residual is
+// ss = (s0 a3 - p) bnd with s0 = sum_i a_i (p(x + e_i) + p(x - e_i)) + wrk1
+// and a3 = 1 / (2 (a0 + a1 + a2)), so r = ss / a3 =
+// (s0 - 2 (a0 + a1 + a2) p) bnd is the source (in wrk1's units) of the
+// equation the error p* - p satisfies.  Cells on an instance's faces (and
+// bnd = 0 cells) get r = 0 and read no neighbours.  r is written in the
+// stacked layout of the fields.  Grid (G, batch): block (g, b) strides over
+// instance b's cells and stores its FP64 partial sum of r^2 at
+// part[b * G + g] (fixed assignment, so the per-instance sums are
+// deterministic).
+__global__ void residual_source_kernel(PoolArgs a, float *__restrict__ r,
+                                       double *__restrict__ part) {
+  const int b = blockIdx.y;
+  const long long n = (long long)a.inz * a.iny * a.inx;
+  double acc = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(i % a.inx), y = (int)((i / a.inx) % a.iny);
+    const int z = (int)(i / ((long long)a.inx * a.iny));
+    const long long k = fine_index(a, b, z, y, x);
+    float v = 0.f;
+    const bool inner = x > 0 && x < a.inx - 1 && y > 0 && y < a.iny - 1 && z > 0 &&
+                       z < a.inz - 1;
+    if (inner && a.bnd[k] != 0.f) {
+      const long long py = a.pitch_e, pz = (long long)a.ny * a.pitch_e;
+      const float pc = a.p[k];
+      const float c0 = a.a0[k], c1 = a.a1[k], c2 = a.a2[k];
+      float s0 = c0 * (a.p[k + pz] + a.p[k - pz]);
+      s0 += c1 * (a.p[k + py] + a.p[k - py]);
+      s0 += c2 * (a.p[k + 1] + a.p[k - 1]);
+      s0 += a.wrk1[k];
+      v = (s0 - 2.f * (c0 + c1 + c2) * pc) * a.bnd[k];
+    }
+    r[k] = v;
+    acc += (double)v * v;
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[(long long)b * gridDim.x + blockIdx.x] = red[0];
+}
+
+// scale[b] = target_rms / rms(r of instance b) over its interior cells
+// (0 when r vanishes); the partials are summed in a fixed order.
+__global__ void inst_scale_kernel(const double *__restrict__ part, int G, int batch,
+                                  long long cells, float target_rms,
+                                  float *__restrict__ scale) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  double s = 0.0;
+  for (int g = 0; g < G; ++g) s += part[(long long)b * G + g];
+  const double rms = sqrt(s / (double)cells);
+  scale[b] = rms > 0.0 ? (float)(target_rms / rms) : 0.f;
 }
 
 }  // namespace
@@ -708,6 +779,8 @@ static PoolArgs pool_args(const NNFields &f) {
   a.flip = f.flip;
   a.wscale = f.wscale;
   a.pscale = f.pscale;
+  a.inst_scale = f.inst_scale;
+  a.p_sub = f.p_sub;
   return a;
 }
 
@@ -733,6 +806,22 @@ int nn_upsample(const NNFields &f, const float *coarse, float *p, bool add, cuda
   const long long n = (long long)a.batch * a.inz * a.iny * a.inx;
   if (n <= 0) return -1;
   upsample_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, coarse, p, add);
+  return (int)cudaGetLastError();
+}
+
+int nn_residual_source(const NNFields &f, float *r, float *inst_scale, float target_rms,
+                       double *work, int work_len, cudaStream_t s) {
+  const PoolArgs a = pool_args(f);
+  if (!a.p || !r || !inst_scale || !work || a.batch < 1) return -1;
+  const int G = work_len / a.batch;
+  if (G < 1) return -1;
+  const int g = G < 64 ? G : 64;
+  residual_source_kernel<<<dim3((unsigned)g, (unsigned)a.batch), 256, 0, s>>>(a, r, work);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return (int)e;
+  const long long cells = (long long)(a.inz - 2) * (a.iny - 2) * (a.inx - 2);
+  inst_scale_kernel<<<(unsigned)((a.batch + 127) / 128), 128, 0, s>>>(
+      work, g, a.batch, cells > 0 ? cells : 1, target_rms, inst_scale);
   return (int)cudaGetLastError();
 }
 

@@ -218,6 +218,8 @@ struct NNFields {
   int inx, iny, inz, nsx, factor, batch;
   float wscale, pscale;
   int flip;  // mirror image: bits 0-2 mirror x/y/z, bit 3 swaps x and y
+  const float *inst_scale;  // per-instance scale of source and solution (NULL: 1)
+  const float *p_sub;       // pool_target: p - p_sub (NULL: p)
 };
 // Each returns 0, -1 for invalid arguments, or the launch's cudaError_t.
 // Device error word for the kernels' bounded waits (set at PSInit).
@@ -236,6 +238,11 @@ int nn_mse(const float *pred, const float *tgt, long long n, void *dy, double *p
 int nn_pool_inputs(const NNFields &f, void *out, cudaStream_t s);
 int nn_pool_target(const NNFields &f, float *out, cudaStream_t s);
 int nn_upsample(const NNFields &f, const float *coarse, float *p, bool add, cudaStream_t s);
+// Residual source r of f.p for the correction problem, in f's stacked
+// layout, and inst_scale[b] = target_rms / rms(r of instance b); work holds
+// work_len doubles (at least one per instance).
+int nn_residual_source(const NNFields &f, float *r, float *inst_scale, float target_rms,
+                       double *work, int work_len, cudaStream_t s);
 
 // ---- Reductions (reduce.cu) ----------------------------------------------
 // Reduces every element of g with op.  The 8-byte result is written to

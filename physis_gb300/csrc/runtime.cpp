@@ -2306,6 +2306,8 @@ static psg::NNFields ws_fields(const PSWarmStartFields *f) {
   n.wscale = f->wscale;
   n.pscale = f->pscale;
   n.flip = f->flip;
+  n.inst_scale = f->inst_scale;
+  n.p_sub = f->p_sub;
   return n;
 }
 
@@ -2362,6 +2364,16 @@ int PSWarmStartLoss(const float *pred, const float *target, long long n, void *d
 int PSWarmStartPool(const PSWarmStartFields *f, void *out, void *stream) {
   if (!ws_fields_ok(f, "PSWarmStartPool", false) || !out) return PS_ERR_INVALID_ARGUMENT;
   return ws_status(psg::nn_pool_inputs(ws_fields(f), out, ws_stream(stream)), "PSWarmStartPool");
+}
+
+int PSWarmStartResidualSource(const PSWarmStartFields *f, float *r, float *inst_scale,
+                              float target_rms, double *work, int work_len, void *stream) {
+  if (!ws_fields_ok(f, "PSWarmStartResidualSource", true) || !r || !inst_scale || !work ||
+      work_len < f->batch || f->flip != 0)
+    return ws_status(-1, "PSWarmStartResidualSource");
+  return ws_status(psg::nn_residual_source(ws_fields(f), r, inst_scale, target_rms, work,
+                                           work_len, ws_stream(stream)),
+                   "PSWarmStartResidualSource");
 }
 
 int PSWarmStartPoolTarget(const PSWarmStartFields *f, float *out, void *stream) {

@@ -184,26 +184,62 @@ class Stack:
             out.append(math.sqrt(max(float(g), 0.0) / self.r0[b]))
         return np.array(out)
 
-    def solve(self, tol, chunk, max_sweeps):
+    def solve(self, tol, chunk, max_sweeps, snapshots=()):
         """Sweeps (a multiple of `chunk`) after which each instance first
-        met `tol`; -1 if it did not within max_sweeps."""
+        met `tol`; -1 if it did not within max_sweeps.  `snapshots` pairs
+        (sweep count, grid): p is copied into the grid when the count is
+        reached (even counts; iterates for training the restarts)."""
         done = np.full(self.count, -1)
+        snaps = sorted(snapshots, key=lambda t: t[0])
         n = 0
-        while n < max_sweeps and (done < 0).any():
-            self.sweeps(chunk)
-            n += chunk
-            r = self.residuals()
-            done[(done < 0) & (r <= tol)] = n
+        while n < max_sweeps and ((done < 0).any() or snaps):
+            stop = (n // chunk + 1) * chunk
+            if snaps and snaps[0][0] < stop:
+                stop = snaps[0][0]
+            self.sweeps(stop - n)
+            n = stop
+            while snaps and snaps[0][0] == n:
+                self.copy_p(snaps.pop(0)[1])
+            if n % chunk == 0 and (done < 0).any():
+                r = self.residuals()
+                done[(done < 0) & (r <= tol)] = n
         return done
 
-    def fields(self, factor, wscale=1.0, pscale=1.0, with_p=False, flip=0):
+    def copy_p(self, grid):
+        """grid = p (p0), through the library's copy kernel."""
+        full = ps.full_domain(self.gshape)
+        ps.stencil_run([ps.stencil_map(ps.PS_KERNEL_COPY, full, [self.grids[0], grid])])
+
+    def residual_source(self, target_rms, p=None):
+        """Residual source r of p (default p0) for the correction problem
+        into self.rgrid, and the per-instance scales that bring r to
+        target_rms (a float32 tensor, one per instance)."""
+        import torch
+        if getattr(self, "rgrid", None) is None:
+            self.rgrid = ps.Grid(self.gshape)
+            self.rwork = torch.empty(self.count * 64, dtype=torch.float64, device="cuda")
+            self.rscale = torch.empty(self.count, dtype=torch.float32, device="cuda")
+        f = self.fields(1, with_p=True)
+        if p is not None:
+            f.p = p.dev_ptr
+        _ok(ps.lib().PSWarmStartResidualSource(
+            ctypes.byref(f), ctypes.c_void_p(self.rgrid.dev_ptr), _p(self.rscale),
+            ctypes.c_float(target_rms), _p(self.rwork), self.rwork.numel(), None))
+        return self.rscale
+
+    def fields(self, factor, wscale=1.0, pscale=1.0, with_p=False, flip=0, wrk1=None,
+               inst_scale=None, p=None, p_sub=None):
         """PSWarmStartFields describing this stack for the pooling kernels
-        (of mirror image `flip` of every instance)."""
+        (of mirror image `flip` of every instance).  wrk1: another source
+        grid (a residual source); inst_scale: per-instance scales (tensor);
+        p / p_sub: the solution grid and an iterate to subtract from it."""
         f = ps.PSWarmStartFields()
         g = self.grids
         f.a0, f.a1, f.a2 = g[2].dev_ptr, g[3].dev_ptr, g[4].dev_ptr
-        f.wrk1, f.bnd = g[13].dev_ptr, g[12].dev_ptr
-        f.p = g[0].dev_ptr if with_p else None
+        f.wrk1, f.bnd = (wrk1 or g[13]).dev_ptr, g[12].dev_ptr
+        f.p = (p or g[0]).dev_ptr if (with_p or p is not None) else None
+        f.inst_scale = None if inst_scale is None else inst_scale.data_ptr()
+        f.p_sub = None if p_sub is None else p_sub.dev_ptr
         f.pitch = g[0].pitch
         f.ny = self.gshape[1]
         f.inz, f.iny, f.inx = self.shape
@@ -217,6 +253,9 @@ class Stack:
     def free(self):
         for g in self.grids + [self.scratch]:
             g.free()
+        if getattr(self, "rgrid", None) is not None:
+            self.rgrid.free()
+            self.rgrid = None
 
 
 def coarse_shape(shape, factor):
@@ -361,13 +400,18 @@ class Dataset:
     """Pooled inputs and targets of many instances, resident on the GPU.
 
     Each solved instance gives `mirrors` training pairs (its mirror images,
-    which solve the mirrored problem).  Samples are stored mirror-major:
-    sample m * count + i is mirror image m of instance i, so contiguous
-    minibatches hold different instances."""
+    which solve the mirrored problem).  With `snapshots` (sweep counts), the
+    iterates of the target solve at those counts give further pairs for the
+    correction problem: input the residual source r of the iterate (scaled
+    per instance to the source's RMS), target the iterate's error p* - p
+    (scaled alike), which is what a learned restart predicts.  Samples are
+    stored kind-major (the source pairs, then each snapshot's pairs), then
+    mirror-major: sample (k * nm + m) * count + i is mirror image m of
+    instance i, so contiguous minibatches hold different instances."""
 
     def __init__(self, rng, count, shape, factor, nsx=15, per_stack=300, tol=1e-7,
                  chunk=256, max_sweeps=40000, wscale=None, pscale=None, log=None, workers=0,
-                 mirrors=1):
+                 mirrors=1, snapshots=()):
         import torch
         self.shape, self.factor = shape, factor
         zc, yc, xc = coarse_shape(shape, factor)
@@ -375,8 +419,12 @@ class Dataset:
         self.flips = mirror_images(shape, mirrors)
         nm = len(self.flips)
         self.count = count
-        self.x = torch.empty((nm * count, zc, yc, xc, C), dtype=torch.bfloat16, device="cuda")
-        self.t = torch.empty((nm * count, zc, yc, xc), dtype=torch.float32, device="cuda")
+        self.snapshots = tuple(int(v) for v in snapshots)
+        kinds = 1 + len(self.snapshots)
+        self.x = torch.empty((kinds * nm * count, zc, yc, xc, C), dtype=torch.bfloat16,
+                             device="cuda")
+        self.t = torch.empty((kinds * nm * count, zc, yc, xc), dtype=torch.float32,
+                             device="cuda")
         self.sweeps = np.zeros(count, int)
         self.wscale, self.pscale = wscale, pscale
         self.solve_seconds = 0.0
@@ -388,9 +436,10 @@ class Dataset:
             if self.wscale is None:
                 self.wscale = 1.0 / float(np.std(np.concatenate([i["wrk1"].ravel() for i in insts])))
             st = Stack(insts, shape, nsx)
+            snaps = [(n, ps.Grid(st.gshape)) for n in self.snapshots]
             ps.synchronize()
             t0 = time.perf_counter()
-            self.sweeps[done:done + k] = st.solve(tol, chunk, max_sweeps)
+            self.sweeps[done:done + k] = st.solve(tol, chunk, max_sweeps, snaps)
             ps.synchronize()
             self.solve_seconds += time.perf_counter() - t0
             if self.pscale is None:
@@ -404,7 +453,17 @@ class Dataset:
                 lo = m * count + done
                 _ok(L.PSWarmStartPool(ctypes.byref(f), _p(self.x[lo:lo + k]), None))
                 _ok(L.PSWarmStartPoolTarget(ctypes.byref(f), _p(self.t[lo:lo + k]), None))
+            for j, (_, g) in enumerate(snaps):
+                scale = st.residual_source(1.0 / self.wscale, p=g)
+                for m, flip in enumerate(self.flips):
+                    f = st.fields(factor, self.wscale, self.pscale, True, flip,
+                                  wrk1=st.rgrid, inst_scale=scale, p_sub=g)
+                    lo = ((1 + j) * nm + m) * count + done
+                    _ok(L.PSWarmStartPool(ctypes.byref(f), _p(self.x[lo:lo + k]), None))
+                    _ok(L.PSWarmStartPoolTarget(ctypes.byref(f), _p(self.t[lo:lo + k]), None))
             ps.synchronize()
+            for _, g in snaps:
+                g.free()
             st.free()
             done += k
             if log:
@@ -450,13 +509,24 @@ def train(net, data, epochs, batch, lr, log=None, seed=0):
     return history, time.perf_counter() - t0
 
 
-def predict_into(net, stack, data_scales, factor, mirrors=1):
+def predict_into(net, stack, data_scales, factor, mirrors=1, restarts=0, nu=0):
     """Warm start: pool the stack's fields, run the network, upsample into
     the stack's p0 (p1 too, so the first sweep starts from it).  With
     mirrors > 1 the prediction is the mean of the network's predictions for
     that many mirror images of each instance, each mapped back to the
     instance (the network is not mirror-equivariant, so their errors partly
-    cancel)."""
+    cancel).
+
+    With restarts > 0, that many learned restarts follow: nu Jacobi sweeps
+    (nu even), then the network applied to the correction problem -- the
+    same coefficients with the current iterate's residual source r, scaled
+    per instance to the source's RMS -- and its prediction of the error
+    added to p0.  The equation is linear in the source, so the same network
+    predicts the solution and the correction; each restart divides the
+    error the network can see by roughly its relative accuracy, and the
+    sweeps between restarts remove the fine-scale part of the error that
+    the coarse grid cannot represent.  The sweeps are real iterations:
+    returns the number run (restarts * nu)."""
     import torch
     wscale, pscale = data_scales
     zc, yc, xc = coarse_shape(stack.shape, factor)
@@ -471,7 +541,22 @@ def predict_into(net, stack, data_scales, factor, mirrors=1):
         up = L.PSWarmStartUpsample if i == 0 else L.PSWarmStartUpsampleAdd
         for g in (stack.grids[0], stack.grids[1]):
             _ok(up(ctypes.byref(f), _p(pred), ctypes.c_void_p(g.dev_ptr), net.stream()))
+    used = 0
+    for _ in range(restarts):
+        torch.cuda.synchronize()
+        stack.sweeps(nu)
+        used += nu
+        scale = stack.residual_source(1.0 / wscale)
+        ps.synchronize()
+        for flip in flips:
+            f = stack.fields(factor, wscale, pscale * len(flips), flip=flip, wrk1=stack.rgrid,
+                             inst_scale=scale)
+            _ok(L.PSWarmStartPool(ctypes.byref(f), _p(x), net.stream()))
+            pred = net.forward(x, (n, zc, yc, xc))
+            _ok(L.PSWarmStartUpsampleAdd(ctypes.byref(f), _p(pred),
+                                         ctypes.c_void_p(stack.grids[0].dev_ptr), net.stream()))
     torch.cuda.synchronize()
+    return used
 
 
 def _time_forward(instances=1024, shape=(65, 33, 33), factor=4, reps=5):

@@ -10,8 +10,10 @@ that do not depend on the size.
     values stay inside the initial range times that factor; the FP64
     reduction equals a host FP64 sum; temporal blocking (k = 2) gives the same
     bits as the plain sweeps;
-  * contracted temporal passes stay within 1e-5 relative per cell over 200
-    steps.
+  * contracted temporal passes stay within 1e-5 relative per cell of the
+    plain (REF) result over 200 and 600 steps; over the whole 1000 steps
+    they drift to about 1.2e-5 (checked to stay under 2e-5), which is why
+    they are not reported as results of the 1000-step run.
 * Himeno 19-point, 257 x 257 x 513 float (the bench's set-up), 12 sweeps:
   every fused residual equals the oracle's FP64 residual of the same sweep,
   the pressure is bit-identical to the oracle's, and the plain sweep writes
@@ -106,6 +108,18 @@ def test_diffusion_512_cubed(rt, oracle):
     fused = run(k=2, fma=True, n_steps=200)
     plain200 = run(n_steps=200)
     assert np.allclose(fused, plain200, rtol=1e-5, atol=0)
+    # Longer runs: the plain sweeps are the REF sequence bit for bit (20
+    # steps against the oracle above, and temporal = plain bits), so this is
+    # the contracted pass against REF.  The drift keeps growing: within 1e-5
+    # at 600 steps, but 1.2e-5 after the benchmark's 1000 steps, so
+    # contracted passes are not reported as results of the 1000-step run.
+    fused = run(k=2, fma=True, n_steps=600)
+    plain600 = run(n_steps=600)
+    rel = float(np.max(np.abs(fused.astype(np.float64) - plain600) / np.abs(plain600)))
+    assert rel <= 1e-5, rel
+    fused = run(k=2, fma=True)
+    rel = float(np.max(np.abs(fused.astype(np.float64) - plain) / np.abs(plain)))
+    assert 1e-6 < rel <= 2e-5, rel
     g1.free()
     g2.free()
 
