@@ -245,3 +245,22 @@ def pool_features(inst, f, wscale):
              pool(w * 3.0 / (a0 + a1 + a2), f) * wscale,
              -np.log(pool(1.0 / a0, f)), -np.log(pool(1.0 / a1, f)), -np.log(pool(1.0 / a2, f))]
     return np.stack(feats, axis=-1)
+
+
+def residual_source(inst, p):
+    """Source of the correction problem for an iterate p of one instance
+    (arrays [z, y, x]): with c_i = a_i and b = 0 the Himeno residual is
+    ss = (s0 a3 - p) bnd, s0 = sum_i a_i (p(x + e_i) + p(x - e_i)) + wrk1,
+    a3 = 1 / (2 (a0 + a1 + a2)) (examples/himeno/himenobmtxpa_original.c:
+    331-334 with these coefficients), and r = ss / a3.  a0 weighs the z
+    neighbours, a1 the y and a2 the x neighbours.  Zero on the faces."""
+    a0, a1, a2 = (np.asarray(inst[k], np.float64) for k in ("a0", "a1", "a2"))
+    w, bnd = np.asarray(inst["wrk1"], np.float64), np.asarray(inst["bnd"], np.float64)
+    p = np.asarray(p, np.float64)
+    r = np.zeros_like(p)
+    i = (slice(1, -1),) * 3
+    s0 = (a0[i] * (p[2:, 1:-1, 1:-1] + p[:-2, 1:-1, 1:-1]) +
+          a1[i] * (p[1:-1, 2:, 1:-1] + p[1:-1, :-2, 1:-1]) +
+          a2[i] * (p[1:-1, 1:-1, 2:] + p[1:-1, 1:-1, :-2]) + w[i])
+    r[i] = (s0 - 2.0 * (a0[i] + a1[i] + a2[i]) * p[i]) * bnd[i]
+    return r

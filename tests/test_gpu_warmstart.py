@@ -242,6 +242,49 @@ def test_pool_and_upsample(rt, shape, flips):
     st.free()
 
 
+def test_residual_source_and_scales(rt):
+    # The correction problem's source r = ss / a3 of an iterate p, per cell,
+    # against the oracle (FP32 kernel, FP64 oracle: 1e-5 of max |r|), and the
+    # per-instance scales target_rms / rms(r) (1e-5 relative).
+    from physis_gb300 import warmstart as ws
+    rng = np.random.default_rng(11)
+    shape = (13, 9, 10)
+    insts = [ws.make_instance(rng, shape) for _ in range(5)]
+    st = ws.Stack(insts, shape, nsx=2)
+    p = rng.normal(size=st.gshape).astype(np.float32)
+    st.grids[0].copyin(p)
+    scale = st.residual_source(0.7)
+    ps.synchronize()
+    r = st.rgrid.copyout()
+    sc = scale.cpu().numpy()
+    for b, inst in enumerate(insts):
+        ref = nn.residual_source(inst, p[st.slot(b)])
+        got = r[st.slot(b)]
+        assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), b
+        n_in = (shape[0] - 2) * (shape[1] - 2) * (shape[2] - 2)
+        want = 0.7 / np.sqrt((ref ** 2).sum() / n_in)
+        assert abs(sc[b] - want) <= 1e-5 * want, (b, sc[b], want)
+    # pooled with the scales: the source channels carry r * scale, and the
+    # target of (p*, iterate) pairs is (p* - iterate) * scale
+    zc, yc, xc = ws.coarse_shape(shape, 4)
+    x = torch.empty(5 * zc * yc * xc * 16, dtype=torch.bfloat16, device="cuda")
+    f = st.fields(4, wscale=0.5, with_p=True, wrk1=st.rgrid, inst_scale=scale)
+    assert ps.lib().PSWarmStartPool(ctypes.byref(f), _p(x), None) == 0
+    st.grids[1].copyin(np.zeros(st.gshape, np.float32) + 0.25)
+    t = torch.empty(5 * zc * yc * xc, dtype=torch.float32, device="cuda")
+    f = st.fields(4, pscale=2.0, with_p=True, inst_scale=scale, p_sub=st.grids[1])
+    assert ps.lib().PSWarmStartPoolTarget(ctypes.byref(f), _p(t), None) == 0
+    ps.synchronize()
+    xs = _np_bf(x, (5, zc, yc, xc, 16))
+    tt = t.cpu().numpy().reshape(5, zc, yc, xc)
+    for b, inst in enumerate(insts):
+        ref3 = nn.pool(r[st.slot(b)].astype(np.float64), 4) * 0.5 * sc[b]
+        assert _within_one_bf16_step(xs[b, ..., 3], ref3), b
+        reft = nn.centre_sample(p[st.slot(b)].astype(np.float64) - 0.25, 4) * 2.0 * sc[b]
+        assert np.allclose(tt[b], reft, rtol=1e-5, atol=1e-5 * np.abs(reft).max())
+    st.free()
+
+
 def test_mirror_argument_checks(rt):
     # the x/y swap needs a square x-y section; flip codes are 0..15
     from physis_gb300 import warmstart as ws
