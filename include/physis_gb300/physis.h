@@ -49,9 +49,9 @@ extern "C" {
 typedef int32_t PSIndex;
 typedef int PSVectorInt[PS_MAX_DIM];
 
-/* include/physis/types.h:16-23 */
+/* include/physis/types.h:16-23 (PS_USER: grids of a user-defined struct) */
 typedef int PSType;
-enum PSPrimitiveType { PS_INT = 0, PS_LONG = 1, PS_FLOAT = 2, PS_DOUBLE = 3 };
+enum PSPrimitiveType { PS_INT = 0, PS_LONG = 1, PS_FLOAT = 2, PS_DOUBLE = 3, PS_USER = 4 };
 
 /* include/physis/reduce.h:16-21 */
 enum PSReduceOp { PS_MAX, PS_MIN, PS_SUM, PS_PROD };
@@ -150,6 +150,42 @@ PSGrid3DFloat PSGrid3DFloatNew(PSIndex nx, PSIndex ny, PSIndex nz, ...);
 PSGrid3DDouble PSGrid3DDoubleNew(PSIndex nx, PSIndex ny, PSIndex nz, ...);
 PSGrid3DInt PSGrid3DIntNew(PSIndex nx, PSIndex ny, PSIndex nz, ...);
 PSGrid3DLong PSGrid3DLongNew(PSIndex nx, PSIndex ny, PSIndex nz, ...);
+
+/* Grids of a user-defined element type (include/physis/physis_user.h:18-58,
+ * DeclareGrid{1,2,3}D(name, type)).  `DeclareGrid3D(Point, struct Point);`
+ * declares the handle type PSGrid3DPoint and PSGrid3DPointNew(nx, ny, nz),
+ * which makes a zero-filled grid of sizeof(struct Point)-byte elements
+ * (PSGridNewUtype).  Such grids are copied in and out like any other (dense
+ * host arrays of the struct), written element by element with __PSGridSet,
+ * and read and written by compiled stencil functions (PSStencilFunctionNew)
+ * whose source holds the struct definition and the same DeclareGrid line;
+ * PSGridGet(g, ...) there returns the struct and PSGridEmitUtype(g.member,
+ * v) writes one member of the point being computed.  Builtin stencils,
+ * point stencils and PSReduce take the primitive types only.  The elements
+ * are stored densely (no row padding), in the host layout. */
+void *PSGridNewUtype(size_t elem_size, int ndims, const PSIndex *dims);
+#define DeclareGrid1D(name, type)                                              \
+  typedef struct __PSGrid1D##name *PSGrid1D##name;                             \
+  static inline PSGrid1D##name PSGrid1D##name##New(PSIndex nx, ...) {          \
+    PSIndex d_[3] = {nx, 1, 1};                                                \
+    return (PSGrid1D##name)PSGridNewUtype(sizeof(type), 1, d_);                \
+  }                                                                            \
+  typedef int PS__DeclaredGrid1D##name
+#define DeclareGrid2D(name, type)                                              \
+  typedef struct __PSGrid2D##name *PSGrid2D##name;                             \
+  static inline PSGrid2D##name PSGrid2D##name##New(PSIndex nx, PSIndex ny, ...) { \
+    PSIndex d_[3] = {nx, ny, 1};                                               \
+    return (PSGrid2D##name)PSGridNewUtype(sizeof(type), 2, d_);                \
+  }                                                                            \
+  typedef int PS__DeclaredGrid2D##name
+#define DeclareGrid3D(name, type)                                              \
+  typedef struct __PSGrid3D##name *PSGrid3D##name;                             \
+  static inline PSGrid3D##name PSGrid3D##name##New(PSIndex nx, PSIndex ny, PSIndex nz, \
+                                                   ...) {                      \
+    PSIndex d_[3] = {nx, ny, nz};                                              \
+    return (PSGrid3D##name)PSGridNewUtype(sizeof(type), 3, d_);                \
+  }                                                                            \
+  typedef int PS__DeclaredGrid3D##name
 
 /* include/physis/physis_common.h:83-86 (libphysis_rt_cuda.cc:101-137). */
 void PSGridCopyin(void *g, const void *src_array);

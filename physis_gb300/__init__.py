@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libphysis_gb300.so")
 
 # enums of include/physis_gb300/physis.h
-PS_INT, PS_LONG, PS_FLOAT, PS_DOUBLE = 0, 1, 2, 3
+PS_INT, PS_LONG, PS_FLOAT, PS_DOUBLE, PS_USER = 0, 1, 2, 3, 4
 PS_MAX, PS_MIN, PS_SUM, PS_PROD = 0, 1, 2, 3
 PS_KERNEL_COPY = 1
 PS_KERNEL_DIFFUSION7 = 2
@@ -45,7 +45,7 @@ EXPORTED = """PSInit PSFinalize PSPrintInternalInfo
 PSGrid1DFloatNew PSGrid1DDoubleNew PSGrid1DIntNew PSGrid1DLongNew
 PSGrid2DFloatNew PSGrid2DDoubleNew PSGrid2DIntNew PSGrid2DLongNew
 PSGrid3DFloatNew PSGrid3DDoubleNew PSGrid3DIntNew PSGrid3DLongNew
-PSGridCopyin PSGridCopyout PSGridFree PSGridDim __PSGridSet __PSGridSetScalar PSGridSetV
+PSGridNewUtype PSGridCopyin PSGridCopyout PSGridFree PSGridDim __PSGridSet __PSGridSetScalar PSGridSetV
 PSDomain1DNew PSDomain2DNew PSDomain3DNew __PSStencilMap PSStencilRun PSReduce
 PSInitV PSGridNewV PSStencilMapV PSStencilRunV PSReduceGridV PSReduceKernelV
 PSReduceGridF64 PSGetLastError PSGetLastErrorString PSGetErrorName PSClearError
@@ -117,6 +117,8 @@ def lib():
     L.PSFinalize.argtypes = []
     L.PSGridNewV.argtypes = [i, i, ctypes.POINTER(ctypes.c_int32)]
     L.PSGridNewV.restype = vp
+    L.PSGridNewUtype.argtypes = [ctypes.c_size_t, i, ctypes.POINTER(ctypes.c_int32)]
+    L.PSGridNewUtype.restype = vp
     L.PSGridCopyin.argtypes = [vp, vp]
     L.PSGridCopyout.argtypes = [vp, vp]
     L.PSGridCopyinAsync.argtypes = [vp, vp]
@@ -252,7 +254,10 @@ class Grid:
         self.shape = shape
         dims = list(reversed(shape)) + [1] * (3 - len(shape))
         arr = (ctypes.c_int32 * 3)(*dims)
-        self.handle = lib().PSGridNewV(TYPE_OF[self.dtype], len(shape), arr)
+        if self.dtype.fields is not None:  # a struct: a user-defined element type
+            self.handle = lib().PSGridNewUtype(self.dtype.itemsize, len(shape), arr)
+        else:
+            self.handle = lib().PSGridNewV(TYPE_OF[self.dtype], len(shape), arr)
         if not self.handle:
             check()
             raise PSError(PS_ERR_OUT_OF_MEMORY, "grid allocation failed")

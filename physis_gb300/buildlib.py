@@ -18,6 +18,10 @@ LIB = os.path.join(HERE, "libphysis_gb300.so")
 SOURCES = ["runtime.cpp", "march.cpp", "stencil7.cu", "temporal7.cu", "himeno19.cu",
            "reduce.cu", "batch.cu", "points.cu", "jit.cpp", "nn.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Translation units whose kernels may contract multiply-adds (the warm-start
+# network's FP32 epilogues and elementwise kernels); every other unit is
+# compiled with contraction off.
+CONTRACTING = {"nn.cu"}
 
 
 def nvcc():
@@ -65,6 +69,11 @@ def _compile(src):
                                    for d in deps):
         return obj
     cmd = [nvcc()] + common_flags() + ["-c", path, "-o", obj]
+    if src not in CONTRACTING:
+        # Bit-exact sweeps: ptxas must not fuse a multiply and an add into
+        # an FMA.  Scalar mul.rn/add.rn are never fused, but packed
+        # mul.rn.f32x2/add.rn.f32x2 pairs are unless contraction is off.
+        cmd += ["-Xptxas", "--fmad=false"]
     if src.endswith(".cpp"):
         cmd += ["-x", "cu"]
     r = subprocess.run(cmd, capture_output=True, text=True)

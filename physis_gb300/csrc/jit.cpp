@@ -29,6 +29,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <regex>
 #include <string>
 #include <vector>
@@ -100,6 +101,7 @@ struct Driver {
   CUresult (*unload)(CUmodule) = nullptr;
   CUresult (*set_attr)(CUfunction, CUfunction_attribute, int) = nullptr;
   CUresult (*occupancy)(int *, CUfunction, int, size_t) = nullptr;
+  CUresult (*global)(CUdeviceptr *, size_t *, CUmodule, const char *) = nullptr;
 };
 Driver g_drv;
 
@@ -125,8 +127,9 @@ bool load_driver(std::string *err) {
   g_drv.set_attr = reinterpret_cast<decltype(g_drv.set_attr)>(sym("cuFuncSetAttribute"));
   g_drv.occupancy = reinterpret_cast<decltype(g_drv.occupancy)>(
       sym("cuOccupancyMaxActiveBlocksPerMultiprocessor"));
+  g_drv.global = reinterpret_cast<decltype(g_drv.global)>(sym("cuModuleGetGlobal"));
   g_drv.ok = g_drv.load && g_drv.get && g_drv.launch && g_drv.unload && g_drv.set_attr &&
-             g_drv.occupancy;
+             g_drv.occupancy && g_drv.global;
   if (!g_drv.ok) {
     cudaGetLastError();
     *err = "driver entry points for module loading are unavailable";
@@ -211,6 +214,14 @@ __device__ __forceinline__ T __ps_getp(const __PSGridDev<T> &g, int x, int y, in
 template <typename T> __device__ __forceinline__ int __ps_dim(const __PSGridDev<T> &g, int d) {
   return d == 0 ? g.nx : (d == 1 ? g.ny : g.nz);
 }
+// Grids of a user-defined element type: the source's own struct definition
+// and DeclareGrid line; PSGridEmitUtype(g.m, v) reaches __PS_EMITU as
+// __PS_EMITU((g).p[(g).cur].m, v) (the front end rewrites the call), i.e. a
+// store to member m of the point being computed.
+#define DeclareGrid1D(N, T) typedef __PSGridDev<T> PSGrid1D##N
+#define DeclareGrid2D(N, T) typedef __PSGridDev<T> PSGrid2D##N
+#define DeclareGrid3D(N, T) typedef __PSGridDev<T> PSGrid3D##N
+#define __PS_EMITU(lhs, v) ((void)((lhs) = (v)))
 #define PSGridGet(g, ...) __ps_get((g), __VA_ARGS__)
 #define PSGridGetPeriodic(g, ...) __ps_getp((g), __VA_ARGS__)
 #define PSGridEmit(g, v) ((void)((g).p[(g).cur] = (v)))
@@ -278,9 +289,24 @@ std::string trim(const std::string &s) {
   return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
 }
 
+// User grid types the source declares: "PSGrid3DPoint" -> (3, "struct Point").
+typedef std::map<std::string, std::pair<int, std::string>> UserGrids;
+
+UserGrids declared_grids(const std::string &src) {
+  UserGrids out;
+  static const std::regex re("\\bDeclareGrid([123])D\\s*\\(\\s*(\\w+)\\s*,\\s*([^)]*?)\\s*\\)");
+  for (auto it = std::sregex_iterator(src.begin(), src.end(), re); it != std::sregex_iterator();
+       ++it) {
+    const int rank = (*it)[1].str()[0] - '0';
+    out["PSGrid" + (*it)[1].str() + "D" + (*it)[2].str()] = {rank, trim((*it)[3].str())};
+  }
+  return out;
+}
+
 // Parses one parameter declaration ("const int x", "PSGrid3DFloat g1",
 // "float c") into p; false if its type is not one the front end knows.
-bool parse_param(const std::string &decl, JitParam *p, std::string *err) {
+bool parse_param(const std::string &decl, JitParam *p, std::string *err,
+                 const UserGrids &user = UserGrids()) {
   static const std::regex grid_re("^PSGrid([123])D(Float|Double|Int|Long)$");
   std::string d = " " + trim(decl) + " ";
   for (const char *q : {" const ", " register ", " volatile "}) {
@@ -301,6 +327,14 @@ bool parse_param(const std::string &decl, JitParam *p, std::string *err) {
   p->decl_type = type;
   p->name = trim(d.substr(cut + 1));
   std::smatch m;
+  const auto u = user.find(type);
+  if (u != user.end()) {
+    p->grid = true;
+    p->rank = u->second.first;
+    p->type = kUser;
+    p->utype = u->second.second;
+    return true;
+  }
   if (std::regex_match(type, m, grid_re)) {
     p->grid = true;
     p->rank = m[1].str()[0] - '0';
@@ -356,9 +390,10 @@ bool parse_signature(const std::string &src, const std::string &name, JitKernel 
   k->params.clear();
   k->nd = 0;
   bool seen_grid = false;
+  const UserGrids user = declared_grids(src);
   for (const std::string &d : decls) {
     JitParam p;
-    if (!parse_param(d, &p, err)) return false;
+    if (!parse_param(d, &p, err, user)) return false;
     if (!p.grid && !seen_grid && p.type == kInt && k->params.empty() && k->nd < 3) {
       k->idx[k->nd++] = p.name;  // a leading index parameter
       continue;
@@ -392,6 +427,11 @@ std::string scalar_ctype(int type) {
   }
 }
 
+// A grid parameter's element type in generated code.
+std::string elem_ctype(const JitParam &p) {
+  return p.type == kUser ? p.utype : scalar_ctype(p.type);
+}
+
 // Source expression of the grid argument arg in an entry: the device view
 // g<i> the entry built from kernel parameter a<i>.
 std::string cur_expr(const JitParam &p, const std::string &g) {
@@ -404,7 +444,7 @@ std::string entry_params(const JitKernel &k) {
   std::string s;
   for (size_t i = 0; i < k.params.size(); ++i) {
     const JitParam &p = k.params[i];
-    s += ", " + (p.grid ? "__PSGridArg<" + scalar_ctype(p.type) + ">" : scalar_ctype(p.type)) +
+    s += ", " + (p.grid ? "__PSGridArg<" + elem_ctype(p) + ">" : scalar_ctype(p.type)) +
          " a" + std::to_string(i);
   }
   return s;
@@ -511,7 +551,7 @@ void choose_stages(JitKernel *k) {
   const std::string &src = k->source;
   std::vector<std::string> emitted;
   {
-    const std::regex emit_re("\\bPSGridEmit\\s*\\(\\s*(\\w+)");
+    const std::regex emit_re("\\bPSGridEmit(?:Utype)?\\s*\\(\\s*(\\w+)");
     for (auto it = std::sregex_iterator(src.begin(), src.end(), emit_re);
          it != std::sregex_iterator(); ++it)
       emitted.push_back((*it)[1].str());
@@ -519,7 +559,7 @@ void choose_stages(JitKernel *k) {
   const std::regex get_re("\\bPSGridGet(Periodic)?\\s*\\(");
   for (size_t pi = 0; pi < k->params.size(); ++pi) {
     const JitParam &p = k->params[pi];
-    if (!p.grid || p.rank != 3) continue;
+    if (!p.grid || p.rank != 3 || p.type == kUser) continue;
     bool is_emitted = false;
     for (const std::string &e : emitted) is_emitted |= (e == p.name);
     if (is_emitted) continue;
@@ -655,6 +695,24 @@ std::string tiled_entry_source(const JitKernel &k) {
 
 namespace {
 
+// PSGridEmitUtype(g.member, v) -> __PS_EMITU((g).p[(g).cur].member, v): the
+// member expression is applied to the point being computed.
+std::string rewrite_emit_utype(const std::string &src) {
+  static const std::regex re("\\bPSGridEmitUtype\\s*\\(\\s*([A-Za-z_]\\w*)");
+  return std::regex_replace(src, re, "__PS_EMITU(($1).p[($1).cur]");
+}
+
+// One device global per user-type grid parameter holding its element size,
+// read back after loading to check the grids a map passes.
+std::string utype_sizes_source(const JitKernel &k) {
+  std::string s;
+  for (size_t i = 0; i < k.params.size(); ++i)
+    if (k.params[i].grid && k.params[i].type == kUser)
+      s += "extern \"C\" __device__ const int __ps_esz" + std::to_string(i) +
+           " = (int)sizeof(" + k.params[i].utype + ");\n";
+  return s;
+}
+
 // Compiles one program text for sm_103a (headers: ps_arith.cuh).
 bool nvrtc_compile(const std::string &program, std::vector<char> *image, std::string *log) {
   nvrtcProgram_t prog = nullptr;
@@ -693,8 +751,9 @@ bool jit_build(const char *source, const char *name, JitKernel *k, std::vector<c
   k->source = source;
   if (!parse_signature(k->source, k->name, k, err)) return false;
   choose_stages(k);
-  const std::string base =
-      std::string(kPrelude) + "#line 1 \"stencil\"\n" + k->source + "\n" + entry_source(*k);
+  const std::string base = std::string(kPrelude) + "#line 1 \"stencil\"\n" +
+                           rewrite_emit_utype(k->source) + "\n" + entry_source(*k) +
+                           utype_sizes_source(*k);
   std::string log;
   // PS_JIT_DUMP=<dir> writes the generated program to <dir>/<name>.cu (for
   // building it offline with nvcc to read its resource usage).
@@ -745,6 +804,25 @@ bool jit_compile(const char *source, const char *name, JitKernel *k, std::string
                k->tiled_occ < 1)) {
     k->tiled_occ = 0;
     fn_t = nullptr;
+  }
+  // element sizes of the user-type grid parameters, as the compiler laid
+  // the structs out
+  for (size_t i = 0; i < k->params.size(); ++i) {
+    JitParam &p = k->params[i];
+    if (!p.grid || p.type != kUser) continue;
+    CUdeviceptr dptr = 0;
+    size_t bytes = 0;
+    int esz = 0;
+    const std::string sym = "__ps_esz" + std::to_string(i);
+    if (g_drv.global(&dptr, &bytes, mod, sym.c_str()) != CUDA_SUCCESS || bytes != sizeof(int) ||
+        cudaMemcpy(&esz, reinterpret_cast<void *>(dptr), sizeof(int), cudaMemcpyDeviceToHost) !=
+            cudaSuccess) {
+      cudaGetLastError();
+      g_drv.unload(mod);
+      *err = "cannot read the element size of " + p.utype;
+      return false;
+    }
+    p.esz = esz;
   }
   k->module = mod;
   k->func = fn;

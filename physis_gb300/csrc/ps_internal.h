@@ -12,7 +12,7 @@
 namespace psg {
 
 // PSPrimitiveType values (include/physis/types.h:16-23 in the reference).
-enum ElemType { kInt = 0, kLong = 1, kFloat = 2, kDouble = 3 };
+enum ElemType { kInt = 0, kLong = 1, kFloat = 2, kDouble = 3, kUser = 4 };
 // PSReduceOp values (include/physis/reduce.h:16-21 in the reference).
 enum ReduceOp { kMax = 0, kMin = 1, kSum = 2, kProd = 3 };
 
@@ -150,6 +150,8 @@ struct JitParam {
   int rank;               // grids: 1..3
   std::string decl_type;  // the type as declared ("PSGrid3DFloat", "float")
   std::string name;       // the parameter's name
+  std::string utype;      // kUser grids: the element type (DeclareGrid's "struct Point")
+  int esz = 0;            // kUser grids: its size in bytes (read from the module; 0 unknown)
 };
 // A grid the tiled entry stages in shared memory: planes of (64 + 2 rxw) x
 // (16 + 2 ry) cells around the CTA's tile (rxw: rx rounded up to 16 bytes),

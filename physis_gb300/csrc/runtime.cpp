@@ -201,6 +201,8 @@ Grid *as_grid(void *g, const char *fn) {
   return p;
 }
 
+constexpr int kMaxUserElem = 4096;  // bytes per user-type element
+
 int esize(int type) {
   switch (type) {
     case PS_INT: return 4;
@@ -432,6 +434,10 @@ bool validate_function_map(const Map &m, const psg::JitKernel &f) {
       return fail(PS_ERR_INVALID_ARGUMENT,
                   "%s: grid argument %d is a %dD grid of type %d, the parameter is %s",
                   f.name.c_str(), gi - 1, g->ndims, g->type, p.decl_type.c_str());
+    if (p.type == PS_USER && p.esz > 0 && g->esz != p.esz)
+      return fail(PS_ERR_INVALID_ARGUMENT,
+                  "%s: grid argument %d has %d-byte elements, the parameter's type (%s) "
+                  "has %d", f.name.c_str(), gi - 1, g->esz, p.utype.c_str(), p.esz);
     if (p.rank != f.nd) continue;
     for (int d = 0; d < 3; ++d)
       if (m.dom.min[d] < m.dom.max[d] &&
@@ -454,6 +460,10 @@ bool validate_map(const Map &m) {
     return fail(PS_ERR_UNKNOWN_KERNEL, "unknown builtin stencil id %d", m.kernel);
   if (sig.fn) return validate_function_map(m, *sig.fn);
   const Grid *g0 = m.grids[0];
+  if (g0->type == PS_USER)
+    return fail(PS_ERR_UNSUPPORTED,
+                "%s: grids of a user-defined type run compiled stencil functions only",
+                sig.name);
   for (const Grid *g : m.grids) {
     if (g->type != g0->type || g->dim[0] != g0->dim[0] || g->dim[1] != g0->dim[1] ||
         g->dim[2] != g0->dim[2])
@@ -696,9 +706,15 @@ bool run_temporal(const Map &a, int iter) {
   return true;
 }
 
-void *grid_new(int type, int ndims, const PSIndex *dims) {
+// esz_user: element size of a PS_USER grid (ignored for the primitive types).
+void *grid_new(int type, int ndims, const PSIndex *dims, size_t esz_user = 0) {
   if (!need_rt("PSGrid*New")) return nullptr;
-  const int esz = esize(type);
+  const int esz = type == PS_USER ? (int)esz_user : esize(type);
+  if (type == PS_USER && (esz_user < 1 || esz_user > kMaxUserElem)) {
+    fail(PS_ERR_INVALID_ARGUMENT, "user element size %zu not in 1..%d", esz_user,
+         kMaxUserElem);
+    return nullptr;
+  }
   if (!esz) {
     fail(PS_ERR_INVALID_ARGUMENT, "unknown grid element type %d", type);
     return nullptr;
@@ -715,7 +731,11 @@ void *grid_new(int type, int ndims, const PSIndex *dims) {
     }
     dim[d] = dims[d];
   }
-  const size_t pitch = (((size_t)dim[0] * esz) + 127) / 128 * 128;
+  // Rows of the primitive types start on 128-byte boundaries (TMA boxes,
+  // 16-byte vectors); user-type rows are dense, so that an element index
+  // times the element size addresses any element.
+  const size_t pitch = type == PS_USER ? (size_t)dim[0] * esz
+                                       : (((size_t)dim[0] * esz) + 127) / 128 * 128;
   const size_t bytes = pitch * (size_t)dim[1] * (size_t)dim[2];
   void *dev = nullptr;
   if (rt->fail_allocs > 0) {
@@ -1327,6 +1347,7 @@ bool batch_build(Batch &b) {
         q.ct = has ? (float)c[4] : 0.f;
         q.cb = has ? (float)c[5] : 0.f;
         q.cc = has ? (float)c[6] : 0.f;
+        psg::s7_pack_coefs(q);
         q.err = rt->dev_err;
       }
     }
@@ -1408,6 +1429,8 @@ bool read_result(int slot, uint64_t *bits) {
 bool reduce_grid(Grid *g, int op, uint64_t *bits) {
   if (op < PS_MAX || op > PS_PROD)
     return fail(PS_ERR_INVALID_ARGUMENT, "unknown reduction op %d", op);
+  if (g->type == PS_USER)
+    return fail(PS_ERR_UNSUPPORTED, "PSReduce: grids of a user-defined type are not reduced");
   const GridView v = view(g);
   const int n = psg::reduce_num_ctas(v, rt->sm_count);
   if (n > kMaxPartials) return fail(PS_ERR_UNSUPPORTED, "reduction grid too large");
@@ -1640,7 +1663,19 @@ void PSPrintInternalInfo(FILE *out) {
 }
 
 void *PSGridNewV(int type, int ndims, const PSIndex *dims) {
+  if (type == PS_USER) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSGridNewV: user-type grids come from PSGridNewUtype");
+    return nullptr;
+  }
   return grid_new(type, ndims, dims);
+}
+
+void *PSGridNewUtype(size_t elem_size, int ndims, const PSIndex *dims) {
+  if (!dims) {
+    fail(PS_ERR_INVALID_ARGUMENT, "PSGridNewUtype: NULL dims");
+    return nullptr;
+  }
+  return grid_new(PS_USER, ndims, dims, elem_size);
 }
 
 #define PS_DEFINE_NEW(RANK, NAME, TYPE, ...)                 \
@@ -1752,6 +1787,11 @@ void __PSGridSetScalar(void *g, int nidx, PSIndex i, PSIndex j, PSIndex k, int i
                        double vf, long long vi) {
   Grid *p = as_grid(g, "PSGridSet");
   if (!p) return;
+  if (p->type == PS_USER) {
+    fail(PS_ERR_INVALID_ARGUMENT,
+         "PSGridSet: a user-type grid takes __PSGridSet(g, &value, indices...)");
+    return;
+  }
   if (nidx != p->ndims) {
     fail(PS_ERR_INVALID_ARGUMENT, "PSGridSet: %d indices for a %d-dimensional grid", nidx,
          p->ndims);

@@ -62,6 +62,15 @@ MANUAL_TESTS = [
     "test_mixed-dim",
     "test_mixed-dim2",
     "test_mixed-dim3",
+    # grids of user-defined struct types
+    "test_user-defined-type-7-pt",
+    "test_user-defined-type-7-pt-periodic",
+    "test_user-defined-type-7-pt-periodic-complex",
+    "test_user-defined-type-multi-dim-member",
+    "test_user-defined-type-multi-members",
+    "test_user-defined-type1",
+    "test_user-defined-type3",
+    "test_user-defined-type5",
 ]
 
 DIFF_N, DIFF_COUNT = 21, 6

@@ -113,3 +113,27 @@ def test_staging_decisions_and_compiles(built, src, name, staged):
         pytest.skip("NVRTC not available: " + log)
     assert code == ps.PS_OK, log
     assert log == staged
+
+
+# Stencil functions over grids of user-defined struct types: they compile
+# for sm_103a, and no user-type grid is staged (PSGridEmitUtype counts as an
+# emit, and struct elements are not staged at all).
+import test_gpu_user_types as ut  # noqa: E402
+
+USER = [(ut.SEVEN_PT, "seven"), (ut.COMPLEX, "csum"), (ut.ARRAY_MEMBER, "am"),
+        (ut.MULTI_DIM, "md"), (ut.MULTI_MEMBERS, "mm"), (ut.XYZ, "xyz"), (ut.PQR, "k1"),
+        (ut.PQR, "k2")]
+
+
+@pytest.mark.parametrize("src,name", USER, ids=[u[1] for u in USER])
+def test_user_type_functions_compile_unstaged(built, src, name):
+    code, log = ps.stencil_function_check(src, name)
+    if code == ps.PS_ERR_UNSUPPORTED:
+        pytest.skip("NVRTC not available: " + log)
+    assert code == ps.PS_OK, log
+    assert "staged" not in log, log
+
+
+def test_user_type_c_program_compiles_and_links(built, tmp_path):
+    from test_abi import compile_c_program
+    assert compile_c_program(tmp_path, ut.C_UTYPE_PROGRAM, "utype").exists()
