@@ -70,9 +70,9 @@ def _compile(src):
         return obj
     cmd = [nvcc()] + common_flags() + ["-c", path, "-o", obj]
     if src not in CONTRACTING:
-        # Bit-exact sweeps: ptxas must not fuse a multiply and an add into
-        # an FMA.  Scalar mul.rn/add.rn are never fused, but packed
-        # mul.rn.f32x2/add.rn.f32x2 pairs are unless contraction is off.
+        # Bit-exact sweeps: no multiply-add contraction anywhere in these
+        # units (their arithmetic is explicit round-to-nearest already; this
+        # keeps any plain expression from being fused too).
         cmd += ["-Xptxas", "--fmad=false"]
     if src.endswith(".cpp"):
         cmd += ["-x", "cu"]
