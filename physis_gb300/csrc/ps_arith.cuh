@@ -54,59 +54,6 @@ struct RN<long long> {
   static __device__ __forceinline__ long long mul(long long a, long long b) { return (long long)((U)a * (U)b); }
 };
 
-// Packed pairs of floats (sm_100-family f32x2 arithmetic): one instruction
-// rounds two independent products, each exactly as the scalar
-// round-to-nearest multiply would.  A packed multiply whose result feeds a
-// packed add is fused into a packed FMA by the assembler (a probe of random
-// operands on GB300 found 31 % of results off by an ulp, with or without
-// --fmad=false), but a packed multiply feeding scalar adds is not: the bit-
-// exact kernels below pair the products and keep the sums scalar.
-typedef unsigned long long f32x2_t;
-__device__ __forceinline__ f32x2_t f2_pack(float lo, float hi) {
-  f32x2_t r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ void f2_unpack(f32x2_t v, float &lo, float &hi) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f32x2_t f2_mul(f32x2_t a, f32x2_t b) {
-  f32x2_t r;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-
-// The 7-point diffusion cc*c + cw*w + ce*e + cs*s + cn*n + cb*b + ct*t,
-// left to right, for four cells: the products two cells per instruction,
-// the sums one cell at a time (round-to-nearest, never fused).  k2 holds the
-// seven coefficients each packed twice (cc, cw, ce, cs, cn, cb, ct);
-// w/e/n/s/b/t are the cells' neighbours with any clamping already applied.
-__device__ __forceinline__ void diffuse7_x4(const float (&c)[4], const float (&w)[4],
-                                            const float (&e)[4], const float (&s)[4],
-                                            const float (&n)[4], const float (&b)[4],
-                                            const float (&t)[4], const f32x2_t (&k2)[7],
-                                            float (&o)[4]) {
-#pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int i = 2 * h;
-    float m[7][2];
-    f2_unpack(f2_mul(k2[0], f2_pack(c[i], c[i + 1])), m[0][0], m[0][1]);
-    f2_unpack(f2_mul(k2[1], f2_pack(w[i], w[i + 1])), m[1][0], m[1][1]);
-    f2_unpack(f2_mul(k2[2], f2_pack(e[i], e[i + 1])), m[2][0], m[2][1]);
-    f2_unpack(f2_mul(k2[3], f2_pack(s[i], s[i + 1])), m[3][0], m[3][1]);
-    f2_unpack(f2_mul(k2[4], f2_pack(n[i], n[i + 1])), m[4][0], m[4][1]);
-    f2_unpack(f2_mul(k2[5], f2_pack(b[i], b[i + 1])), m[5][0], m[5][1]);
-    f2_unpack(f2_mul(k2[6], f2_pack(t[i], t[i + 1])), m[6][0], m[6][1]);
-#pragma unroll
-    for (int l = 0; l < 2; ++l) {
-      float v = m[0][l];
-#pragma unroll
-      for (int j = 1; j < 7; ++j) v = __fadd_rn(v, m[j][l]);
-      o[i + l] = v;
-    }
-  }
-}
-
 // Error bits written into the runtime's device error word.
 enum : int {
   kDevErrWaitTimeout = 1,  // an mbarrier wait ran past its iteration limit

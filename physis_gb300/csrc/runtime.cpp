@@ -1347,7 +1347,6 @@ bool batch_build(Batch &b) {
         q.ct = has ? (float)c[4] : 0.f;
         q.cb = has ? (float)c[5] : 0.f;
         q.cc = has ? (float)c[6] : 0.f;
-        psg::s7_pack_coefs(q);
         q.err = rt->dev_err;
       }
     }

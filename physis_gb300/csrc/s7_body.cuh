@@ -3,9 +3,6 @@
 // marched over planes [zs, ze).  See stencil7.cu for the design.
 #pragma once
 
-#include <cstring>
-#include <type_traits>
-
 #include "ps_device.cuh"
 #include "ps_internal.h"
 
@@ -25,21 +22,8 @@ struct S7Params {
   int64_t items;  // tiles * chunks
   int ns;
   T cc, cw, ce, cs, cn, cb, ct;  // expression order of DIFFUSION7
-  f32x2_t k2[7];  // float grids: (cc, cw, ce, cs, cn, cb, ct), each packed twice
   int *err;
 };
-
-// Fills p.k2 from the scalar coefficients (host side; float grids use it).
-template <typename T>
-inline void s7_pack_coefs(S7Params<T> &p) {
-  const T kc[7] = {p.cc, p.cw, p.ce, p.cs, p.cn, p.cb, p.ct};
-  for (int i = 0; i < 7; ++i) {
-    const float f = (float)kc[i];
-    uint32_t u;
-    memcpy(&u, &f, 4);
-    p.k2[i] = ((f32x2_t)u << 32) | u;
-  }
-}
 
 __host__ __device__ constexpr int s7_bar_bytes(int ns) { return 128 * ((8 * ns + 127) / 128); }
 __host__ __device__ constexpr uint32_t s7_stage_bytes(uint32_t b) { return (b + 127u) & ~127u; }
@@ -165,17 +149,6 @@ __device__ __forceinline__ bool s7_item(const CUtensorMap *tin, const S7Params<T
         T right = shfl_down1(c[r][0]);
         if (lane == 0) left = cur[cen0 + r * W - 1];
         if (lane == 31) right = cur[cen0 + r * W + VEC];
-        if constexpr (std::is_same<T, float>::value && kClamp) {
-          // bit-identical to the scalar form below, two cells per instruction
-          float w[4], e[4];
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            w[i] = (i == 0) ? (west_face ? c[r][0] : left) : c[r][i - 1];
-            e[i] = (i == 3) ? right : c[r][i + 1];
-            if (i == east_elem) e[i] = c[r][i];
-          }
-          diffuse7_x4(c[r], w, e, ss, nn, b[r], t[r], p.k2, o);
-        } else
 #pragma unroll
         for (int i = 0; i < VEC; ++i) {
           T w = (i == 0) ? left : c[r][i - 1];

@@ -141,7 +141,6 @@ cudaError_t launch_t(const Stencil7Args &a, const MarchConfig &cfg,
   p.ct = (T)a.coef[4];
   p.cb = (T)a.coef[5];
   p.cc = (T)a.coef[6];
-  s7_pack_coefs(p);
   p.err = dev_err;
   const int ex = a.dom.max[0] - p.xbase;
   const int ey = a.dom.max[1] - a.dom.min[1];

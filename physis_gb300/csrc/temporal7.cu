@@ -28,7 +28,6 @@
 // __syncthreads per step separates a slot's writes from its next reads.
 // Work items are (z-chunk, tile) pairs in chunk-major order taken
 // round-robin by a persistent grid (as in stencil7.cu).
-#include <cstring>
 #include <type_traits>
 
 #include "ps_device.cuh"
@@ -47,7 +46,6 @@ struct TParams {
   int64_t items;
   int ns;
   T cc, cw, ce, cs, cn, cb, ct;
-  f32x2_t k2[7];  // float: (cc, cw, ce, cs, cn, cb, ct), each packed twice
   int *err;
 };
 
@@ -63,21 +61,6 @@ __device__ __forceinline__ void diffuse_row(const T (&c)[VEC], const T (&n)[VEC]
                                             bool west_face, int east_elem,
                                             const TParams<T> &p, T (&o)[VEC]) {
   typedef RN<T> R;
-  if constexpr (std::is_same<T, float>::value && !FMA) {
-    // bit-identical to the scalar form below, two cells per instruction
-    float w[4], e[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      w[i] = (i == 0) ? left : c[i - 1];
-      e[i] = (i == 3) ? right : c[i + 1];
-      if (CLAMP) {
-        if (i == 0 && west_face) w[i] = c[0];
-        if (i == east_elem) e[i] = c[i];
-      }
-    }
-    diffuse7_x4(c, w, e, s, n, b, t, p.k2, o);
-    return;
-  }
 #pragma unroll
   for (int i = 0; i < VEC; ++i) {
     T w = (i == 0) ? left : c[i - 1];
@@ -413,16 +396,6 @@ cudaError_t launch_t(const Temporal7Args &a, const MarchConfig &cfg, const CUten
   p.ct = (T)a.coef[4];
   p.cb = (T)a.coef[5];
   p.cc = (T)a.coef[6];
-  {
-    // the float coefficients, each packed twice (low half first)
-    const T kc[7] = {p.cc, p.cw, p.ce, p.cs, p.cn, p.cb, p.ct};
-    for (int i = 0; i < 7; ++i) {
-      const float f = (float)kc[i];
-      uint32_t u;
-      memcpy(&u, &f, 4);
-      p.k2[i] = ((f32x2_t)u << 32) | u;
-    }
-  }
   p.err = dev_err;
   if (cfg.warps < 1 || cfg.warps > 8 || cfg.ns < 2 || cfg.ns > 16)
     return cudaErrorInvalidConfiguration;
