@@ -60,7 +60,8 @@ PSSetBatchShape __PSStencilMapRedBlack __PSStencilMapRed __PSStencilMapBlack
 PSStencilMapColorV PSPointStencilNew PSStencilFunctionNew
 PSStencilFunctionCheck PSWarmStartConv PSWarmStartWeightGrad PSWarmStartPrepareWeights
 PSWarmStartAdam PSWarmStartLoss PSWarmStartPool PSWarmStartPoolTarget
-PSWarmStartUpsample PSWarmStartUpsampleAdd PSWarmStartResidualSource""".split()
+PSWarmStartUpsample PSWarmStartUpsampleAdd PSWarmStartResidualSource
+PSWarmStartAddCorrection""".split()
 
 
 class PSDomain(ctypes.Structure):
@@ -199,10 +200,11 @@ def lib():
     L.PSWarmStartUpsample.argtypes = [fp, vp, vp, vp]
     L.PSWarmStartUpsampleAdd.argtypes = [fp, vp, vp, vp]
     L.PSWarmStartResidualSource.argtypes = [fp, vp, vp, ctypes.c_float, vp, i, vp]
+    L.PSWarmStartAddCorrection.argtypes = [fp, vp, vp, vp]
     for name in ("PSWarmStartConv", "PSWarmStartWeightGrad", "PSWarmStartPrepareWeights",
                  "PSWarmStartAdam", "PSWarmStartLoss", "PSWarmStartPool",
                  "PSWarmStartPoolTarget", "PSWarmStartUpsample", "PSWarmStartUpsampleAdd",
-                 "PSWarmStartResidualSource"):
+                 "PSWarmStartResidualSource", "PSWarmStartAddCorrection"):
         getattr(L, name).restype = i
     _lib = L
     return L

@@ -673,6 +673,20 @@ __global__ void residual_source_kernel(PoolArgs a, float *__restrict__ r,
   if (threadIdx.x == 0) part[(long long)b * gridDim.x + blockIdx.x] = red[0];
 }
 
+// p += delta at every cell of every instance (stored layout): one rounding
+// of p per restart, whatever number of mirror predictions delta sums.
+__global__ void add_correction_kernel(PoolArgs a, const float *__restrict__ delta,
+                                      float *__restrict__ p) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = (long long)a.batch * a.inz * a.iny * a.inx;
+  if (i >= n) return;
+  const int x = (int)(i % a.inx), y = (int)((i / a.inx) % a.iny);
+  const int z = (int)((i / ((long long)a.inx * a.iny)) % a.inz);
+  const int b = (int)(i / ((long long)a.inx * a.iny * a.inz));
+  const long long k = fine_index(a, b, z, y, x);
+  p[k] = p[k] + delta[k];
+}
+
 // scale[b] = target_rms / rms(r of instance b) over its interior cells
 // (0 when r vanishes); the partials are summed in a fixed order.
 __global__ void inst_scale_kernel(const double *__restrict__ part, int G, int batch,
@@ -822,6 +836,14 @@ int nn_residual_source(const NNFields &f, float *r, float *inst_scale, float tar
   const long long cells = (long long)(a.inz - 2) * (a.iny - 2) * (a.inx - 2);
   inst_scale_kernel<<<(unsigned)((a.batch + 127) / 128), 128, 0, s>>>(
       work, g, a.batch, cells > 0 ? cells : 1, target_rms, inst_scale);
+  return (int)cudaGetLastError();
+}
+
+int nn_add_correction(const NNFields &f, const float *delta, float *p, cudaStream_t s) {
+  const PoolArgs a = pool_args(f);
+  const long long n = (long long)a.batch * a.inz * a.iny * a.inx;
+  if (n <= 0 || !delta || !p) return -1;
+  add_correction_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, delta, p);
   return (int)cudaGetLastError();
 }
 

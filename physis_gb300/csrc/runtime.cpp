@@ -2415,6 +2415,14 @@ int PSWarmStartResidualSource(const PSWarmStartFields *f, float *r, float *inst_
                    "PSWarmStartResidualSource");
 }
 
+int PSWarmStartAddCorrection(const PSWarmStartFields *f, const float *delta, float *p,
+                             void *stream) {
+  if (!ws_fields_ok(f, "PSWarmStartAddCorrection", false) || !delta || !p || f->flip != 0)
+    return ws_status(-1, "PSWarmStartAddCorrection");
+  return ws_status(psg::nn_add_correction(ws_fields(f), delta, p, ws_stream(stream)),
+                   "PSWarmStartAddCorrection");
+}
+
 int PSWarmStartPoolTarget(const PSWarmStartFields *f, float *out, void *stream) {
   if (!ws_fields_ok(f, "PSWarmStartPoolTarget", true) || !out) return PS_ERR_INVALID_ARGUMENT;
   return ws_status(psg::nn_pool_target(ws_fields(f), out, ws_stream(stream)),

@@ -548,13 +548,19 @@ def predict_into(net, stack, data_scales, factor, mirrors=1, restarts=0, nu=0):
         used += nu
         scale = stack.residual_source(1.0 / wscale)
         ps.synchronize()
-        for flip in flips:
+        # the mirror predictions summed into a scratch grid, then added to
+        # the iterate with a single rounding
+        for i, flip in enumerate(flips):
             f = stack.fields(factor, wscale, pscale * len(flips), flip=flip, wrk1=stack.rgrid,
                              inst_scale=scale)
             _ok(L.PSWarmStartPool(ctypes.byref(f), _p(x), net.stream()))
             pred = net.forward(x, (n, zc, yc, xc))
-            _ok(L.PSWarmStartUpsampleAdd(ctypes.byref(f), _p(pred),
-                                         ctypes.c_void_p(stack.grids[0].dev_ptr), net.stream()))
+            up = L.PSWarmStartUpsample if i == 0 else L.PSWarmStartUpsampleAdd
+            _ok(up(ctypes.byref(f), _p(pred), ctypes.c_void_p(stack.scratch.dev_ptr),
+                   net.stream()))
+        f = stack.fields(factor)
+        _ok(L.PSWarmStartAddCorrection(ctypes.byref(f), ctypes.c_void_p(stack.scratch.dev_ptr),
+                                       ctypes.c_void_p(stack.grids[0].dev_ptr), net.stream()))
     torch.cuda.synchronize()
     return used
 
