@@ -1207,7 +1207,8 @@ def run_gpu_warmstart(args, dist):
     counts, r_start = {}, {}
     for name, k in modes.items():
         reset()
-        used = ws.predict_into(net, st, scales, factor, pm, restarts=k, nu=nu)
+        used = ws.predict_into(net, st, scales, factor, pm, restarts=k, nu=nu,
+                               restart_mirrors=args.ws_restart_mirrors)
         r_start[name] = st.residuals()
         c = st.solve(1e-6, echunk, args.ws_max_sweeps)
         counts[name] = np.where(c > 0, c + used, c)
@@ -1223,7 +1224,8 @@ def run_gpu_warmstart(args, dist):
         torch.cuda.synchronize()
         t = time.perf_counter()
         if k is not None:
-            ws.predict_into(net, st, scales, factor, pm, restarts=k, nu=nu)
+            ws.predict_into(net, st, scales, factor, pm, restarts=k, nu=nu,
+                            restart_mirrors=args.ws_restart_mirrors)
         st.sweeps(n)
         ps.synchronize()
         return time.perf_counter() - t
@@ -1353,7 +1355,7 @@ def main():
                     help="batch workload with 48 small grids (launch-bound regime)")
     ap.add_argument("--workload", default="diffusion",
                     choices=["diffusion", "himeno", "batch", "points27", "points7",
-                             "function7", "function27", "warmstart"],
+                             "function7", "function27", "warmstart", "reduce"],
                     help="diffusion: 7-point 512^3 (the headline); himeno: "
                          "19-point Jacobi 257x257x513 with fused residual")
     ap.add_argument("--temporal", type=int, default=1,
@@ -1380,6 +1382,8 @@ def main():
     ap.add_argument("--ws-max-sweeps", type=int, default=12000)
     ap.add_argument("--ws-restarts", type=int, default=3,
                     help="warm start: learned restarts after the prediction (0: single shot)")
+    ap.add_argument("--ws-restart-mirrors", type=int, default=1,
+                    help="warm start: mirror images averaged in each restart's prediction")
     ap.add_argument("--ws-nu", type=int, default=32,
                     help="warm start: Jacobi sweeps before each learned restart (even)")
     ap.add_argument("--ws-snapshots", default="32,128,512,2048",
@@ -1403,6 +1407,13 @@ def main():
             run_gpu_batch(args, dist)
         elif args.workload == "warmstart":
             run_gpu_warmstart(args, dist)
+        elif args.workload == "reduce":
+            os.environ.setdefault("PS_DEVICE", str(dist.local))
+            import physis_gb300 as ps
+            ps.init()
+            out = reduce_measure(ps, reps=max(args.steps, 3), cpu=not args.no_cpu_baseline)
+            if dist.rank == 0:
+                print(json.dumps(out), flush=True)
         elif args.workload in ("points27", "points7", "function7", "function27"):
             run_gpu_points(args, dist)
         else:

@@ -509,7 +509,8 @@ def train(net, data, epochs, batch, lr, log=None, seed=0):
     return history, time.perf_counter() - t0
 
 
-def predict_into(net, stack, data_scales, factor, mirrors=1, restarts=0, nu=0):
+def predict_into(net, stack, data_scales, factor, mirrors=1, restarts=0, nu=0,
+                 restart_mirrors=None):
     """Warm start: pool the stack's fields, run the network, upsample into
     the stack's p0 (p1 too, so the first sweep starts from it).  With
     mirrors > 1 the prediction is the mean of the network's predictions for
@@ -542,6 +543,7 @@ def predict_into(net, stack, data_scales, factor, mirrors=1, restarts=0, nu=0):
         for g in (stack.grids[0], stack.grids[1]):
             _ok(up(ctypes.byref(f), _p(pred), ctypes.c_void_p(g.dev_ptr), net.stream()))
     used = 0
+    rflips = flips if restart_mirrors is None else mirror_images(stack.shape, restart_mirrors)
     for _ in range(restarts):
         torch.cuda.synchronize()
         stack.sweeps(nu)
@@ -550,8 +552,8 @@ def predict_into(net, stack, data_scales, factor, mirrors=1, restarts=0, nu=0):
         ps.synchronize()
         # the mirror predictions summed into a scratch grid, then added to
         # the iterate with a single rounding
-        for i, flip in enumerate(flips):
-            f = stack.fields(factor, wscale, pscale * len(flips), flip=flip, wrk1=stack.rgrid,
+        for i, flip in enumerate(rflips):
+            f = stack.fields(factor, wscale, pscale * len(rflips), flip=flip, wrk1=stack.rgrid,
                              inst_scale=scale)
             _ok(L.PSWarmStartPool(ctypes.byref(f), _p(x), net.stream()))
             pred = net.forward(x, (n, zc, yc, xc))

@@ -345,25 +345,44 @@ def test_network_gradients_match_oracle(rt, conv_form):
 
 
 def test_trained_network_saves_sweeps(rt):
-    # Small instances (33 x 17 x 17), 384 solved for training and 32 held
-    # out; a short GPU training run; the held-out solves from the warm start
-    # reach relative residual 1e-6 in fewer sweeps than from zero.
+    # Small instances (33 x 17 x 17), 384 solved for training (with iterates
+    # of their solves for the restarts) and 32 held out; a short GPU
+    # training run.  The held-out solves reach relative residual 1e-6 from
+    # the single-shot prediction and from the prediction plus learned
+    # restarts in fewer sweeps than from zero (restart sweeps counted), all
+    # at the same tolerance.  The bounds sit just under the gains measured
+    # on GB300 for this seed and size (printed).
     from physis_gb300 import warmstart as ws
     rng = np.random.default_rng(7)
     shape, factor = (33, 17, 17), 4
-    data = ws.Dataset(rng, 384, shape, factor, nsx=15, per_stack=400, tol=1e-7, chunk=64)
+    data = ws.Dataset(rng, 384, shape, factor, nsx=15, per_stack=400, tol=1e-7, chunk=64,
+                      snapshots=(16, 64, 256))
     net = ws.Net(seed=1)
     hist, _ = ws.train(net, data, epochs=80, batch=32, lr=2e-3)
     assert hist[-1] < 0.5 * hist[0]
     held = [ws.make_instance(rng, shape) for _ in range(32)]
     st = ws.Stack(held, shape, nsx=15)
+    zeros = np.zeros(st.gshape, np.float32)
     zero = st.solve(1e-6, 16, 20000)
-    st.grids[0].copyin(np.zeros(st.gshape, np.float32))
-    st.grids[1].copyin(np.zeros(st.gshape, np.float32))
-    ws.predict_into(net, st, (data.wscale, data.pscale), factor)
-    warm = st.solve(1e-6, 16, 20000)
-    r = st.residuals()
+    counts = {}
+    for name, k in (("single", 0), ("restarts", 3)):
+        st.grids[0].copyin(zeros)
+        st.grids[1].copyin(zeros)
+        used = ws.predict_into(net, st, (data.wscale, data.pscale), factor, 16, restarts=k,
+                               nu=16)
+        c = st.solve(1e-6, 16, 20000)
+        assert (c > 0).all(), (name, c)
+        assert (st.residuals() <= 1e-6).all(), name
+        counts[name] = c + used
     st.free()
-    assert (zero > 0).all() and (warm > 0).all()
-    assert (r <= 1e-6).all()
-    assert warm.mean() < 0.95 * zero.mean(), (warm.mean(), zero.mean())
+    assert (zero > 0).all()
+    ratio = {k: zero.mean() / v.mean() for k, v in counts.items()}
+    print("sweeps: zero %.0f, single %.0f, restarts %.0f; ratios %s" % (
+        zero.mean(), counts["single"].mean(), counts["restarts"].mean(), ratio))
+    assert ratio["single"] > SINGLE_MIN, ratio
+    assert ratio["restarts"] > RESTART_MIN, ratio
+
+
+# lower bounds of the held-out sweep ratios above
+SINGLE_MIN = 1.05
+RESTART_MIN = 1.5
