@@ -1169,7 +1169,9 @@ def run_gpu_warmstart(args, dist):
         shape, factor, nsx, per_stack, chunk = (257, 129, 129), 16, 16, 64, 2000
     else:
         shape, factor, nsx, per_stack, chunk = (args.ws_nz, args.ws_ny, args.ws_nx), 4, 15, 300, 256
-    snapshots = [int(v) for v in args.ws_snapshots.split(",") if v.strip()]
+    nu = args.ws_nu or 2 * factor * factor
+    snapshots = ([int(v) for v in args.ws_snapshots.split(",") if v.strip()] or
+                 [nu, 4 * nu, 16 * nu, 64 * nu])
     rng = np.random.default_rng(5)
     workers = min(16, os.cpu_count() or 1)
     t0 = time.perf_counter()
@@ -1194,7 +1196,7 @@ def run_gpu_warmstart(args, dist):
 
     scales = (data.wscale, data.pscale)
     pm = args.ws_predict_mirrors
-    K, nu = args.ws_restarts, args.ws_nu
+    K = args.ws_restarts
     # Sweep counts, checked every `echunk` sweeps.  Float32 Jacobi has a
     # residual floor near 1e-7 * ||p|| / ||ss(0)||; instances whose floor lies
     # above 1e-6 never get there from any start and are left out of the
@@ -1380,15 +1382,17 @@ def main():
     ap.add_argument("--ws-ny", type=int, default=33)
     ap.add_argument("--ws-nz", type=int, default=65)
     ap.add_argument("--ws-max-sweeps", type=int, default=12000)
-    ap.add_argument("--ws-restarts", type=int, default=3,
+    ap.add_argument("--ws-restarts", type=int, default=2,
                     help="warm start: learned restarts after the prediction (0: single shot)")
-    ap.add_argument("--ws-restart-mirrors", type=int, default=1,
+    ap.add_argument("--ws-restart-mirrors", type=int, default=16,
                     help="warm start: mirror images averaged in each restart's prediction")
-    ap.add_argument("--ws-nu", type=int, default=32,
-                    help="warm start: Jacobi sweeps before each learned restart (even)")
-    ap.add_argument("--ws-snapshots", default="32,128,512,2048",
+    ap.add_argument("--ws-nu", type=int, default=0,
+                    help="warm start: Jacobi sweeps before each learned restart (even; "
+                         "0: 2 x pooling factor^2, i.e. 32 reduced, 512 at --ws-full)")
+    ap.add_argument("--ws-snapshots", default="",
                     help="warm start: sweep counts of the target solves whose iterates "
-                         "train the restarts (comma-separated, even)")
+                         "train the restarts (comma-separated, even; default: nu x 1, 4, "
+                         "16, 64)")
     ap.add_argument("--ws-full", action="store_true",
                     help="config 5 at the specified 129x129x257 (use --ws-train/--ws-held "
                          "to size it, e.g. 128/32, and --ws-max-sweeps 100000)")
