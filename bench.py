@@ -171,11 +171,11 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """dram bytes (read + write) of one 512^3 launch of the sweep kernel,
-    from the committed ncu summary of a full-size capture
-    (profiles/diffusion7_512.md, line `traffic_bytes_per_launch:`)."""
-    p = os.path.join(ROOT, "profiles", "diffusion7_512.md")
+def profiled_traffic(name="diffusion7_512.md"):
+    """dram bytes (read + write) of one launch of a kernel at the bench's
+    full size, from the committed ncu summary of that capture
+    (profiles/<name>, line `traffic_bytes_per_launch:`)."""
+    p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -660,7 +660,8 @@ def reduce_measure(ps, reps=20, cpu=True):
         "rel_err_vs_fp64": abs(v64 - exact) / exact,
         "roofline": {"bound": "hbm", "achieved": nbytes / (ms / 1e3) / 1e9, "peak": peak,
                      "unit": "GB/s", "frac": nbytes / (ms / 1e3) / 1e9 / peak,
-                     "traffic": None, "peak_source": peak_kind, "bytes_per_element": 4},
+                     "traffic": profiled_traffic("reduce_512.md"), "peak_source": peak_kind,
+                     "bytes_per_element": 4},
         "l2": "512 MiB grid > L2",
         "cpu_baseline": None,
     }
@@ -806,7 +807,8 @@ def himeno_measure(ps, dist, K, W, cpu_seconds, with_cpu):
                 "job_seconds": e2e_max, "last_gosa": float(gosa)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": profiled_traffic("himeno19_traffic_257x257x513.md"),
                      "peak_source": peak_kind,
                      "bytes_per_lup": HIM_BYTES_PER_LUP},
         "clocks": clk,
