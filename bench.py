@@ -1212,7 +1212,8 @@ def run_gpu_warmstart(args, dist):
     for name, k in modes.items():
         reset()
         used = ws.predict_into(net, st, scales, factor, pm, restarts=k, nu=nu,
-                               restart_mirrors=args.ws_restart_mirrors)
+                               restart_mirrors=args.ws_restart_mirrors,
+                               pullback=args.ws_pullback)
         r_start[name] = st.residuals()
         c = st.solve(1e-6, echunk, args.ws_max_sweeps)
         counts[name] = np.where(c > 0, c + used, c)
@@ -1229,7 +1230,7 @@ def run_gpu_warmstart(args, dist):
         t = time.perf_counter()
         if k is not None:
             ws.predict_into(net, st, scales, factor, pm, restarts=k, nu=nu,
-                            restart_mirrors=args.ws_restart_mirrors)
+                            restart_mirrors=args.ws_restart_mirrors, pullback=args.ws_pullback)
         st.sweeps(n)
         ps.synchronize()
         return time.perf_counter() - t
@@ -1295,7 +1296,8 @@ def run_gpu_warmstart(args, dist):
                 "sweeps_ratio_mean": float(zero[both].mean() / counts[name][both].mean()),
                 "at_1e-6_after_timed_run": oks[name],
                 "initial_residual_median": float(np.median(r_start[name])),
-                "restarts": modes[name], "sweeps_per_restart": nu if modes[name] else 0}
+                "restarts": modes[name], "sweeps_per_restart": nu if modes[name] else 0,
+                "pullback": args.ws_pullback if modes[name] else 0.0}
 
     line = {
         "metric": "Poisson time-to-1e-6 resid, learned vs plain (speed-up of the warm start)",
@@ -1386,6 +1388,9 @@ def main():
     ap.add_argument("--ws-max-sweeps", type=int, default=12000)
     ap.add_argument("--ws-restarts", type=int, default=2,
                     help="warm start: learned restarts after the prediction (0: single shot)")
+    ap.add_argument("--ws-pullback", type=float, default=1e-4,
+                    help="warm start: relative pull of the restarted iterate toward zero "
+                         "(keeps float32 Jacobi out of 2-cycles near the tolerance)")
     ap.add_argument("--ws-restart-mirrors", type=int, default=16,
                     help="warm start: mirror images averaged in each restart's prediction")
     ap.add_argument("--ws-nu", type=int, default=0,

@@ -403,14 +403,16 @@ int PSWarmStartUpsampleAdd(const PSWarmStartFields *f, const float *coarse, floa
  * adds the network's prediction of the error: a learned restart. */
 int PSWarmStartResidualSource(const PSWarmStartFields *f, float *r, float *inst_scale,
                               float target_rms, double *work, int work_len, void *stream);
-/* p += delta at every cell of every instance (the fields' stacked layout;
- * flip 0).  A restart sums the mirror predictions into delta with
- * PSWarmStartUpsample/UpsampleAdd and adds them to the iterate with one
- * rounding: sixteen rounded additions into the iterate itself, near the
- * float32 floor, left some instances' Jacobi iteration in a 2-cycle above
- * the tolerance. */
-int PSWarmStartAddCorrection(const PSWarmStartFields *f, const float *delta, float *p,
-                             void *stream);
+/* p = p_scale * p + delta at every cell of every instance (the fields'
+ * stacked layout; flip 0; delta may be NULL).  A restart sums the mirror
+ * predictions into delta with PSWarmStartUpsample/UpsampleAdd and adds them
+ * to the iterate with one rounding.  With delta NULL and p_scale = 1 - c
+ * the iterate is pulled toward zero by a relative c: the last approach of
+ * float32 Jacobi to its fixed point then runs along the solution, as a zero
+ * start's does, instead of ending in a 2-cycle just above the tolerance
+ * (which iterates brought very close by restarts often do). */
+int PSWarmStartAddCorrection(const PSWarmStartFields *f, const float *delta, float p_scale,
+                             float *p, void *stream);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop

@@ -200,7 +200,7 @@ def lib():
     L.PSWarmStartUpsample.argtypes = [fp, vp, vp, vp]
     L.PSWarmStartUpsampleAdd.argtypes = [fp, vp, vp, vp]
     L.PSWarmStartResidualSource.argtypes = [fp, vp, vp, ctypes.c_float, vp, i, vp]
-    L.PSWarmStartAddCorrection.argtypes = [fp, vp, vp, vp]
+    L.PSWarmStartAddCorrection.argtypes = [fp, vp, ctypes.c_float, vp, vp]
     for name in ("PSWarmStartConv", "PSWarmStartWeightGrad", "PSWarmStartPrepareWeights",
                  "PSWarmStartAdam", "PSWarmStartLoss", "PSWarmStartPool",
                  "PSWarmStartPoolTarget", "PSWarmStartUpsample", "PSWarmStartUpsampleAdd",

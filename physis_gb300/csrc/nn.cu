@@ -673,10 +673,11 @@ __global__ void residual_source_kernel(PoolArgs a, float *__restrict__ r,
   if (threadIdx.x == 0) part[(long long)b * gridDim.x + blockIdx.x] = red[0];
 }
 
-// p += delta at every cell of every instance (stored layout): one rounding
-// of p per restart, whatever number of mirror predictions delta sums.
+// p = p_scale * p + delta at every cell of every instance (stored layout;
+// delta may be NULL): one rounding of p per restart, whatever number of
+// mirror predictions delta sums.
 __global__ void add_correction_kernel(PoolArgs a, const float *__restrict__ delta,
-                                      float *__restrict__ p) {
+                                      float p_scale, float *__restrict__ p) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long n = (long long)a.batch * a.inz * a.iny * a.inx;
   if (i >= n) return;
@@ -684,7 +685,8 @@ __global__ void add_correction_kernel(PoolArgs a, const float *__restrict__ delt
   const int z = (int)((i / ((long long)a.inx * a.iny)) % a.inz);
   const int b = (int)(i / ((long long)a.inx * a.iny * a.inz));
   const long long k = fine_index(a, b, z, y, x);
-  p[k] = p[k] + delta[k];
+  const float v = p_scale == 1.f ? p[k] : __fmul_rn(p_scale, p[k]);
+  p[k] = delta ? __fadd_rn(v, delta[k]) : v;
 }
 
 // scale[b] = target_rms / rms(r of instance b) over its interior cells
@@ -839,11 +841,12 @@ int nn_residual_source(const NNFields &f, float *r, float *inst_scale, float tar
   return (int)cudaGetLastError();
 }
 
-int nn_add_correction(const NNFields &f, const float *delta, float *p, cudaStream_t s) {
+int nn_add_correction(const NNFields &f, const float *delta, float p_scale, float *p,
+                      cudaStream_t s) {
   const PoolArgs a = pool_args(f);
   const long long n = (long long)a.batch * a.inz * a.iny * a.inx;
-  if (n <= 0 || !delta || !p) return -1;
-  add_correction_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, delta, p);
+  if (n <= 0 || !p) return -1;
+  add_correction_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, delta, p_scale, p);
   return (int)cudaGetLastError();
 }
 

@@ -245,8 +245,10 @@ int nn_upsample(const NNFields &f, const float *coarse, float *p, bool add, cuda
 // work_len doubles (at least one per instance).
 int nn_residual_source(const NNFields &f, float *r, float *inst_scale, float target_rms,
                        double *work, int work_len, cudaStream_t s);
-// p += delta over every cell of every instance (f's stacked layout).
-int nn_add_correction(const NNFields &f, const float *delta, float *p, cudaStream_t s);
+// p = p_scale * p + delta over every cell of every instance (f's stacked
+// layout; delta may be NULL).
+int nn_add_correction(const NNFields &f, const float *delta, float p_scale, float *p,
+                      cudaStream_t s);
 
 // ---- Reductions (reduce.cu) ----------------------------------------------
 // Reduces every element of g with op.  The 8-byte result is written to

@@ -2415,11 +2415,11 @@ int PSWarmStartResidualSource(const PSWarmStartFields *f, float *r, float *inst_
                    "PSWarmStartResidualSource");
 }
 
-int PSWarmStartAddCorrection(const PSWarmStartFields *f, const float *delta, float *p,
-                             void *stream) {
-  if (!ws_fields_ok(f, "PSWarmStartAddCorrection", false) || !delta || !p || f->flip != 0)
+int PSWarmStartAddCorrection(const PSWarmStartFields *f, const float *delta, float p_scale,
+                             float *p, void *stream) {
+  if (!ws_fields_ok(f, "PSWarmStartAddCorrection", false) || !p || f->flip != 0)
     return ws_status(-1, "PSWarmStartAddCorrection");
-  return ws_status(psg::nn_add_correction(ws_fields(f), delta, p, ws_stream(stream)),
+  return ws_status(psg::nn_add_correction(ws_fields(f), delta, p_scale, p, ws_stream(stream)),
                    "PSWarmStartAddCorrection");
 }
 

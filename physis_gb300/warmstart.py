@@ -510,7 +510,7 @@ def train(net, data, epochs, batch, lr, log=None, seed=0):
 
 
 def predict_into(net, stack, data_scales, factor, mirrors=1, restarts=0, nu=0,
-                 restart_mirrors=None):
+                 restart_mirrors=None, pullback=0.0):
     """Warm start: pool the stack's fields, run the network, upsample into
     the stack's p0 (p1 too, so the first sweep starts from it).  With
     mirrors > 1 the prediction is the mean of the network's predictions for
@@ -527,7 +527,13 @@ def predict_into(net, stack, data_scales, factor, mirrors=1, restarts=0, nu=0,
     error the network can see by roughly its relative accuracy, and the
     sweeps between restarts remove the fine-scale part of the error that
     the coarse grid cannot represent.  The sweeps are real iterations:
-    returns the number run (restarts * nu)."""
+    returns the number run (restarts * nu).
+
+    pullback > 0 scales the restarted iterate by 1 - pullback at the end.
+    Restarts can bring an iterate so close that float32 Jacobi then locks
+    into a 2-cycle a little above 1e-6; pulled back along the solution
+    itself, the last approach runs like a zero start's, which ends at a
+    fixed point."""
     import torch
     wscale, pscale = data_scales
     zc, yc, xc = coarse_shape(stack.shape, factor)
@@ -562,6 +568,11 @@ def predict_into(net, stack, data_scales, factor, mirrors=1, restarts=0, nu=0,
                    net.stream()))
         f = stack.fields(factor)
         _ok(L.PSWarmStartAddCorrection(ctypes.byref(f), ctypes.c_void_p(stack.scratch.dev_ptr),
+                                       ctypes.c_float(1.0),
+                                       ctypes.c_void_p(stack.grids[0].dev_ptr), net.stream()))
+    if restarts and pullback > 0:
+        f = stack.fields(factor)
+        _ok(L.PSWarmStartAddCorrection(ctypes.byref(f), None, ctypes.c_float(1.0 - pullback),
                                        ctypes.c_void_p(stack.grids[0].dev_ptr), net.stream()))
     torch.cuda.synchronize()
     return used
