@@ -156,3 +156,24 @@ def test_mirror_image_lists():
     assert ws.mirror_images((65, 33, 33), 0) == [0]
     assert ws.coarse_shape((257, 129, 129), 16) == (17, 9, 9)
     assert ws.coarse_shape((65, 33, 33), 4) == (17, 9, 9)
+
+
+def test_residual_source_is_the_himeno_residual_over_a3():
+    # The correction problem's source r = ss / a3 (nn.residual_source)
+    # against the REF Himeno sweep of the C oracle: its gosa is sum ss^2, and
+    # with omega = 1 its update is p1 = p0 + ss, so ss = p1 - p0.
+    from oracle import pyoracle
+    from physis_gb300 import warmstart as ws
+    rng = np.random.default_rng(3)
+    shape = (11, 9, 8)
+    inst = ws.make_instance(rng, shape)
+    p = rng.normal(size=shape).astype(np.float32)
+    arrays = [p.copy(), np.zeros(shape, np.float32)] + ws.himeno_arrays(inst)
+    nz, ny, nx = shape
+    g_ref, g64 = pyoracle.himeno19(arrays, (1, nx - 1, 1, ny - 1, 1, nz - 1), np.float32(1.0))
+    ss = (arrays[1].astype(np.float64) - p)[1:-1, 1:-1, 1:-1]
+    a3 = arrays[5].astype(np.float64)[1:-1, 1:-1, 1:-1]
+    r = nn.residual_source(inst, p)
+    assert np.allclose(r[1:-1, 1:-1, 1:-1] * a3, ss, rtol=1e-5, atol=1e-5 * np.abs(ss).max())
+    assert abs(float(((r[1:-1, 1:-1, 1:-1] * a3) ** 2).sum()) - g64) <= 1e-4 * g64
+    assert not r[0].any() and not r[-1].any() and not r[:, 0].any() and not r[:, :, -1].any()
