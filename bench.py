@@ -1386,7 +1386,7 @@ def main():
     ap.add_argument("--ws-ny", type=int, default=33)
     ap.add_argument("--ws-nz", type=int, default=65)
     ap.add_argument("--ws-max-sweeps", type=int, default=12000)
-    ap.add_argument("--ws-restarts", type=int, default=2,
+    ap.add_argument("--ws-restarts", type=int, default=4,
                     help="warm start: learned restarts after the prediction (0: single shot)")
     ap.add_argument("--ws-pullback", type=float, default=1e-4,
                     help="warm start: relative pull of the restarted iterate toward zero "
