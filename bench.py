@@ -1174,7 +1174,7 @@ def run_gpu_warmstart(args, dist):
     nu = args.ws_nu or 2 * factor * factor
     snapshots = ([int(v) for v in args.ws_snapshots.split(",") if v.strip()] or
                  [nu, 4 * nu, 16 * nu, 64 * nu])
-    rng = np.random.default_rng(5)
+    rng = np.random.default_rng(args.ws_seed)
     workers = min(16, os.cpu_count() or 1)
     t0 = time.perf_counter()
     data = ws.Dataset(rng, args.ws_train, shape, factor, nsx=nsx, per_stack=per_stack, tol=1e-7,
@@ -1304,7 +1304,7 @@ def run_gpu_warmstart(args, dist):
         "value": tz / secs[head], "unit": "x", "n_gpus": 1, "steps": args.ws_held,
         "warmup": max(args.warmup, 3), "ms_per_step": secs[head] / args.ws_held * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16",
-        "data": f"synthetic seeded instances (seed 5), {args.ws_train} solved for training "
+        "data": f"synthetic seeded instances (seed {args.ws_seed}), {args.ws_train} solved for training "
                 f"(x {len(data.flips)} mirror images, + {len(snapshots)} solve iterates each "
                 f"for the restarts), {args.ws_held} held out",
         "config": {"workload": f"learned warm start, 19-point Jacobi {shape[2]}x{shape[1]}x"
@@ -1388,6 +1388,8 @@ def main():
     ap.add_argument("--ws-max-sweeps", type=int, default=12000)
     ap.add_argument("--ws-restarts", type=int, default=4,
                     help="warm start: learned restarts after the prediction (0: single shot)")
+    ap.add_argument("--ws-seed", type=int, default=5,
+                    help="warm start: seed of the training and held-out instances")
     ap.add_argument("--ws-pullback", type=float, default=1e-4,
                     help="warm start: relative pull of the restarted iterate toward zero "
                          "(keeps float32 Jacobi out of 2-cycles near the tolerance)")
