@@ -59,7 +59,16 @@ pts_kernel(const __grid_constant__ PtsParams<T> p, const __grid_constant__ PtsTm
 // waits with wait_group<kPtsPrefetch>; a TMA plane lands in one copy, and one
 // plane ahead is enough (measured: the smaller ring fits more CTAs per SM and
 // runs the 7-point stencil 5 % faster).
-int points_prefetch(bool tma) { return tma ? 1 : kPtsPrefetch; }
+// PS_POINTS_PREFETCH=<1..4> overrides the TMA depth (a tuning knob).
+int points_prefetch(bool tma) {
+  if (!tma) return kPtsPrefetch;
+  static const int depth = [] {
+    const char *e = getenv("PS_POINTS_PREFETCH");
+    const int v = e ? atoi(e) : 0;
+    return (v >= 1 && v <= 4) ? v : 1;
+  }();
+  return depth;
+}
 
 // Offsets' extent per axis: lo <= 0 <= hi.
 void extents(const PointsArgs &a, int lo[3], int hi[3]) {
