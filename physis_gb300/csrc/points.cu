@@ -57,8 +57,8 @@ pts_kernel(const __grid_constant__ PtsParams<T> p, const __grid_constant__ PtsTm
 
 // Planes in flight ahead of the newest plane a step reads: the cp.async ring
 // waits with wait_group<kPtsPrefetch>; a TMA plane lands in one copy, and one
-// plane ahead is enough (measured: the smaller ring fits more CTAs per SM and
-// runs the 7-point stencil 5 % faster).
+// plane ahead is enough (measured at 512^3: two or three planes ahead run the
+// 7-point stencil 4-15 % and the 27-point 1-2 % slower, whatever the tile).
 // PS_POINTS_PREFETCH=<1..4> overrides the TMA depth (a tuning knob).
 int points_prefetch(bool tma) {
   if (!tma) return kPtsPrefetch;

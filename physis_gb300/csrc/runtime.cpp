@@ -1612,7 +1612,9 @@ void PSInitV(int trace) {
     r->tshapes[k] = MarchConfig{8, 4, 3, 0, 0};
     r->tblock[k] = 1;
   }
-  r->shapes[kSlotPoints] = MarchConfig{8, 4, 4, 0, 0};  // point stencils: 8 warps x 4 rows
+  // point stencils: 4 warps x 4 rows (a 128 x 16 tile; at 512^3 it equals 8 x 4 for the
+  // 7-point stencil and is 6 % faster for the 27-point one: smaller rings, more CTAs)
+  r->shapes[kSlotPoints] = MarchConfig{4, 4, 4, 0, 0};
   r->shapes[PS_KERNEL_HIMENO19] = MarchConfig{4, 1, 5, 2, 0};
   r->shapes[PS_KERNEL_HIMENO19_GOSA] = MarchConfig{4, 1, 5, 2, 0};
   cudaDeviceSynchronize();
