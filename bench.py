@@ -22,12 +22,12 @@ Printed JSON line (one, rank 0):
 
 Further keys of the same line (leave them out with --no-extras), each with
 its own CUDA-event timing, roofline and CPU baseline:
-  himeno     config 3: 19-point Himeno Jacobi at 257x257x513 with the fused
+  himeno     19-point Himeno Jacobi at 257x257x513 with the fused
              residual, max(K, 50) sweeps, 56 algorithmic bytes per interior
              cell update;
-  batch      config 4: 48 uneven grids (half diffusion, half Himeno), 200
+  batch      48 uneven grids (half diffusion, half Himeno), 200
              steps each, batched against 48 separate runs;
-  config1    64^3 x 100 steps + PSReduce sum (the REF program's
+  diffusion64  64^3 x 100 steps + PSReduce sum (the REF program's
              configuration), device and end to end;
   reduce     PSReduce over a 512^3 float grid, GB/s.
 
@@ -470,7 +470,8 @@ def run_gpu(args, dist):
     shape_used = ps.get_launch_shape(ps.PS_KERNEL_DIFFUSION7)
 
     # the other headline configurations, each with its own CUDA-event timing,
-    # roofline and CPU baseline (config 3, config 4, config 1, PSReduce)
+    # roofline and CPU baseline (Himeno 257x257x513, 48 uneven grids, 64^3 x 100
+    # steps, PSReduce over 512^3)
     extras = {}
     if not args.no_extras:
         with_cpu = dist.rank == 0 and not args.no_cpu_baseline
@@ -478,7 +479,7 @@ def run_gpu(args, dist):
         extras["himeno"] = himeno_measure(ps, dist, hk, W, args.cpu_seconds / 2, with_cpu)
         extras["batch"] = batch_measure(ps, dist, 200, False, args.cpu_seconds / 2, with_cpu)
         if dist.rank == 0:
-            extras["config1"] = config1_measure(ps)
+            extras["diffusion64"] = diffusion64_measure(ps)
             extras["reduce"] = reduce_measure(ps, cpu=with_cpu)
 
     cpu = None
@@ -529,10 +530,10 @@ def run_gpu(args, dist):
 
 
 # ---------------------------------------------------------------------------
-# Config 1 (64^3 x 100 steps + PSReduce) and the grid form of PSReduce
+# 64^3 x 100 steps + PSReduce, and the grid form of PSReduce
 # ---------------------------------------------------------------------------
 
-def config1_measure(ps, reps=20):
+def diffusion64_measure(ps, reps=20):
     """64^3 clamped diffusion, seed 0, 100 steps (50 iterations of the two
     maps) and a PSReduce sum of the final grid, as the reference's REF
     program runs it.  Device: CUDA events around the 100 steps.  e2e: the
@@ -678,7 +679,7 @@ def reduce_measure(ps, reps=20, cpu=True):
 
 
 # ---------------------------------------------------------------------------
-# Himeno 19-point Jacobi with the fused residual (config 3)
+# Himeno 19-point Jacobi with the fused residual, 257x257x513
 # ---------------------------------------------------------------------------
 
 HIM = (257, 257, 513)  # nx, ny, nz
@@ -830,7 +831,7 @@ def run_gpu_himeno(args, dist):
 
 
 # ---------------------------------------------------------------------------
-# Batched uneven grids (config 4)
+# Batched uneven grids (48 problems)
 # ---------------------------------------------------------------------------
 
 def batch_dims(seed=2, n=48, xy=(32, 320), z=(32, 512)):
@@ -1141,7 +1142,7 @@ def run_gpu_points(args, dist):
 
 
 # ---------------------------------------------------------------------------
-# Learned warm start for the 19-point Jacobi solve (config 5, reduced scale)
+# Learned warm start for the 19-point Jacobi solve
 # ---------------------------------------------------------------------------
 
 def measured_bf16_tflops():
@@ -1349,7 +1350,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
-                    help="diffusion: leave out the temporal/himeno/batch/config1/reduce "
+                    help="diffusion: leave out the temporal/himeno/batch/diffusion64/reduce "
                          "keys (the plain sweep alone, e.g. for a profiler)")
     ap.add_argument("--warps", type=int, default=0)
     ap.add_argument("--rows", type=int, default=0)
@@ -1403,7 +1404,7 @@ def main():
                          "train the restarts (comma-separated, even; default: nu x 1, 4, "
                          "16, 64)")
     ap.add_argument("--ws-full", action="store_true",
-                    help="config 5 at the specified 129x129x257 (use --ws-train/--ws-held "
+                    help="warm start at 129x129x257 (use --ws-train/--ws-held "
                          "to size it, e.g. 128/32, and --ws-max-sweeps 100000)")
     args = ap.parse_args()
     global N

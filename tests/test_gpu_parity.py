@@ -5,7 +5,7 @@ All tests here run on a GB300 through the C ABI (ctypes).  The bar:
   order, round-to-nearest, no FMA contraction on either side);
 * system-test programs: exact stdout text of the reference's own oracles;
 * float reductions: within 1e-6 relative of the FP64 oracle (the REF fold's
-  own error is reported beside it, it is not the judge); integer reductions
+  own error is reported beside it, it is not the criterion); integer reductions
   exact (modulo 2^32 / 2^64 like the REF fold).
 """
 import numpy as np
@@ -143,7 +143,7 @@ def test_himeno_matches_original(rt):
 
 # ---- seeded configurations vs the oracle -----------------------------------
 
-def test_config1_diffusion_64cubed_100_steps(rt, oracle):
+def test_diffusion_64cubed_100_steps_then_reduce(rt, oracle):
     # 64^3 uniform[0,1) seed 0, cc=0.4 others 0.1, clamped, 100 steps
     # (50 x 2 maps), then PSReduce sum: cell-by-cell bit-exact vs REF.
     shape = (64, 64, 64)
