@@ -222,7 +222,7 @@ void PSSetBatchShape(int warps, int rows, int ns7, int nsp, int nsc);
  * Scratch: a static device array of 2048 per-CTA partials plus a ticket
  * (16 KiB), held by every GPU that loads the library until exit.  A launch
  * that would need more partial slots than that is rejected
- * (PS_ERR_UNSUPPORTED; a 152-SM GB300 needs at most 1216).  All calls share
+ * (PS_ERR_UNSUPPORTED; a 152-SM GB300 needs at most 608).  All calls share
  * the array and it keeps the last call's contents (the ticket is cleared on
  * the stream before each launch): calls whose work overlaps on the GPU race.
  * Set-up: the first call on a device (and the first after the device's

@@ -7,14 +7,18 @@
 // (runtime/reduce.h:14-49).
 //
 // One pass: warps stride over x-rows; lanes read 16-byte vectors (a warp
-// reads 512 contiguous bytes per step) and accumulate in the element type
+// reads 512 contiguous bytes per load) and accumulate in the element type
 // (FP32 for float grids; a float PS_PROD accumulates in FP64, because a long
 // FP32 product loses about sqrt(n) ulps whatever the order), then warp
-// shuffles and a shared-memory tree give one partial per CTA.  Partials are stored as 8-byte values (FP64 for
+// shuffles and a shared-memory tree give one partial per CTA.  Each lane
+// issues kLoadsInFlight vector loads of a row before it combines any of them,
+// so every warp keeps 2 KiB in flight; four CTAs of 256 threads per SM then
+// cover the HBM latency.  Partials are stored as 8-byte values (FP64 for
 // float/double grids, 64-bit integers for int/long grids) and the last CTA to
-// finish (atomic ticket) combines them in a fixed order: FP64 for floating
-// grids, wrapping integer arithmetic for integer grids (the REF fold wraps the
-// same way).  The result is deterministic run to run.
+// finish (atomic ticket) combines them in a fixed order, all 256 threads
+// strided over the partials: FP64 for floating grids, wrapping integer
+// arithmetic for integer grids (the REF fold wraps the same way).  The result
+// is deterministic run to run.
 #include <atomic>
 #include <mutex>
 #include <type_traits>
@@ -29,6 +33,8 @@ namespace psg {
 namespace {
 
 constexpr int kReduceThreads = 256;
+constexpr int kLoadsInFlight = 4;  // 16-byte loads per lane before combining
+constexpr int kReduceCtasPerSm = 4;
 
 template <typename T> struct RTraits;
 template <> struct RTraits<float> {
@@ -100,8 +106,11 @@ __global__ void __launch_bounds__(kReduceThreads)
 reduce_kernel(const char *__restrict__ base, int64_t pitch, int nx, int ny, int nz,
               int op, uint64_t *partials, unsigned *ticket, uint64_t *result) {
   constexpr int VEC = 16 / (int)sizeof(T);
+  constexpr int U = kLoadsInFlight;
   __shared__ A red[kReduceThreads / 32];
   __shared__ bool red_has[kReduceThreads / 32];
+  __shared__ C redc[kReduceThreads / 32];
+  __shared__ bool redc_has[kReduceThreads / 32];
   __shared__ int last_cta;
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -116,18 +125,29 @@ reduce_kernel(const char *__restrict__ base, int64_t pitch, int nx, int ny, int 
   A acc = identity<T, A>(op);
   bool has = false;
   for (int64_t r = gw; r < rows; r += nw) {
-    const char *rp = base + (r / ny) * pitch * ny + (r % ny) * pitch;
+    // Row r of plane r / ny starts at ((r / ny) * ny + r % ny) * pitch.
+    const char *rp = base + r * pitch;
     const uint4 *vp = reinterpret_cast<const uint4 *>(rp);
-#pragma unroll 4
-    for (int v = lane; v < nvec; v += 32) {
-      union { uint4 u; T t[VEC]; } cvt;
-      cvt.u = __ldcs(vp + v);
+    // A lane takes vectors lane, lane + 32, lane + 64, ... in that order.
+    for (int v0 = 0; v0 < nvec; v0 += 32 * U) {
+      uint4 u[U];
 #pragma unroll
-      for (int i = 0; i < VEC; ++i) {
-        const A e = to_acc<T, A>(cvt.t[i]);
-        acc = has ? combine<T, A>(op, acc, e)
-                  : ((op == kSum || op == kProd) ? combine<T, A>(op, acc, e) : e);
-        has = true;
+      for (int j = 0; j < U; ++j) {
+        const int v = v0 + lane + 32 * j;
+        u[j] = (v < nvec) ? __ldcs(vp + v) : make_uint4(0u, 0u, 0u, 0u);
+      }
+#pragma unroll
+      for (int j = 0; j < U; ++j) {
+        if (v0 + lane + 32 * j >= nvec) break;
+        union { uint4 u; T t[VEC]; } cvt;
+        cvt.u = u[j];
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) {
+          const A e = to_acc<T, A>(cvt.t[i]);
+          acc = has ? combine<T, A>(op, acc, e)
+                    : ((op == kSum || op == kProd) ? combine<T, A>(op, acc, e) : e);
+          has = true;
+        }
       }
     }
     if (lane < tail) {
@@ -174,11 +194,11 @@ reduce_kernel(const char *__restrict__ base, int64_t pitch, int nx, int ny, int 
     last_cta = (prev == gridDim.x - 1);
   }
   __syncthreads();
-  if (last_cta && warp == 0) {
+  if (last_cta) {  // uniform across the CTA (shared flag after the barrier)
     __threadfence();
     C v = (C)identity<T, A>(op);
     bool vh = false;
-    for (unsigned i = lane; i < gridDim.x; i += 32) {
+    for (unsigned i = threadIdx.x; i < gridDim.x; i += kReduceThreads) {
       const uint64_t bits = __ldcg(reinterpret_cast<const unsigned long long *>(partials) + i);
       C e;
       if constexpr (sizeof(C) == 8) {
@@ -197,6 +217,18 @@ reduce_kernel(const char *__restrict__ base, int64_t pitch, int nx, int ny, int 
       vh = vh || oh;
     }
     if (lane == 0) {
+      redc[warp] = v;
+      redc_has[warp] = vh;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      v = (C)identity<T, A>(op);
+      vh = false;
+      for (int w = 0; w < kReduceThreads / 32; ++w) {
+        if (!redc_has[w]) continue;
+        v = vh ? combine<T, C>(op, v, redc[w]) : redc[w];
+        vh = true;
+      }
       uint64_t bits;
       if constexpr (sizeof(C) == 8) {
         bits = *reinterpret_cast<uint64_t *>(&v);
@@ -237,7 +269,7 @@ int reduce_num_ctas(const GridView &g, int sm_count) {
   const int64_t rows = (int64_t)g.ny * g.nz;
   const int64_t warps = kReduceThreads / 32;
   int64_t n = (rows + warps - 1) / warps;
-  const int64_t cap = (int64_t)sm_count * 8;
+  const int64_t cap = (int64_t)sm_count * kReduceCtasPerSm;
   if (n > cap) n = cap;
   if (n < 1) n = 1;
   return (int)n;
