@@ -228,7 +228,7 @@ void PSSetBatchShape(int warps, int rows, int ns7, int nsp, int nsc);
  * Set-up: the first call on a device (and the first after the device's
  * context was destroyed, e.g. by cudaDeviceReset) looks up the array's
  * device address with cudaGetSymbolAddress, which loads the module into the
- * current context; make that call before any stream capture.  Set-up from
+ * current context and may synchronise with the device.  Set-up from
  * several host threads at once is serialised by a lock; after it, calls
  * take no lock.
  * Returns PS_OK or an error code (also recorded for PSGetLastError). */
