@@ -555,26 +555,43 @@ def diffusion64_measure(ps, reps=20):
     hin, hout = L.PSHostAlloc(nbytes), L.PSHostAlloc(nbytes)
     ctypes.memmove(hin, init.ctypes.data, nbytes)
     total = np.zeros(1, np.float32)
-    dev_ms, job_s = [], []
-    for r in range(reps + 3):
+
+    def timed_jobs():
+        dev_ms, job_s = [], []
+        for r in range(reps + 3):
+            L.PSGridCopyin(g1.handle, hin)
+            ps.synchronize()
+            L.PSEventRecord(0)
+            ps.stencil_run([m1, m2], steps // 2)
+            L.PSEventRecord(1)
+            ps.synchronize()
+            t0 = time.perf_counter()
+            L.PSGridCopyin(g1.handle, hin)
+            ps.stencil_run([m1, m2], steps // 2)
+            L.PSReduceGridV(total.ctypes.data_as(ctypes.c_void_p), ps.PS_SUM, g1.handle)
+            L.PSGridCopyout(g1.handle, hout)
+            el = time.perf_counter() - t0
+            if r >= 3:
+                dev_ms.append(L.PSEventElapsedMs(0, 1))
+                job_s.append(el)
+        ps.check()
+        out = np.empty_like(init)
+        ctypes.memmove(out.ctypes.data, hout, nbytes)
+        return float(np.median(dev_ms)), float(min(job_s)), out, float(total[0])
+
+    dms, js, got, tsum = timed_jobs()
+    # The same jobs with the library's autotuner on (PSSetAutotune): its trials
+    # (launch shapes and bit-identical temporal depths) run in untimed jobs,
+    # then the tuned plan is timed the same way.
+    ps.set_autotune(True)
+    for _ in range(3):
         L.PSGridCopyin(g1.handle, hin)
-        ps.synchronize()
-        L.PSEventRecord(0)
         ps.stencil_run([m1, m2], steps // 2)
-        L.PSEventRecord(1)
-        ps.synchronize()
-        t0 = time.perf_counter()
-        L.PSGridCopyin(g1.handle, hin)
-        ps.stencil_run([m1, m2], steps // 2)
-        L.PSReduceGridV(total.ctypes.data_as(ctypes.c_void_p), ps.PS_SUM, g1.handle)
-        L.PSGridCopyout(g1.handle, hout)
-        el = time.perf_counter() - t0
-        if r >= 3:
-            dev_ms.append(L.PSEventElapsedMs(0, 1))
-            job_s.append(el)
-    ps.check()
-    got = np.empty_like(init)
-    ctypes.memmove(got.ctypes.data, hout, nbytes)
+    ps.synchronize()
+    tuned, shape_t, k_t, tshape_t = ps.stencil_plan(m1)
+    dms_t, js_t, got_t, tsum_t = timed_jobs()
+    ps.set_autotune(False)
+    total[0] = tsum
     L.PSHostFree(hin)
     L.PSHostFree(hout)
     g1.free()
@@ -587,8 +604,6 @@ def diffusion64_measure(ps, reps=20):
     cpu_s = time.perf_counter() - t0
     exact = pyoracle.reduce_fp64(r1, pyoracle.PS_SUM)
     cells = float(n) ** 3
-    dms = float(np.median(dev_ms))
-    js = float(min(job_s))
     return {
         "workload": "7-point fp32 diffusion 64^3, seed 0, 100 steps + PSReduce sum "
                     "(the reference REF program's configuration)",
@@ -600,6 +615,16 @@ def diffusion64_measure(ps, reps=20):
                 "what": "PSGridCopyin(pinned) + PSStencilRun(50 x 2 maps) + PSReduce + "
                         "PSGridCopyout(pinned), wall clock, best of reps"},
         "bit_exact_vs_oracle": bool(np.array_equal(got.view(np.uint32), r1.view(np.uint32))),
+        "autotuned": {
+            "value": cells * steps / (dms_t / 1e3) / 1e9, "unit": "GLUPS",
+            "us_per_step": dms_t / steps * 1e3,
+            "e2e": {"value": cells * steps / js_t / 1e9, "unit": "GLUPS", "job_us": js_t * 1e6},
+            "plan": {"tuned": tuned, "temporal_k": k_t, "launch_shape": list(shape_t),
+                     "temporal_shape": list(tshape_t)},
+            "bit_exact_vs_oracle": bool(np.array_equal(got_t.view(np.uint32),
+                                                       r1.view(np.uint32))),
+            "sum_rel_err": abs(tsum_t - exact) / abs(exact),
+            "what": "the same jobs after PSSetAutotune(1) tuned the run in untimed jobs"},
         "reduce": {"value": float(total[0]), "fp64_oracle": exact,
                    "rel_err": abs(float(total[0]) - exact) / abs(exact),
                    "ref_fold": float(ref_sum)},
